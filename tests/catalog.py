@@ -1,0 +1,217 @@
+"""The expression catalog of tests/cpp/catalog_cases.inc, restated for the oracle.
+
+run_catalog(domain) evaluates every case with the CPU restatement and returns records in the
+same form as nebo_io.read_records, so they can be compared with the golden vectors that the
+reference produced and with the GPU results of tests/cpp/catalog_gpu.cu.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import nebo_io
+import oracle_dsl as O
+from oracle_dsl import cond
+
+DOMAINS = [
+    dict(n=(7, 6, 5), ghost=1, bc=(0, 0, 0), L=(9.1, 5.4, 5.5)),
+    dict(n=(6, 5, 4), ghost=1, bc=(1, 1, 1), L=(6.0, 6.5, 3.2)),
+    dict(n=(6, 6, 6), ghost=2, bc=(0, 0, 0), L=(6.0, 7.2, 4.8)),
+]
+
+
+class Ctx:
+    def __init__(self, domain):
+        d = DOMAINS[domain]
+        self.domain, self.n, self.ghost, self.bc = domain, d["n"], d["ghost"], d["bc"]
+        self.db = O.OpDB(self.n, d["L"])
+        self.inputs = {}
+        self.records = {}
+
+    def glob(self, loc):
+        return O.glob_dims(loc, self.n, self.ghost, self.bc)
+
+    def make(self, loc, values):
+        g = self.glob(loc)
+        return O.Field(loc, values.reshape(g[2], g[1], g[0]).copy(), self.ghost, self.bc)
+
+    def inp(self, loc, k):
+        key = (loc, k)
+        if key not in self.inputs:
+            g = self.glob(loc)
+            v = nebo_io.uniform_pm1(nebo_io.field_stream(nebo_io.TYPE_CODES[loc], k, self.domain), g[0] * g[1] * g[2])
+            self.inputs[key] = self.make(loc, v)
+        return self.inputs[key]
+
+    def fresh(self, loc):
+        g = self.glob(loc)
+        return self.make(loc, np.full(g[0] * g[1] * g[2], nebo_io.SENTINEL))
+
+    def mask_points(self, k):
+        return nebo_io.mask_points(k, self.domain, self.n, self.ghost)
+
+    def mask(self, loc, k):
+        return O.Mask.from_points(loc, self.mask_points(k), self.glob(loc), self.ghost, self.bc)
+
+    def rec(self, name, f):
+        self.records[name] = ("field", nebo_io.TYPE_CODES[f.loc], f.data)
+
+    def val(self, name, v):
+        self.records[name] = ("value", v)
+
+    def case(self, name, fn):
+        try:
+            fn()
+        except O.NeboError as e:
+            self.records[name] = ("error", str(e))
+
+
+def run_catalog(domain):
+    C = Ctx(domain)
+    db = C.db
+    a, b, c = C.inp("SVol", 0), C.inp("SVol", 1), C.inp("SVol", 2)
+    xa, xb, xc = C.inp("XVol", 0), C.inp("XVol", 1), C.inp("XVol", 2)
+
+    def simple(name, loc, expr_fn, use_ghost=True):
+        def body():
+            out = C.fresh(loc)
+            O.assign(out, expr_fn(), use_ghost)
+            C.rec(name, out)
+        C.case(name, body)
+
+    # pointwise
+    simple("s_copy", "SVol", lambda: a)
+    simple("s_scalar", "SVol", lambda: O.Scalar(3.25))
+    simple("s_add", "SVol", lambda: a + b)
+    simple("s_sub", "SVol", lambda: a - b)
+    simple("s_mul", "SVol", lambda: a * b)
+    simple("s_div", "SVol", lambda: a / (b + 3.0))
+    simple("s_scalar_mix", "SVol", lambda: 2.5 * a - b / 4.0 + 1.0 - (0.5 - c) * 3.0)
+    simple("s_neg", "SVol", lambda: -a + -(b * c))
+    simple("s_sin", "SVol", lambda: O.sin(a))
+    simple("s_cos", "SVol", lambda: O.cos(a))
+    simple("s_tan", "SVol", lambda: O.tan(a))
+    simple("s_exp", "SVol", lambda: O.exp(a))
+    simple("s_tanh", "SVol", lambda: O.tanh(a * 2.0))
+    simple("s_abs", "SVol", lambda: O.abs_(a))
+    simple("s_sqrt", "SVol", lambda: O.sqrt(O.abs_(a)))
+    simple("s_log", "SVol", lambda: O.log(a * a + 0.5))
+    simple("s_log10", "SVol", lambda: O.log10(O.abs_(b) + 0.25))
+    simple("s_pow", "SVol", lambda: O.pow_(O.abs_(a) + 0.1, b))
+    simple("s_powint", "SVol", lambda: O.pow_(a, 3))
+    simple("s_square", "SVol", lambda: O.square(a) + O.cube(b))
+    simple("s_maxmin", "SVol", lambda: O.max_(a, b) - O.min_(c, 0.25))
+
+    # cond
+    simple("s_cond_cmp", "SVol", lambda: cond(a > b, a, a < -0.5, b, c))
+    simple("s_cond_logic", "SVol", lambda: cond((a > 0.0) & (b > 0.0), 1.0,
+                                                (a <= 0.0) | ~(b < 0.5), 2.0,
+                                                (a == a) & (b != c), 3.0, 4.0))
+    simple("s_cond_ge", "SVol", lambda: cond(a >= 0.25, a * 2.0, b))
+
+    # masks
+    simple("s_cond_mask", "SVol", lambda: cond(C.mask("SVol", 0), a, C.mask("SVol", 1), 7.0, b))
+    simple("s_cond_mask_logic", "SVol",
+           lambda: cond(C.mask("SVol", 0) | C.mask("SVol", 1), 1.0,
+                        ~C.mask("SVol", 0) & (a > 0.0), 2.0, 3.0))
+
+    def masked():
+        out = C.fresh("SVol")
+        O.masked_assign(C.mask_points(0), out, a * b)
+        C.rec("s_masked_assign", out)
+    C.case("s_masked_assign", masked)
+    simple("s_interior", "SVol", lambda: a + 2.0 * b, use_ghost=False)
+
+    # SVol basic operator types
+    fx, fy, fz = O.FACES["SVol"]
+    simple("s_interpc2fx", fx, lambda: db.interp("SVol", fx)(a))
+    simple("s_interpc2fy", fy, lambda: db.interp("SVol", fy)(a))
+    simple("s_interpc2fz", fz, lambda: db.interp("SVol", fz)(a))
+    simple("s_gradx", fx, lambda: db.grad("SVol", fx)(a))
+    simple("s_grady", fy, lambda: db.grad("SVol", fy)(a))
+    simple("s_gradz", fz, lambda: db.grad("SVol", fz)(a))
+    simple("s_divx", "SVol", lambda: db.div(fx, "SVol")(C.inp(fx, 0)))
+    simple("s_divy", "SVol", lambda: db.div(fy, "SVol")(C.inp(fy, 0)))
+    simple("s_divz", "SVol", lambda: db.div(fz, "SVol")(C.inp(fz, 0)))
+    simple("s_interpf2cx", "SVol", lambda: db.interp(fx, "SVol")(C.inp(fx, 1)))
+    simple("s_interpf2cy", "SVol", lambda: db.interp(fy, "SVol")(C.inp(fy, 1)))
+    simple("s_interpf2cz", "SVol", lambda: db.interp(fz, "SVol")(C.inp(fz, 1)))
+
+    # staggered volume <-> scalar volume
+    simple("s2x_interp", "XVol", lambda: db.interp("SVol", "XVol")(a))
+    simple("s2y_grad", "YVol", lambda: db.grad("SVol", "YVol")(a))
+    simple("s2z_interp", "ZVol", lambda: db.interp("SVol", "ZVol")(b))
+    simple("x2s_grad", "SVol", lambda: db.grad("XVol", "SVol")(xa))
+    simple("y2s_interp", "SVol", lambda: db.interp("YVol", "SVol")(C.inp("YVol", 0)))
+    simple("z2s_grad", "SVol", lambda: db.grad("ZVol", "SVol")(C.inp("ZVol", 0)))
+
+    # XVol basic operator types
+    xfx, xfy, xfz = O.FACES["XVol"]
+    simple("x_gradx", xfx, lambda: db.grad("XVol", xfx)(xa))
+    simple("x_interpc2fy", xfy, lambda: db.interp("XVol", xfy)(xa))
+    simple("x_divz", "XVol", lambda: db.div(xfz, "XVol")(C.inp(xfz, 0)))
+
+    # 4-point interpolants
+    simple("s2xsurfy_interp4", "XSurfY", lambda: db.interp("SVol", "XSurfY")(a))
+    simple("s2zsurfx_interp4", "ZSurfX", lambda: db.interp("SVol", "ZSurfX")(b))
+    simple("x2y_interp4", "YVol", lambda: db.interp("XVol", "YVol")(xa))
+    simple("x2z_interp4", "ZVol", lambda: db.interp("XVol", "ZVol")(xb))
+
+    # null interpolants
+    simple("x2ssurfx_null", "SSurfX", lambda: db.interp("XVol", "SSurfX")(xa))
+    simple("s_null", "SVol", lambda: db.interp("SVol", "SVol")(a))
+
+    # finite-difference stencils
+    simple("s_fd_gradx", "SVol", lambda: db.fd("grad", 0)(a))
+    simple("s_fd_grady", "SVol", lambda: db.fd("grad", 1)(a))
+    simple("s_fd_interpz", "SVol", lambda: db.fd("interp", 2)(a))
+    simple("x_fd_gradz", "XVol", lambda: db.fd("grad", 2)(xa))
+
+    # box filter
+    simple("s_filter", "SVol", lambda: db.filter()(a))
+    simple("x_filter", "XVol", lambda: db.filter()(xa))
+
+    # chains
+    is2x, gx2s, box = db.interp("SVol", "XVol"), db.grad("XVol", "SVol"), db.filter()
+    simple("chain_igi", "XVol", lambda: is2x(gx2s(is2x(a))))
+
+    def deep():
+        m = C.mask("XVol", 0)
+        out = C.fresh("XVol")
+        O.assign(out, O.Scalar(0.0))
+        O.assign(out, cond(m, 0.0, is2x(gx2s(is2x(a))) * O.exp(xb) + O.sin(xc)))
+        f = C.fresh("XVol")
+        O.assign(f, box(out))
+        C.rec("chain_deep_out", out)
+        C.rec("chain_deep_filt", f)
+        C.val("chain_deep_sum", O.reduce("sum", f))
+        C.val("chain_deep_max", O.reduce("max", f))
+        C.val("chain_deep_norm", O.reduce("norm", f))
+    C.case("chain_deep", deep)
+
+    def heat_rhs():
+        ix, iy, iz = (db.interp("SVol", f) for f in (fx, fy, fz))
+        gx, gy, gz = (db.grad("SVol", f) for f in (fx, fy, fz))
+        dx, dy, dz = (db.div(f, "SVol") for f in (fx, fy, fz))
+        return a + 0.05 * (dx(ix(b) * gx(a)) + dy(iy(b) * gy(a)) + dz(iz(b) * gz(a)))
+    simple("chain_heat_rhs", "SVol", heat_rhs)
+    simple("chain_filter_cond", "SVol", lambda: db.filter()(cond(a > 0.0, a, b * 0.5)))
+
+    # reductions
+    def red_field():
+        for op in ("sum", "max", "min", "norm"):
+            C.val("red_" + op, O.reduce(op, a))
+        for op in ("sum", "max", "min", "norm"):
+            C.val(f"red_{op}_interior", O.reduce(op, a, interior=True))
+    C.case("red_field", red_field)
+
+    def red_expr():
+        C.val("red_expr_sum", O.reduce("sum", a * b + c))
+        C.val("red_expr_max", O.reduce("max", O.sin(a) - b))
+        C.val("red_expr_norm_interior", O.reduce("norm", a - b, interior=True))
+    C.case("red_expr", red_expr)
+
+    def red_x():
+        C.val("red_x_sum", O.reduce("sum", xa))
+        C.val("red_x_max_interior", O.reduce("max", xb, interior=True))
+    C.case("red_xvol", red_x)
+    return C.records
