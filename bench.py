@@ -1,0 +1,421 @@
+"""Benchmark of the GB300-native Nebo evaluator (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload W]
+
+Default workload (the headline): the deep fused FP64 expression at 256^3 interior + 1 ghost
+layer -- out <<= cond(mask,0)(Interp(Grad(Interp(a)))*exp(b)+sin(c)), f <<= BoxFilter(out),
+then nebo_sum/max/norm(f) -- on seeded synthetic inputs (a, b, c ~ U(-1,1), mask = 5% of
+cells + every boundary cell).  A step is one pass of that chain; the metric is cell-updates
+per second (interior cells x steps / time).  Other workloads (--workload heat, heat32) time the
+fused heat-equation step.
+
+value    device time of K steps, inputs resident in HBM, CUDA events on the launching stream.
+         Every input is larger than L2 (129 MB), so no flush is needed between steps.
+e2e      the same steps through the C ABI with host buffers: each step copies its inputs from
+         pinned host memory and reads the reductions back.
+roofline the dominant kernel's algorithmic bytes per launch / its mean event-timed duration.
+cpu_baseline  the oracle (CPU restatement of the reference's serial walk) on a bounded sample.
+
+--impl reference times the reference's CPU path (the oracle port with every host thread;
+the reference tree itself does not exist on the GPU host) on the same metric.
+Multi-GPU: the path does not shard across GPUs here (replicas only): each rank runs the full
+workload on its own GPU and value sums the ranks' cell-updates over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import __graft_entry__ as graft  # noqa: E402
+
+N_DEFAULT = 256
+BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
+    "deep": 8 * 3 + 8 + 1.0 / 8.0,   # a, b, c read, out written, 1 mask bit
+    "heat": 8 * 3,                   # T, lambda read, T' written
+    "heat32": 4 * 3,
+}
+DOMINANT = {"deep": "deep_chain", "heat": "heat_step_f64", "heat32": "heat_step_f32"}
+
+
+def measured_peak_hbm():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary (profiles/traffic.txt), or None."""
+    p = os.path.join(REPO, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and parts[1] == workload:
+            return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.rows = []
+        self.proc = None
+        self.bus_id = bus_id
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.bus_id:
+            cmd += ["-i", self.bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- workloads
+class Deep:
+    name = "deep"
+
+    def __init__(self, N, n):
+        import torch
+
+        from spatialops_gb300 import workloads as W
+
+        self.N, self.n = N, n
+        a, b, c, pts = W.deep_inputs((n, n, n))
+        self.host = [torch.from_numpy(x).pin_memory() for x in (a, b, c)]
+        words = W.mask_bits_from_points(pts, (n, n, n))
+        self.host_mask = torch.from_numpy(words.view(np.int32)).pin_memory()
+        self.A = N.Field("SVol", n, 1)
+        self.B = N.Field("XVol", n, 1)
+        self.C = N.Field("XVol", n, 1)
+        for f, h in zip((self.A, self.B, self.C), self.host):
+            f.tensor.copy_(h)
+        self.words = self.host_mask.to("cuda")
+        self.out = N.Field("XVol", n, 1)
+        self.filt = N.Field("XVol", n, 1)
+        self.red = torch.zeros(3, dtype=torch.float64, device="cuda")
+        self.cells = n ** 3
+        self.launches_per_step = 2 + 3 * 2
+        self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
+        self.d2h_bytes = 3 * 8
+        self.host_red = torch.zeros(3, dtype=torch.float64).pin_memory()
+
+    def step(self):
+        N = self.N
+        N.deep_chain(self.A, self.B, self.C, self.words, self.out, self.filt)
+        N.reduce_async(self.filt, "sum", False, self.red[0:1])
+        N.reduce_async(self.filt, "max", False, self.red[1:2])
+        N.reduce_async(self.filt, "norm", False, self.red[2:3])
+
+    def step_e2e(self):
+        for f, h in zip((self.A, self.B, self.C), self.host):
+            f.tensor.copy_(h, non_blocking=True)
+        self.words.copy_(self.host_mask, non_blocking=True)
+        self.step()
+        self.host_red.copy_(self.red, non_blocking=True)
+
+
+class Heat:
+    def __init__(self, N, n, dtype):
+        import torch
+
+        from spatialops_gb300 import workloads as W
+
+        self.name = "heat" if dtype == "f64" else "heat32"
+        self.N, self.n = N, n
+        lam, T0, dt = W.heat_inputs((n, n, n))
+        self.dt = dt
+        tdt = torch.float64 if dtype == "f64" else torch.float32
+        self.host = [torch.from_numpy(x).to(tdt).pin_memory() for x in (T0, lam)]
+        self.T = N.Field("SVol", n, 1, dtype=dtype)
+        self.Tt = N.Field("SVol", n, 1, dtype=dtype)
+        self.L = N.Field("SVol", n, 1, dtype=dtype)
+        self.T.tensor.copy_(self.host[0])
+        self.L.tensor.copy_(self.host[1])
+        N.fill_periodic(self.T)
+        N.fill_periodic(self.L)
+        self.cells = n ** 3
+        self.launches_per_step = 1
+        self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host)
+        self.d2h_bytes = 8
+        self.red = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.host_red = torch.zeros(1, dtype=torch.float64).pin_memory()
+        self.k = 0
+
+    def step(self):
+        a, b = (self.T, self.Tt) if self.k % 2 == 0 else (self.Tt, self.T)
+        self.N.heat_step(a, b, self.L, self.dt)
+        self.k += 1
+
+    def step_e2e(self):
+        self.T.tensor.copy_(self.host[0], non_blocking=True)
+        self.L.tensor.copy_(self.host[1], non_blocking=True)
+        self.k = 0
+        self.step()
+        self.N.reduce_async(self.Tt, "sum", False, self.red)
+        self.host_red.copy_(self.red, non_blocking=True)
+
+
+def make_workload(N, name, n):
+    if name == "deep":
+        return Deep(N, n)
+    if name == "heat":
+        return Heat(N, n, "f64")
+    if name == "heat32":
+        return Heat(N, n, "f32")
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def _oracle():
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_dsl as O  # the checker / CPU restatement of the reference's serial walk
+
+    return O
+
+
+def cpu_run(workload, n_xy, nz, threads):
+    """One step of the workload on the CPU oracle over an n_xy x n_xy x nz block; returns seconds."""
+    O = _oracle()
+    from spatialops_gb300 import workloads as W
+
+    shape = (n_xy, n_xy, nz)
+    if workload == "deep":
+        a, b, c, pts = W.deep_inputs(shape)
+        bits = W.mask_bits_from_points(pts, shape)
+        t0 = time.perf_counter()
+        O.deep_run(a, b, c, bits, shape, 1.0, threads)
+        return time.perf_counter() - t0
+    lam, T0, dt = W.heat_inputs(shape)
+    t0 = time.perf_counter()
+    O.heat_run(lam, T0, shape, 1, dt, threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(workload, n, budget_s=10.0):
+    """Serial oracle (1 core) on the full workload, repeated until ~budget_s of CPU work."""
+    reps, total = 0, 0.0
+    while total < budget_s and reps < 20:
+        total += cpu_run("deep" if workload == "deep" else "heat", n, n, 1)
+        reps += 1
+    cells = reps * n ** 3
+    return {"value": cells / total / 1e9, "unit": "Gcell-upd/s", "cores": 1, "kind": "port",
+            "sample": f"{reps} full {n}^3 step(s) of the {workload} workload, serial oracle walk, {total:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    graft._import_pkg()
+    threads = os.cpu_count() or 1
+    n = args.n
+    nz = 16
+    workload = args.workload if args.workload in ("deep", "heat") else "heat"
+    for _ in range(max(args.warmup, 0)):
+        cpu_run(workload, n, nz, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        t += cpu_run(workload, n, nz, threads)
+    cells = args.steps * n * n * nz
+    value = cells / t / 1e9
+    line = {
+        "impl": "reference", "metric": f"{workload} cell-updates/s", "value": value, "unit": "Gcell-upd/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if workload != "heat32" else "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{workload} {n}^3", "sample": f"{n}x{n}x{nz} slab per step"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-upd/s", "cores": threads, "kind": "port",
+                         "sample": f"{n}x{n}x{nz} slab of the {n}^3 {workload} workload per step, "
+                                   f"oracle restatement of the reference's serial walk, z-slabs over {threads} threads"},
+        "e2e": {"value": value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="deep", choices=["deep", "heat", "heat32"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    graft.build() if not os.path.exists(os.path.join(REPO, "spatialops-threadfix_gb300", "_build",
+                                                     "libnebo_gb300.so")) else None
+    N = graft._import_pkg()
+    W = make_workload(N, args.workload, args.n)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        W.step()
+    barrier()
+
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id
+    except Exception:
+        bus = None
+    sampler = ClockSampler(bus if isinstance(bus, str) else None)
+    sampler.start()
+    time.sleep(0.3)
+    N.profile_enable(True)
+    N.profile_report(reset=True)
+    launches0 = N.kernel_launch_count()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        W.step()
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = N.kernel_launch_count() - launches0
+    prof = N.profile_report(reset=True)
+    N.profile_enable(False)
+    clocks = sampler.stop()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * W.cells * args.steps / (ms * 1e-3) / 1e9
+
+    # e2e: host buffers, copies inside the timed region
+    e_steps = max(3, min(args.steps, 50))
+    for _ in range(2):
+        W.step_e2e()
+    barrier()
+    e0.record(stream)
+    for _ in range(e_steps):
+        W.step_e2e()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * W.cells * e_steps / (e2e_ms * 1e-3) / 1e9
+
+    dom = DOMINANT[W.name]
+    peak, peak_kind = measured_peak_hbm()
+    roof = None
+    if dom in prof and prof[dom]["launches"]:
+        kms = prof[dom]["ms"] / prof[dom]["launches"]
+        alg = BYTES_PER_CELL[W.name] * W.cells
+        achieved = alg / (kms * 1e-3) / 1e9
+        traffic = ncu_traffic(dom, f"{W.name}{args.n}")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dom, "kernel_ms": kms, "alg_bytes_per_launch": alg,
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else
+                "fallback 6.8 TB/s",
+                "kernels": {k: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1)}
+                            for k, v in prof.items()}}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(W.name, args.n)
+    line = {
+        "metric": f"{W.name} cell-updates/s", "value": value, "unit": "Gcell-upd/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if W.name == "heat32" else "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"{W.name} {args.n}^3 + 1 ghost", "cells_per_step": W.cells,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (129 MB); no flush between steps"},
+        "e2e": {"value": e2e_value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": W.h2d_bytes,
+                "d2h_bytes_per_step": W.d2h_bytes, "steps": e_steps},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,154 @@
+/*
+ * nebo_gb300.h -- C ABI of the GB300-native (sm_103a) Nebo field-expression evaluator.
+ *
+ * Everything here is plain C: device pointers, sizes, POD descriptors and an int status.
+ * No exception crosses this boundary; the C++ drop-in headers (include/spatialops/...) turn a
+ * non-zero status into std::runtime_error("Nebo error in ..."), as the reference does
+ * (spatialops/NeboLhs.h:107-152, spatialops/NeboBasic.h:65-93).
+ *
+ * One process drives one GPU.  Every launching entry point takes the cudaStream_t on which it
+ * enqueues its work (the reference's per-field stream, spatialops/structured/FieldInfo.h:264)
+ * and returns without synchronising unless it says otherwise.  A null stream means the
+ * per-thread default stream.
+ *
+ * Layout contract (spatialops/structured/MemoryWindow.h:63-321): a field is one allocation of
+ * glob[0]*glob[1]*glob[2] elements, x fastest; interior-relative index (x,y,z) lives at
+ *   (offset[0]+ghost_minus[0]+x) + glob[0]*((offset[1]+ghost_minus[1]+y) + glob[1]*(...z))
+ * with glob = n + ghost_minus + ghost_plus (+ one BC cell on + faces that have a boundary and
+ * whose location carries BCExtra), or 1 on an axis of extent 1.
+ */
+#ifndef NEBO_GB300_H
+#define NEBO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* nebo_stream_t; /* == cudaStream_t */
+
+/* ------------------------------------------------------------------ status */
+enum nebo_status_code {
+  NEBO_OK = 0,
+  NEBO_ERR_INVALID = 1,   /* bad descriptor, size, pointer or argument */
+  NEBO_ERR_GHOST = 2,     /* not enough valid ghost / BC cells (NeboBasic.h:65-93) */
+  NEBO_ERR_ALLOC = 3,     /* device allocation failed */
+  NEBO_ERR_LAUNCH = 4,    /* kernel launch or CUDA runtime error */
+  NEBO_ERR_TIMEOUT = 5,   /* a bounded device-side wait gave up */
+  NEBO_ERR_UNSUPPORTED = 6,
+  NEBO_ERR_NO_DEVICE = 7
+};
+
+enum nebo_dtype { NEBO_F64 = 0, NEBO_F32 = 1 };
+
+enum nebo_reduction { NEBO_RED_SUM = 0, NEBO_RED_MAX = 1, NEBO_RED_MIN = 2, NEBO_RED_NORM = 3 };
+
+/* Field descriptor: SpatialField's window/ghost/BC state (SpatialField.h:128-603). */
+typedef struct nebo_field {
+  void* data;              /* device pointer to glob element (0,0,0) */
+  int32_t glob[3];         /* MemoryWindow::glob_dim */
+  int32_t offset[3];       /* MemoryWindow::offset */
+  int32_t extent[3];       /* MemoryWindow::extent (window incl. ghosts) */
+  int32_t ghost_minus[3];  /* valid ghost cells on - faces */
+  int32_t ghost_plus[3];   /* valid ghost cells on + faces */
+  int32_t has_bc[3];       /* BoundaryCellInfo::has_bc */
+  int32_t bc_extra[3];     /* BoundaryCellInfo::has_extra (0 or the location's BCExtra) */
+  int32_t dtype;           /* nebo_dtype */
+} nebo_field;
+
+/* Human-readable text of a status code; the last error message of the calling thread. */
+const char* nebo_status_string(int status);
+const char* nebo_last_error(void);
+
+/* ------------------------------------------------------------------ device and memory
+ * Replace FieldInfo's device bookkeeping and the Pool<T> / CUDADeviceInterface allocator
+ * (spatialops/structured/FieldInfo.h:92-415, MemoryPool.cpp:104-216,
+ *  CudaMemoryAllocator.cu:28-240, 390-578).  Allocation is stream ordered
+ * (cudaMallocAsync on the device's default memory pool). */
+int nebo_device_init(int device);
+int nebo_device_count(int* count);
+int nebo_alloc(size_t bytes, void** ptr, nebo_stream_t stream);
+int nebo_free(void* ptr, nebo_stream_t stream);
+int nebo_memcpy_h2d(void* dst, const void* src, size_t bytes, nebo_stream_t stream);
+int nebo_memcpy_d2h(void* dst, const void* src, size_t bytes, nebo_stream_t stream);
+int nebo_memcpy_d2d(void* dst, const void* src, size_t bytes, nebo_stream_t stream);
+int nebo_memset(void* dst, int byte, size_t bytes, nebo_stream_t stream);
+int nebo_stream_sync(nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ ghost bookkeeping (host)
+ * calculate_actual_ghost (spatialops/NeboBasic.h:61-100) and the write region of
+ * NeboField<Initial>::assign (spatialops/NeboLhs.h:67-98).  Integer host code, exact.
+ * rhs_minus/rhs_plus: ghosts_with_bc() of the right-hand side.  limits = {xlo,xhi,ylo,yhi,
+ * zlo,zhi} in interior-relative coordinates.  Returns NEBO_ERR_GHOST with the reference's
+ * message when a BC axis lacks valid extra cells. */
+int nebo_write_limits(const nebo_field* lhs, int use_ghost, const int32_t rhs_minus[3],
+                      const int32_t rhs_plus[3], int32_t limits[6]);
+
+/* ------------------------------------------------------------------ periodic ghost exchange
+ * Every ghost cell of f takes the value of its wrapped interior image (the in-HBM stand-in for
+ * a halo exchange on a single periodic patch).  f must have equal ghosts on both faces and no
+ * BC cells. */
+int nebo_fill_periodic(const nebo_field* f, nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ masks
+ * SpatialMask / BitField (spatialops/structured/SpatialMask.h:99-181, BitField.h:291-333):
+ * one bit per cell of the ghosted window, word = flat/32, bit = flat%32, x fastest.
+ * points: device int32 triples in interior-relative coordinates (ghost = -1).  words must be
+ * zeroed by the caller (nebo_memset) or hold an earlier mask to OR into. */
+int nebo_mask_from_points(uint32_t* words, const int32_t glob[3], const int32_t offset[3],
+                          const int32_t* points, int32_t npoints, nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ reductions
+ * nebo_sum / nebo_max / nebo_min / nebo_norm and their _interior forms
+ * (spatialops/NeboReductions.h:45-240) over one field: ghost-inclusive (valid ghosts) unless
+ * interior != 0.  Accumulation is FP64 for both dtypes; sums use compensated (Neumaier)
+ * partials.  nebo_reduce writes *result on the host and synchronises the stream (the reference
+ * returns the value synchronously); nebo_reduce_async leaves it in device memory. */
+int nebo_reduce(const nebo_field* f, int op, int interior, double* result, nebo_stream_t stream);
+int nebo_reduce_async(const nebo_field* f, int op, int interior, double* d_result,
+                      nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ fused heat equation
+ * One explicit Euler step of the reference's scalar heat RHS
+ *   Tout <<= T + dt*( DivX(InterpX(lam)*GradX(T)) + DivY(...) + DivZ(...) )
+ * (examples/heat_equation.cpp:216-220; operators of StencilBuilder.cpp:60-72 on SVolField)
+ * as ONE kernel on a single periodic patch: reads T's ghosts, writes Tout's interior and, in
+ * the same pass, Tout's ghost cells as periodic images (the next step's ghost fill).
+ * T, Tout, lam: SVol, one ghost layer, same shape and dtype.  spacing = {dx,dy,dz}.
+ * FP64: same operations and roundings as the reference's serial walk (bit-exact).
+ * FP32: FP32 storage and arithmetic. */
+int nebo_heat_step(const nebo_field* T, const nebo_field* Tout, const nebo_field* lam, double dt,
+                   const double spacing[3], nebo_stream_t stream);
+
+/* steps Euler steps, ping-ponging T and Ttmp; the result is left in T (ghosts filled).
+ * use_graph != 0 captures the step sequence in a CUDA graph once and replays it. */
+int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
+                  double dt, const double spacing[3], int use_graph, nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ deep fused chain
+ *   out <<= cond(mask, 0.0)( Interp_{S->X}(Grad_{X->S}(Interp_{S->X}(a))) * exp(b) + sin(c) )
+ *   filt <<= Filter_{X->X}(out)                       (27-point box, 1/27)
+ * a: SVol, b, c, out, filt: XVol, one ghost layer, no BC, FP64; mask: XVol bit words.
+ * Write regions follow calculate_actual_ghost: out is written on x in [1,n), y,z in [-1,n+1)
+ * (the chain's negative x ghost); filt on the interior.  Cells outside keep their contents.
+ * dx: the x spacing of the gradient (coefficients -1/dx, 1/dx). */
+int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* c,
+                    const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
+                    double dx, nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ launch accounting
+ * Every kernel launch of this library is counted; with profiling on, each launch (outside
+ * graph capture) is also bracketed by CUDA events on its stream.  nebo_profile_report
+ * synchronises those events and writes {"<kernel>": {"launches": n, "ms": total}, ...} as
+ * JSON into buf (reset != 0 clears the totals).  Plays the part of NEBO_REPORT_BACKEND and
+ * TimeLogger (spatialops/NeboLhs.h:321-392, util/TimeLogger.h:85-263). */
+unsigned long long nebo_kernel_launch_count(void);
+int nebo_profile_enable(int on);
+int nebo_profile_report(char* buf, size_t len, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEBO_GB300_H */

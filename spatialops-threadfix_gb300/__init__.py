@@ -1,7 +1,267 @@
 """GB300-native Nebo field-expression evaluation: Python host mirror of the C-ABI library.
 
 The product is libnebo_gb300.so (CUDA kernels for sm_103a behind the C ABI declared in
-include/nebo_gb300.h) plus the drop-in C++ headers under include/spatialops.  This package
-loads the library with ctypes for the tests and the benchmark; it has no compute path of its
-own and raises if the library is missing.
+include/nebo_gb300.h) plus the drop-in C++ headers under include/spatialops.  This module binds
+the C ABI with ctypes for tests and the benchmark.  It computes nothing itself: every call goes
+to the CUDA library, and loading fails loudly if the library has not been built.
+
+Names follow the reference's API (spatialops/NeboReductions.h, NeboStencilBuilder.h,
+structured/SpatialField.h); errors raise RuntimeError with the library's "Nebo error in ..."
+message, as the reference throws std::runtime_error.
 """
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libnebo_gb300.so")
+
+F64, F32 = 0, 1
+RED = {"sum": 0, "max": 1, "min": 2, "norm": 3}
+
+# location type -> (offset, BCExtra), spatialops/structured/FVStaggeredLocationTypes.h:63-126
+BCEXTRA = {
+    "SVol": (0, 0, 0), "SSurfX": (1, 0, 0), "SSurfY": (0, 1, 0), "SSurfZ": (0, 0, 1),
+    "XVol": (1, 0, 0), "XSurfX": (0, 0, 0), "XSurfY": (0, 1, 0), "XSurfZ": (0, 0, 1),
+    "YVol": (0, 1, 0), "YSurfX": (1, 0, 0), "YSurfY": (0, 0, 0), "YSurfZ": (0, 0, 1),
+    "ZVol": (0, 0, 1), "ZSurfX": (1, 0, 0), "ZSurfY": (0, 1, 0), "ZSurfZ": (0, 0, 0),
+}
+
+
+class NeboField(ctypes.Structure):
+    """struct nebo_field (include/nebo_gb300.h)."""
+
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("glob", ctypes.c_int32 * 3),
+        ("offset", ctypes.c_int32 * 3),
+        ("extent", ctypes.c_int32 * 3),
+        ("ghost_minus", ctypes.c_int32 * 3),
+        ("ghost_plus", ctypes.c_int32 * 3),
+        ("has_bc", ctypes.c_int32 * 3),
+        ("bc_extra", ctypes.c_int32 * 3),
+        ("dtype", ctypes.c_int32),
+    ]
+
+
+# (name, restype, argtypes) of every entry point declared in include/nebo_gb300.h
+_P = ctypes.c_void_p
+_FP = ctypes.POINTER(NeboField)
+_I = ctypes.c_int
+_D = ctypes.c_double
+_I3 = ctypes.POINTER(ctypes.c_int32)
+SIGNATURES = [
+    ("nebo_status_string", ctypes.c_char_p, [_I]),
+    ("nebo_last_error", ctypes.c_char_p, []),
+    ("nebo_device_init", _I, [_I]),
+    ("nebo_device_count", _I, [ctypes.POINTER(_I)]),
+    ("nebo_alloc", _I, [ctypes.c_size_t, ctypes.POINTER(_P), _P]),
+    ("nebo_free", _I, [_P, _P]),
+    ("nebo_memcpy_h2d", _I, [_P, _P, ctypes.c_size_t, _P]),
+    ("nebo_memcpy_d2h", _I, [_P, _P, ctypes.c_size_t, _P]),
+    ("nebo_memcpy_d2d", _I, [_P, _P, ctypes.c_size_t, _P]),
+    ("nebo_memset", _I, [_P, _I, ctypes.c_size_t, _P]),
+    ("nebo_stream_sync", _I, [_P]),
+    ("nebo_write_limits", _I, [_FP, _I, _I3, _I3, _I3]),
+    ("nebo_fill_periodic", _I, [_FP, _P]),
+    ("nebo_mask_from_points", _I, [_P, _I3, _I3, _P, ctypes.c_int32, _P]),
+    ("nebo_reduce", _I, [_FP, _I, _I, ctypes.POINTER(_D), _P]),
+    ("nebo_reduce_async", _I, [_FP, _I, _I, _P, _P]),
+    ("nebo_heat_step", _I, [_FP, _FP, _FP, _D, ctypes.POINTER(_D), _P]),
+    ("nebo_heat_run", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
+    ("nebo_deep_chain", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _P]),
+    ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
+    ("nebo_profile_enable", _I, [_I]),
+    ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
+]
+
+_lib = None
+
+
+def lib():
+    """Load libnebo_gb300.so (raises if it was not built: there is no fallback path)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"Nebo error: CUDA library not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        msg = lib().nebo_last_error().decode()
+        raise RuntimeError(msg or lib().nebo_status_string(rc).decode())
+
+
+def _i3(v):
+    return (ctypes.c_int32 * 3)(*[int(t) for t in v])
+
+
+def _stream(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def glob_dims(loc, n, ghost, bc=(0, 0, 0)):
+    ex = BCEXTRA[loc]
+    return tuple((n[i] + 2 * ghost + (ex[i] if bc[i] else 0)) if n[i] > 1 else 1 for i in range(3))
+
+
+class Field:
+    """A SpatialField-like handle: one device allocation (a torch tensor) + window/ghost/BC state.
+
+    tensor has numpy shape (gz, gy, gx); the window covers the whole allocation.
+    """
+
+    def __init__(self, loc, n, ghost=1, bc=(0, 0, 0), dtype="f64", tensor=None, device="cuda"):
+        import torch
+
+        self.loc = loc
+        self.n = tuple(int(v) for v in ((n,) * 3 if np.isscalar(n) else n))
+        self.ghost = int(ghost)
+        self.bc = tuple(int(b) for b in bc)
+        self.dtype = F64 if dtype in ("f64", "float64", torch.float64) else F32
+        g = glob_dims(loc, self.n, self.ghost, self.bc)
+        self.glob = g
+        tdt = torch.float64 if self.dtype == F64 else torch.float32
+        if tensor is None:
+            tensor = torch.zeros((g[2], g[1], g[0]), dtype=tdt, device=device)
+        if tuple(tensor.shape) != (g[2], g[1], g[0]) or tensor.dtype != tdt or not tensor.is_contiguous():
+            raise RuntimeError(f"Nebo error: tensor does not match the {loc} window {g[::-1]} ({tdt})")
+        self.tensor = tensor
+
+    @classmethod
+    def from_numpy(cls, loc, arr, ghost=1, bc=(0, 0, 0), dtype="f64"):
+        import torch
+
+        gz, gy, gx = arr.shape
+        ex = BCEXTRA[loc]
+        n = tuple((d - 2 * ghost - (ex[i] if bc[i] else 0)) for i, d in enumerate((gx, gy, gz)))
+        tdt = torch.float64 if dtype in ("f64", "float64") else torch.float32
+        t = torch.from_numpy(np.ascontiguousarray(arr)).to(dtype=tdt, device="cuda")
+        return cls(loc, n, ghost, bc, dtype, tensor=t)
+
+    def desc(self):
+        d = NeboField()
+        d.data = self.tensor.data_ptr()
+        d.glob[:] = self.glob
+        d.offset[:] = (0, 0, 0)
+        d.extent[:] = self.glob
+        gm = [0 if self.glob[i] == 1 else self.ghost for i in range(3)]
+        d.ghost_minus[:] = gm
+        d.ghost_plus[:] = gm
+        d.has_bc[:] = self.bc
+        d.bc_extra[:] = [BCEXTRA[self.loc][i] if self.bc[i] else 0 for i in range(3)]
+        d.dtype = self.dtype
+        return d
+
+    def numpy(self):
+        return self.tensor.detach().cpu().numpy()
+
+
+# ----------------------------------------------------------------------------- entry points
+def device_count():
+    n = ctypes.c_int(0)
+    rc = lib().nebo_device_count(ctypes.byref(n))
+    return n.value if rc == 0 else 0
+
+
+def write_limits(lhs: Field, rhs_minus, rhs_plus, use_ghost=True):
+    """calculate_actual_ghost + NeboField::assign limits, host code (no GPU needed)."""
+    lim = (ctypes.c_int32 * 6)()
+    d = lhs.desc() if isinstance(lhs, Field) else lhs
+    _check(lib().nebo_write_limits(ctypes.byref(d), int(use_ghost), _i3(rhs_minus), _i3(rhs_plus), lim))
+    return tuple(lim)
+
+
+def fill_periodic(f: Field, stream=None):
+    d = f.desc()
+    _check(lib().nebo_fill_periodic(ctypes.byref(d), _stream(stream)))
+
+
+def mask_words(glob):
+    import torch
+
+    nwords = (glob[0] * glob[1] * glob[2] + 31) // 32
+    return torch.zeros(nwords, dtype=torch.int32, device="cuda")
+
+
+def mask_from_points(words, glob, ghost, points, stream=None):
+    """OR the bits of `points` (int32 (N,3), interior-relative) into device mask words."""
+    import torch
+
+    pts = torch.as_tensor(np.ascontiguousarray(points, dtype=np.int32)).to("cuda")
+    _check(lib().nebo_mask_from_points(ctypes.c_void_p(words.data_ptr()), _i3(glob), _i3((ghost,) * 3),
+                                       ctypes.c_void_p(pts.data_ptr()), len(points), _stream(stream)))
+    return words
+
+
+def _reduce(f, op, interior, stream=None):
+    out = ctypes.c_double()
+    d = f.desc()
+    _check(lib().nebo_reduce(ctypes.byref(d), RED[op], int(interior), ctypes.byref(out), _stream(stream)))
+    return out.value
+
+
+def nebo_sum(f, stream=None): return _reduce(f, "sum", False, stream)
+def nebo_max(f, stream=None): return _reduce(f, "max", False, stream)
+def nebo_min(f, stream=None): return _reduce(f, "min", False, stream)
+def nebo_norm(f, stream=None): return _reduce(f, "norm", False, stream)
+def nebo_sum_interior(f, stream=None): return _reduce(f, "sum", True, stream)
+def nebo_max_interior(f, stream=None): return _reduce(f, "max", True, stream)
+def nebo_min_interior(f, stream=None): return _reduce(f, "min", True, stream)
+def nebo_norm_interior(f, stream=None): return _reduce(f, "norm", True, stream)
+
+
+def reduce_async(f, op, interior, d_result, stream=None):
+    d = f.desc()
+    _check(lib().nebo_reduce_async(ctypes.byref(d), RED[op], int(interior), ctypes.c_void_p(d_result.data_ptr()),
+                                   _stream(stream)))
+
+
+def heat_step(T, Tout, lam, dt, spacing=(1.0, 1.0, 1.0), stream=None):
+    a, b, c = T.desc(), Tout.desc(), lam.desc()
+    sp = (ctypes.c_double * 3)(*spacing)
+    _check(lib().nebo_heat_step(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), float(dt), sp, _stream(stream)))
+
+
+def heat_run(T, Ttmp, lam, steps, dt, spacing=(1.0, 1.0, 1.0), use_graph=True, stream=None):
+    a, b, c = T.desc(), Ttmp.desc(), lam.desc()
+    sp = (ctypes.c_double * 3)(*spacing)
+    _check(lib().nebo_heat_run(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt), sp,
+                               int(use_graph), _stream(stream)))
+
+
+def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None):
+    da, db, dc, do, df = a.desc(), b.desc(), c.desc(), out.desc(), filt.desc()
+    _check(lib().nebo_deep_chain(ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                 ctypes.c_void_p(words.data_ptr()), ctypes.byref(do), ctypes.byref(df), float(dx),
+                                 _stream(stream)))
+
+
+def kernel_launch_count():
+    return int(lib().nebo_kernel_launch_count())
+
+
+def profile_enable(on=True):
+    _check(lib().nebo_profile_enable(int(on)))
+
+
+def profile_report(reset=True):
+    """{kernel: {"launches": n, "ms": total}} for launches timed since the last reset."""
+    import json
+
+    buf = ctypes.create_string_buffer(1 << 16)
+    _check(lib().nebo_profile_report(buf, len(buf), int(reset)))
+    return json.loads(buf.value.decode())

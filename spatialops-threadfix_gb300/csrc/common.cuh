@@ -1,0 +1,92 @@
+// Shared helpers of the sm_103a Nebo library: status/error plumbing, descriptor checks and the
+// device-side view of a field (the reference's NeboField/NeboConstField GPUWalk indexing,
+// spatialops/NeboLhs.h:632-699 and spatialops/NeboRhs.h:294-327).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+#include "nebo_gb300.h"
+
+namespace nebo {
+
+// Record a message for nebo_last_error() and return the status.
+int fail(int status, const char* fmt, ...);
+// Map a CUDA error to NEBO_ERR_LAUNCH (or NEBO_OK) with context.
+int cuda_fail(cudaError_t e, const char* where);
+
+#define NEBO_CUDA_TRY(call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::nebo::cuda_fail(e_, #call); \
+  } while (0)
+
+#define NEBO_LAUNCH_CHECK(where)                              \
+  do {                                                        \
+    cudaError_t e_ = cudaGetLastError();                      \
+    if (e_ != cudaSuccess) return ::nebo::cuda_fail(e_, where); \
+  } while (0)
+
+inline size_t elem_size(int dtype) { return dtype == NEBO_F32 ? 4 : 8; }
+
+// Interior extents of a field: window extent minus valid ghosts (includes BC cells).
+inline void interior_extent(const nebo_field& f, int n[3]) {
+  for (int i = 0; i < 3; ++i) n[i] = f.extent[i] - f.ghost_minus[i] - f.ghost_plus[i];
+}
+
+// Structural checks every entry point applies to a descriptor.
+int check_field(const nebo_field* f, const char* what);
+// Same shape, ghosts and dtype.
+int check_same_layout(const nebo_field* a, const nebo_field* b, const char* what);
+// Uniform periodic patch: equal ghosts g on all six faces, no BC cells, window == allocation.
+int check_periodic_patch(const nebo_field* f, int g, const char* what);
+
+// Device view: interior-relative (x,y,z) -> element.
+template <typename T>
+struct View {
+  T* base;  // element (0,0,0) of the interior
+  int sy;   // glob[0]
+  long sz;  // glob[0]*glob[1]
+  __host__ __device__ long idx(int x, int y, int z) const { return (long)x + (long)sy * y + sz * z; }
+};
+
+template <typename T>
+inline View<T> make_view(const nebo_field& f) {
+  View<T> v;
+  v.sy = f.glob[0];
+  v.sz = (long)f.glob[0] * f.glob[1];
+  v.base = static_cast<T*>(f.data) + (long)(f.offset[0] + f.ghost_minus[0]) +
+           (long)v.sy * (f.offset[1] + f.ghost_minus[1]) + v.sz * (f.offset[2] + f.ghost_minus[2]);
+  return v;
+}
+
+// Counts one kernel launch and, while profiling is on, times it with events on its stream.
+// Construct immediately before the launch; the destructor records the end event.
+class LaunchScope {
+ public:
+  LaunchScope(const char* name, cudaStream_t s);
+  ~LaunchScope();
+  LaunchScope(const LaunchScope&) = delete;
+  LaunchScope& operator=(const LaunchScope&) = delete;
+
+ private:
+  const char* name_;
+  cudaStream_t s_;
+  void* a_;
+  void* b_;
+};
+
+inline int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+}  // namespace nebo

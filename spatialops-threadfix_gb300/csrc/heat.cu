@@ -1,0 +1,301 @@
+// Fused heat-equation step: Tout <<= T + dt*( DivX(InterpX(lam)*GradX(T)) + DivY(..) + DivZ(..) )
+// on a single periodic SVol patch with one ghost layer, as one sm_103a kernel.
+//
+// Reference: the expression of examples/heat_equation.cpp:216-220 with the operators of
+// spatialops/structured/stencil/StencilBuilder.cpp:60-72 (interp {1/2,1/2} at points (-1,0),
+// grad {-1/dx,1/dx} at (-1,0), div {-1/dx,1/dx} at (0,+1)), evaluated by the reference as the
+// nested tree of spatialops/NeboStencils.h:407-448 (each face flux recomputed per use).
+//
+// Design.  Blocks of 32x8 threads own a 32x8 column of cells and march a chunk of z planes.
+// Every face flux is computed once: each thread computes the flux of its low x-, y- and
+// z-face; high x/y faces come from the neighbour thread through shared memory (one warp of the
+// block computes the tile's +x and +y halo faces), and the high z-face is carried in a register
+// to the next plane.  The new value is written to the interior and, in the same pass, to its
+// periodic ghost images, so no separate ghost-fill kernel runs between steps.
+//
+// Arithmetic.  FP64 with unit spacing uses the scaled form F' = (la+lb)*(tb-ta) = 2*F and
+// T' = T + (dt/2)*(((Dx'+Dy')+Dz')); every scaling is by a power of two, so each rounding is the
+// one the reference's serial walk performs and the result is bit-identical.  FP64 with general
+// spacing evaluates the reference's own form (same operations, same order).  Both use _rn
+// intrinsics so no multiply-add is contracted.  FP32 (storage and arithmetic) uses the scaled
+// form with per-direction weights and lets the compiler fuse.
+#include <climits>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "common.cuh"
+
+namespace nebo {
+namespace {
+
+constexpr int BX = 32;
+constexpr int BY = 8;
+
+struct ExactD {
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+};
+struct FastF {
+  static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+  static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+};
+
+enum { MODE_UNIT = 0, MODE_REFERENCE = 1, MODE_WEIGHTED = 2 };
+
+template <typename T>
+struct HeatParams {
+  T dt;       // time step
+  T hdt;      // dt/2 (MODE_UNIT)
+  T c0[3];    // -1/d per axis (MODE_REFERENCE)
+  T c1[3];    // +1/d per axis
+  T w[3];     // dt/(2 d^2) per axis (MODE_WEIGHTED)
+};
+
+// Flux through the face between cell a (low side) and cell b (high side).
+template <typename T, class A, int MODE>
+__device__ __forceinline__ T face_flux(T la, T lb, T ta, T tb, T c0, T c1) {
+  if (MODE == MODE_REFERENCE) {
+    const T interp = A::add(A::mul(la, T(0.5)), A::mul(lb, T(0.5)));
+    const T grad = A::add(A::mul(ta, c0), A::mul(tb, c1));
+    return A::mul(interp, grad);
+  } else {
+    return A::mul(A::add(la, lb), A::sub(tb, ta));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_with_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny,
+                                                  int nz, T v) {
+  int xs[3], ys[3], zs[3];
+  int cx = 0, cy = 0, cz = 0;
+  xs[cx++] = x;
+  if (x == 0) xs[cx++] = nx;
+  if (x == nx - 1) xs[cx++] = -1;
+  ys[cy++] = y;
+  if (y == 0) ys[cy++] = ny;
+  if (y == ny - 1) ys[cy++] = -1;
+  zs[cz++] = z;
+  if (z == 0) zs[cz++] = nz;
+  if (z == nz - 1) zs[cz++] = -1;
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+}
+
+template <typename T, class A, int MODE>
+__global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__ tin, T* __restrict__ tout,
+                                                           const T* __restrict__ lam, int sy, long sz, int nx, int ny,
+                                                           int nz, int zchunk, HeatParams<T> p) {
+  __shared__ T sfx[2][BY][BX + 1];
+  __shared__ T sfy[2][BY + 1][BX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk;
+  const int z1 = min(z0 + zchunk, nz);
+  const bool active = x < nx && y < ny;
+  // inactive threads read the +ghost column/row, which exists, and write nothing
+  const int xc = min(x, nx), yc = min(y, ny);
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+
+  T tc = __ldg(tin + at(xc, yc, z0));
+  T lc = __ldg(lam + at(xc, yc, z0));
+  T fzlo = face_flux<T, A, MODE>(__ldg(lam + at(xc, yc, z0 - 1)), lc, __ldg(tin + at(xc, yc, z0 - 1)), tc, p.c0[2],
+                                 p.c1[2]);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = z & 1;
+    const T tn = __ldg(tin + at(xc, yc, z + 1));
+    const T ln = __ldg(lam + at(xc, yc, z + 1));
+    const T fzhi = face_flux<T, A, MODE>(lc, ln, tc, tn, p.c0[2], p.c1[2]);
+    const T fx = face_flux<T, A, MODE>(__ldg(lam + at(xc - 1, yc, z)), lc, __ldg(tin + at(xc - 1, yc, z)), tc, p.c0[0],
+                                       p.c1[0]);
+    const T fy = face_flux<T, A, MODE>(__ldg(lam + at(xc, yc - 1, z)), lc, __ldg(tin + at(xc, yc - 1, z)), tc, p.c0[1],
+                                       p.c1[1]);
+    sfx[buf][ty][tx] = fx;
+    sfy[buf][ty][tx] = fy;
+    if (ty == 0) {
+      // +y halo face of column x: between rows y0+BY-1 and y0+BY
+      const int yh = y0 + BY;
+      if (yh <= ny && x <= nx) {
+        sfy[buf][BY][tx] = face_flux<T, A, MODE>(__ldg(lam + at(xc, yh - 1, z)), __ldg(lam + at(xc, yh, z)),
+                                                 __ldg(tin + at(xc, yh - 1, z)), __ldg(tin + at(xc, yh, z)), p.c0[1],
+                                                 p.c1[1]);
+      }
+    } else if (ty == 1 && tx < BY) {
+      // +x halo face of row y0+tx: between columns x0+BX-1 and x0+BX
+      const int xh = x0 + BX, yr = y0 + tx;
+      if (xh <= nx && yr < ny) {
+        sfx[buf][tx][BX] = face_flux<T, A, MODE>(__ldg(lam + at(xh - 1, yr, z)), __ldg(lam + at(xh, yr, z)),
+                                                 __ldg(tin + at(xh - 1, yr, z)), __ldg(tin + at(xh, yr, z)), p.c0[0],
+                                                 p.c1[0]);
+      }
+    }
+    __syncthreads();
+    if (active) {
+      const T fxhi = sfx[buf][ty][tx + 1];
+      const T fyhi = sfy[buf][ty + 1][tx];
+      T v;
+      if (MODE == MODE_UNIT) {
+        const T s = A::add(A::add(A::sub(fxhi, fx), A::sub(fyhi, fy)), A::sub(fzhi, fzlo));
+        v = A::add(tc, A::mul(p.hdt, s));
+      } else if (MODE == MODE_REFERENCE) {
+        const T dx = A::add(A::mul(fx, p.c0[0]), A::mul(fxhi, p.c1[0]));
+        const T dy = A::add(A::mul(fy, p.c0[1]), A::mul(fyhi, p.c1[1]));
+        const T dz = A::add(A::mul(fzlo, p.c0[2]), A::mul(fzhi, p.c1[2]));
+        v = A::add(tc, A::mul(p.dt, A::add(A::add(dx, dy), dz)));
+      } else {
+        v = tc + p.w[0] * (fxhi - fx) + p.w[1] * (fyhi - fy) + p.w[2] * (fzhi - fzlo);
+      }
+      store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
+    }
+    tc = tn;
+    lc = ln;
+    fzlo = fzhi;
+  }
+}
+
+int check_heat(const nebo_field* T, const nebo_field* To, const nebo_field* L, const char* what) {
+  int rc;
+  if ((rc = check_field(T, what)) || (rc = check_field(To, what)) || (rc = check_field(L, what))) return rc;
+  if ((rc = check_same_layout(T, To, what)) || (rc = check_same_layout(T, L, what))) return rc;
+  if ((rc = check_periodic_patch(T, 1, what))) return rc;
+  if (T->data == To->data) return fail(NEBO_ERR_INVALID, "Nebo error in %s: in-place stencil update", what);
+  return NEBO_OK;
+}
+
+template <typename T>
+int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* Lf, double dt, const double sp[3],
+                cudaStream_t s) {
+  int n[3];
+  interior_extent(*Tf, n);
+  const View<T> vin = make_view<T>(*Tf), vout = make_view<T>(*Tof), vl = make_view<T>(*Lf);
+  HeatParams<T> p;
+  p.dt = (T)dt;
+  p.hdt = (T)(0.5 * dt);
+  for (int i = 0; i < 3; ++i) {
+    p.c0[i] = (T)(-1.0 / sp[i]);
+    p.c1[i] = (T)(1.0 / sp[i]);
+    p.w[i] = (T)(0.5 * dt / (sp[i] * sp[i]));
+  }
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  // z chunks: enough blocks for ~4 resident blocks per SM, each chunk at least 8 planes
+  const int target = num_sms() * 8;
+  int chunks = (target + gxb * gyb - 1) / (gxb * gyb);
+  chunks = max(1, min(chunks, (n[2] + 7) / 8));
+  const int zchunk = (n[2] + chunks - 1) / chunks;
+  chunks = (n[2] + zchunk - 1) / zchunk;
+  dim3 grid(gxb, gyb, chunks), block(BX, BY);
+  const bool unit = sp[0] == 1.0 && sp[1] == 1.0 && sp[2] == 1.0;
+  if constexpr (sizeof(T) == 8) {
+    LaunchScope ls("heat_step_f64", s);
+    if (unit)
+      heat_step_kernel<double, ExactD, MODE_UNIT><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz,
+                                                                         n[0], n[1], n[2], zchunk, p);
+    else
+      heat_step_kernel<double, ExactD, MODE_REFERENCE><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
+                                                                              vin.sz, n[0], n[1], n[2], zchunk, p);
+  } else {
+    LaunchScope ls("heat_step_f32", s);
+    heat_step_kernel<float, FastF, MODE_WEIGHTED><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz,
+                                                                         n[0], n[1], n[2], zchunk, p);
+  }
+  NEBO_LAUNCH_CHECK("nebo_heat_step");
+  return NEBO_OK;
+}
+
+int heat_step_any(const nebo_field* T, const nebo_field* To, const nebo_field* L, double dt, const double sp[3],
+                  cudaStream_t s) {
+  return T->dtype == NEBO_F64 ? launch_heat<double>(T, To, L, dt, sp, s) : launch_heat<float>(T, To, L, dt, sp, s);
+}
+
+// CUDA-graph cache for nebo_heat_run: one instantiated graph per argument set.
+struct GraphKey {
+  void *t, *t2, *l;
+  int glob[3], dtype, steps;
+  double dt, sp[3];
+  bool operator<(const GraphKey& o) const {
+    return std::tie(t, t2, l, glob[0], glob[1], glob[2], dtype, steps, dt, sp[0], sp[1], sp[2]) <
+           std::tie(o.t, o.t2, o.l, o.glob[0], o.glob[1], o.glob[2], o.dtype, o.steps, o.dt, o.sp[0], o.sp[1], o.sp[2]);
+  }
+};
+std::mutex g_graph_mu;
+std::map<GraphKey, cudaGraphExec_t> g_graphs;
+
+}  // namespace
+
+int fill_periodic_any(const nebo_field* f, cudaStream_t s);  // ghost.cu
+
+}  // namespace nebo
+
+using namespace nebo;
+
+extern "C" int nebo_heat_step(const nebo_field* T, const nebo_field* Tout, const nebo_field* lam, double dt,
+                              const double spacing[3], nebo_stream_t stream) {
+  const double unit[3] = {1.0, 1.0, 1.0};
+  int rc = check_heat(T, Tout, lam, "nebo_heat_step");
+  if (rc) return rc;
+  return heat_step_any(T, Tout, lam, dt, spacing ? spacing : unit, (cudaStream_t)stream);
+}
+
+extern "C" int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps, double dt,
+                             const double spacing[3], int use_graph, nebo_stream_t stream) {
+  const double unit[3] = {1.0, 1.0, 1.0};
+  const double* sp = spacing ? spacing : unit;
+  int rc = check_heat(T, Ttmp, lam, "nebo_heat_run");
+  if (rc) return rc;
+  if (steps < 0) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_heat_run: negative step count");
+  cudaStream_t s = (cudaStream_t)stream;
+  // T's ghosts must hold the periodic images before the first step
+  if ((rc = fill_periodic_any(T, s))) return rc;
+  if (steps == 0) return NEBO_OK;
+  const size_t bytes = (size_t)T->glob[0] * T->glob[1] * T->glob[2] * elem_size(T->dtype);
+  if (!use_graph) {
+    for (int k = 0; k < steps; ++k) {
+      const nebo_field* a = (k & 1) ? Ttmp : T;
+      const nebo_field* b = (k & 1) ? T : Ttmp;
+      if ((rc = heat_step_any(a, b, lam, dt, sp, s))) return rc;
+    }
+    if (steps & 1) NEBO_CUDA_TRY(cudaMemcpyAsync(T->data, Ttmp->data, bytes, cudaMemcpyDeviceToDevice, s));
+    return NEBO_OK;
+  }
+  GraphKey key{T->data, Ttmp->data, lam->data, {T->glob[0], T->glob[1], T->glob[2]}, T->dtype, steps, dt,
+               {sp[0], sp[1], sp[2]}};
+  cudaGraphExec_t exec = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    auto it = g_graphs.find(key);
+    if (it != g_graphs.end()) exec = it->second;
+  }
+  if (!exec) {
+    cudaStream_t cap;
+    NEBO_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    NEBO_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps && !rc; ++k) {
+      const nebo_field* a = (k & 1) ? Ttmp : T;
+      const nebo_field* b = (k & 1) ? T : Ttmp;
+      rc = heat_step_any(a, b, lam, dt, sp, cap);
+    }
+    if (!rc && (steps & 1)) {
+      cudaError_t e = cudaMemcpyAsync(T->data, Ttmp->data, bytes, cudaMemcpyDeviceToDevice, cap);
+      if (e != cudaSuccess) rc = cuda_fail(e, "nebo_heat_run capture copy");
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "nebo_heat_run capture");
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "nebo_heat_run instantiate");
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    g_graphs[key] = exec;
+  }
+  NEBO_CUDA_TRY(cudaGraphLaunch(exec, s));
+  return NEBO_OK;
+}

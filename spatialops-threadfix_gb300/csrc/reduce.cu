@@ -1,0 +1,203 @@
+// Reductions nebo_sum / nebo_max / nebo_min / nebo_norm (and _interior) over one field
+// (spatialops/NeboReductions.h:45-240).  The reference folds serially on the CPU; here a
+// two-pass, deterministic tree runs on the device:
+//   pass 1: one block per slice of rows, x-contiguous loads, per-thread Neumaier-compensated
+//           FP64 sums (or max/min), warp shuffles, one partial per block;
+//   pass 2: one block combines the partials in a fixed order.
+// FP32 fields are accumulated in FP64.  max/min use the reference's comparisons
+// ((r < v) ? v : r and (r > v) ? v : r), so they are exact.
+#include <cmath>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace nebo {
+namespace {
+
+constexpr int RED_THREADS = 256;
+constexpr int RED_MAX_BLOCKS = 1024;
+
+struct Acc {
+  double s, c;  // sum and running compensation (sum/norm), or the extremum in s
+};
+
+__device__ __forceinline__ void two_sum_add(Acc& a, double v) {
+  const double t = a.s + v;
+  if (fabs(a.s) >= fabs(v))
+    a.c += (a.s - t) + v;
+  else
+    a.c += (v - t) + a.s;
+  a.s = t;
+}
+
+__device__ __forceinline__ void merge(Acc& a, const Acc& b, int op) {
+  if (op == NEBO_RED_MAX) {
+    a.s = (a.s < b.s) ? b.s : a.s;
+  } else if (op == NEBO_RED_MIN) {
+    a.s = (a.s > b.s) ? b.s : a.s;
+  } else {
+    two_sum_add(a, b.s);
+    a.c += b.c;
+  }
+}
+
+__device__ __forceinline__ Acc identity(int op) {
+  Acc a;
+  a.s = op == NEBO_RED_MAX ? -INFINITY : (op == NEBO_RED_MIN ? INFINITY : 0.0);
+  a.c = 0.0;
+  return a;
+}
+
+__device__ Acc block_reduce(Acc a, int op) {
+  __shared__ Acc sh[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    Acc b;
+    b.s = __shfl_down_sync(0xffffffffu, a.s, o);
+    b.c = __shfl_down_sync(0xffffffffu, a.c, o);
+    merge(a, b, op);
+  }
+  if (lane == 0) sh[wid] = a;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  a = (threadIdx.x < nw) ? sh[threadIdx.x] : identity(op);
+  if (wid == 0) {
+    for (int o = 16; o > 0; o >>= 1) {
+      Acc b;
+      b.s = __shfl_down_sync(0xffffffffu, a.s, o);
+      b.c = __shfl_down_sync(0xffffffffu, a.c, o);
+      merge(a, b, op);
+    }
+  }
+  return a;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) reduce_rows_kernel(const T* __restrict__ base, int sy, long sz, int x0,
+                                                                  int x1, int y0, int ny, int z0, long nrows, int op,
+                                                                  Acc* __restrict__ partials) {
+  Acc a = identity(op);
+  for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const int y = y0 + (int)(r % ny);
+    const int z = z0 + (int)(r / ny);
+    const T* row = base + (long)sy * y + sz * z;
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      const double v = (double)__ldg(row + x);
+      if (op == NEBO_RED_MAX)
+        a.s = (a.s < v) ? v : a.s;
+      else if (op == NEBO_RED_MIN)
+        a.s = (a.s > v) ? v : a.s;
+      else if (op == NEBO_RED_NORM)
+        two_sum_add(a, v * v);
+      else
+        two_sum_add(a, v);
+    }
+  }
+  a = block_reduce(a, op);
+  if (threadIdx.x == 0) partials[blockIdx.x] = a;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) reduce_final_kernel(const Acc* __restrict__ partials, int n, int op,
+                                                                   double* __restrict__ out) {
+  Acc a = identity(op);
+  // fixed assignment of partials to threads -> deterministic result
+  for (int i = threadIdx.x; i < n; i += blockDim.x) merge(a, partials[i], op);
+  a = block_reduce(a, op);
+  if (threadIdx.x == 0) {
+    double r = (op == NEBO_RED_SUM || op == NEBO_RED_NORM) ? a.s + a.c : a.s;
+    if (op == NEBO_RED_NORM) r = sqrt(r);
+    *out = r;
+  }
+}
+
+// Per-call scratch from the stream-ordered pool: concurrent reductions on different streams
+// never share partials.
+int scratch_alloc(Acc** partials, double** result, cudaStream_t s) {
+  void* p = nullptr;
+  NEBO_CUDA_TRY(cudaMallocAsync(&p, RED_MAX_BLOCKS * sizeof(Acc) + 64, s));
+  *partials = (Acc*)p;
+  *result = (double*)((char*)p + RED_MAX_BLOCKS * sizeof(Acc));
+  return NEBO_OK;
+}
+
+}  // namespace
+
+// Region of a field reduction in glob coordinates: whole window (valid ghosts included) or the
+// window minus its valid ghosts (interior, BC cells included), as nebo_fold does.
+void reduction_region(const nebo_field& f, int interior, int lo[3], int hi[3]) {
+  for (int i = 0; i < 3; ++i) {
+    const int gm = f.extent[i] <= 1 ? 0 : f.ghost_minus[i];
+    const int gp = f.extent[i] <= 1 ? 0 : f.ghost_plus[i];
+    lo[i] = f.offset[i] + (interior ? gm : 0);
+    hi[i] = f.offset[i] + f.extent[i] - (interior ? gp : 0);
+  }
+}
+
+int reduce_field_into(const nebo_field* f, int op, int interior, double* d_result, Acc* partials, cudaStream_t s) {
+  int lo[3], hi[3];
+  reduction_region(*f, interior, lo, hi);
+  const long nrows = (long)(hi[1] - lo[1]) * (hi[2] - lo[2]);
+  if (nrows <= 0 || hi[0] <= lo[0]) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce: empty region");
+  int blocks = (int)(nrows < (long)num_sms() * 4 ? nrows : (long)num_sms() * 4);
+  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  const int sy = f->glob[0];
+  const long sz = (long)f->glob[0] * f->glob[1];
+  {
+    LaunchScope ls("reduce_rows", s);
+    if (f->dtype == NEBO_F64)
+    reduce_rows_kernel<double><<<blocks, RED_THREADS, 0, s>>>((const double*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                              hi[1] - lo[1], lo[2], nrows, op, partials);
+  else
+    reduce_rows_kernel<float><<<blocks, RED_THREADS, 0, s>>>((const float*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                             hi[1] - lo[1], lo[2], nrows, op, partials);
+  }
+  {
+    LaunchScope ls("reduce_final", s);
+    reduce_final_kernel<<<1, RED_THREADS, 0, s>>>(partials, blocks, op, d_result);
+  }
+  NEBO_LAUNCH_CHECK("nebo_reduce");
+  return NEBO_OK;
+}
+
+static int check_reduce_args(const nebo_field* f, int op) {
+  int rc = check_field(f, "nebo_reduce");
+  if (rc) return rc;
+  if (op < NEBO_RED_SUM || op > NEBO_RED_NORM) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce: bad op %d", op);
+  return NEBO_OK;
+}
+
+}  // namespace nebo
+
+using namespace nebo;
+
+extern "C" int nebo_reduce_async(const nebo_field* f, int op, int interior, double* d_result, nebo_stream_t stream) {
+  int rc = check_reduce_args(f, op);
+  if (rc) return rc;
+  if (!d_result) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_async: null result pointer");
+  Acc* partials;
+  double* dres;
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((rc = scratch_alloc(&partials, &dres, s))) return rc;
+  rc = reduce_field_into(f, op, interior, d_result, partials, s);
+  cudaFreeAsync(partials, s);
+  return rc;
+}
+
+extern "C" int nebo_reduce(const nebo_field* f, int op, int interior, double* result, nebo_stream_t stream) {
+  int rc = check_reduce_args(f, op);
+  if (rc) return rc;
+  if (!result) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce: null result pointer");
+  Acc* partials;
+  double* dres;
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((rc = scratch_alloc(&partials, &dres, s))) return rc;
+  rc = reduce_field_into(f, op, interior, dres, partials, s);
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(result, dres, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "nebo_reduce copy");
+  }
+  cudaFreeAsync(partials, s);
+  if (rc) return rc;
+  NEBO_CUDA_TRY(cudaStreamSynchronize(s));
+  return NEBO_OK;
+}

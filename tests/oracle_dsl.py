@@ -455,3 +455,13 @@ def fill_periodic(f, g):
     gz, gy, gx = f.shape
     lib().orc_fill_periodic(_p(f), _i3((gx - 2 * g, gy - 2 * g, gz - 2 * g)), int(g))
     return f
+
+
+def ghosts(expr, with_bc=True):
+    """ghosts_with_bc() / ghosts_without_bc() of an expression (minus[3], plus[3])."""
+    comp = _Compiled(expr)
+    m = (ctypes.c_int32 * 3)()
+    p = (ctypes.c_int32 * 3)()
+    if lib().orc_ghosts(ctypes.byref(comp.e), int(with_bc), m, p) != 0:
+        raise NeboError("ghost analysis failed")
+    return tuple(m), tuple(p)

@@ -1,0 +1,96 @@
+"""Fused heat step on the GPU against the reference (golden vectors) and the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_dsl as O
+import spatialops_gb300 as N
+from spatialops_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+
+
+def _run(lam, T0, steps, dt, dtype="f64", use_graph=True):
+    T = N.Field.from_numpy("SVol", T0, 1, dtype=dtype)
+    Tt = N.Field.from_numpy("SVol", np.zeros_like(T0), 1, dtype=dtype)
+    L = N.Field.from_numpy("SVol", lam, 1, dtype=dtype)
+    N.heat_run(T, Tt, L, steps, dt, use_graph=use_graph)
+    return T
+
+
+def test_heat_fp64_bitexact_vs_reference_golden():
+    z = np.load(os.path.join(GOLD, "heat.npz"))
+    T = _run(z["lam"], z["T0"], int(z["steps"]), float(z["dt"]))
+    assert (_bits(T.numpy()) == _bits(z["f:T"])).all()
+    # reductions: max exact; sum/norm within the compensated-sum bound
+    assert N.nebo_max(T) == float(z["v:max"])
+    absum = float(np.abs(z["f:T"]).sum())
+    assert abs(N.nebo_sum(T) - float(z["v:sum"])) <= 1e-13 * absum
+    assert abs(N.nebo_norm(T) - float(z["v:norm"])) <= 1e-13 * float(z["v:norm"])
+
+
+@pytest.mark.parametrize("n,steps", [((64, 64, 64), 20), ((37, 29, 18), 7), ((33, 9, 65), 4), ((2, 8, 5), 3)])
+def test_heat_fp64_bitexact_vs_oracle(n, steps):
+    lam, T0, dt = W.heat_inputs(n, sigma=min(n) / 4.0)
+    ref = O.heat_run(lam, T0, n, steps, dt)
+    T = _run(lam, T0, steps, dt)
+    assert (_bits(T.numpy()) == _bits(ref)).all()
+
+
+def test_heat_graph_equals_stream_launches():
+    lam, T0, dt = W.heat_inputs((40, 36, 20))
+    a = _run(lam, T0, 9, dt, use_graph=True).numpy()
+    b = _run(lam, T0, 9, dt, use_graph=False).numpy()
+    assert (_bits(a) == _bits(b)).all()
+
+
+def test_heat_fp32_error_vs_fp64_oracle():
+    n = (64, 48, 40)
+    lam, T0, dt = W.heat_inputs(n)
+    ref = O.heat_run(lam, T0, n, 50, dt)
+    T = _run(lam, T0, 50, dt, dtype="f32").numpy().astype(np.float64)
+    err = np.abs(T - ref).max() / np.abs(ref).max()
+    assert err <= 1e-5, err
+
+
+def test_heat_general_spacing_bitexact():
+    # non-unit spacing runs the reference's own operation order
+    n = (20, 16, 12)
+    lam, T0, _ = W.heat_inputs(n)
+    sp = (1.5, 0.75, 2.0)
+    dt = 0.1
+    T = N.Field.from_numpy("SVol", T0, 1)
+    Tt = N.Field.from_numpy("SVol", np.zeros_like(T0), 1)
+    L = N.Field.from_numpy("SVol", lam, 1)
+    N.heat_run(T, Tt, L, 3, dt, spacing=sp)
+    # oracle: generic expression evaluator with the registered operators for L = n*spacing
+    db = O.OpDB(n, tuple(n[i] * sp[i] for i in range(3)))
+    cur = T0.copy()
+    lamf = O.fill_periodic(lam.copy(), 1)
+    for _ in range(3):
+        O.fill_periodic(cur, 1)
+        nxt = cur.copy()
+        Tf, Lf, Nf = (O.Field("SVol", a, 1) for a in (cur, lamf, nxt))
+        fx, fy, fz = O.FACES["SVol"]
+        rhs = (db.div(fx, "SVol")(db.interp("SVol", fx)(Lf) * db.grad("SVol", fx)(Tf))
+               + db.div(fy, "SVol")(db.interp("SVol", fy)(Lf) * db.grad("SVol", fy)(Tf))
+               + db.div(fz, "SVol")(db.interp("SVol", fz)(Lf) * db.grad("SVol", fz)(Tf)))
+        O.assign(Nf, Tf + dt * rhs)
+        cur = nxt
+    O.fill_periodic(cur, 1)
+    assert (_bits(T.numpy()) == _bits(cur)).all()
+
+
+def test_heat_rejects_in_place_and_bad_ghosts():
+    T = N.Field("SVol", (8, 8, 8), 1)
+    with pytest.raises(RuntimeError, match="in-place"):
+        N.heat_step(T, T, T, 0.1)
+    T2 = N.Field("SVol", (8, 8, 8), 2)
+    with pytest.raises(RuntimeError, match="ghost"):
+        N.heat_step(T2, N.Field("SVol", (8, 8, 8), 2), N.Field("SVol", (8, 8, 8), 2), 0.1)
