@@ -110,6 +110,18 @@ int nebo_reduce(const nebo_field* f, int op, int interior, double* result, nebo_
 int nebo_reduce_async(const nebo_field* f, int op, int interior, double* d_result,
                       nebo_stream_t stream);
 
+/* Same reduction, same result as nebo_reduce_async, but it allocates nothing: no counterpart in
+ * the reference.  For callers that must not enter the CUDA allocator at the call (a host
+ * framework that reserved the device memory up front in its own pool, so another allocation
+ * fails or breaks its accounting; code running where the allocator may not be entered).  The
+ * block partials live in a fixed device array of 1024 slots (16 KiB, held on every GPU that
+ * loads the library until exit); a reduction that would need more slots is rejected with
+ * NEBO_ERR_INVALID.  The first call on a device looks the array up (cudaGetSymbolAddress) with
+ * that device current and should come before any stream capture.  All calls share the array:
+ * calls whose kernels overlap on the GPU race on it.  The result is written to d_result. */
+int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, double* d_result,
+                        nebo_stream_t stream);
+
 /* ------------------------------------------------------------------ fused heat equation
  * One explicit Euler step of the reference's scalar heat RHS
  *   Tout <<= T + dt*( DivX(InterpX(lam)*GradX(T)) + DivY(...) + DivZ(...) )

@@ -70,6 +70,7 @@ SIGNATURES = [
     ("nebo_mask_from_points", _I, [_P, _I3, _I3, _P, ctypes.c_int32, _P]),
     ("nebo_reduce", _I, [_FP, _I, _I, ctypes.POINTER(_D), _P]),
     ("nebo_reduce_async", _I, [_FP, _I, _I, _P, _P]),
+    ("nebo_reduce_noalloc", _I, [_FP, _I, _I, _P, _P]),
     ("nebo_heat_step", _I, [_FP, _FP, _FP, _D, ctypes.POINTER(_D), _P]),
     ("nebo_heat_run", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
     ("nebo_deep_chain", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _P]),

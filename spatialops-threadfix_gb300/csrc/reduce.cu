@@ -201,3 +201,87 @@ extern "C" int nebo_reduce(const nebo_field* f, int op, int interior, double* re
   NEBO_CUDA_TRY(cudaStreamSynchronize(s));
   return NEBO_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// Reduction without any allocation.
+//
+// nebo_reduce / nebo_reduce_async take their block partials from the stream-ordered pool on
+// every call.  Callers that must not enter the CUDA allocator at that point (a host framework
+// that has reserved the device memory up front in its own pool, so a further cudaMalloc fails or
+// breaks its accounting; code that runs where the allocator may not be entered) use
+// nebo_reduce_noalloc instead: the same two kernels, with the partials in the fixed array below.
+//
+// The array lives in this module's device memory for every GPU that loads the library, until the
+// process exits.  Host code cannot use the symbol's name as a device address, so the first call
+// on each device (with that device current) looks the address up with cudaGetSymbolAddress and
+// caches it; that first call should come before any stream capture.  All calls share the array
+// and it keeps the last call's contents: pass 1 writes every slot that pass 2 reads, so nothing
+// needs clearing, but calls whose kernels overlap on the GPU (different streams, no ordering
+// between them) race on it.
+namespace nebo {
+namespace {
+
+constexpr int NOALLOC_MAX_PARTIALS = 1024;  // 16 KiB: one (sum, compensation) pair per block
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static __device__ __align__(256) Acc g_noalloc_partials[NOALLOC_MAX_PARTIALS];
+
+std::mutex g_noalloc_mu;
+Acc* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+int noalloc_partials(Acc** out) {
+  int dev = 0;
+  NEBO_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_reduce_noalloc: device index %d beyond %d", dev,
+                NOALLOC_MAX_DEVICES);
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess) return cuda_fail(e, "nebo_reduce_noalloc (cudaGetSymbolAddress)");
+    g_noalloc_addr[dev] = static_cast<Acc*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return NEBO_OK;
+}
+
+}  // namespace
+}  // namespace nebo
+
+extern "C" int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, double* d_result,
+                                   nebo_stream_t stream) {
+  int rc = check_reduce_args(f, op);
+  if (rc) return rc;
+  if (!d_result) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_noalloc: null result pointer");
+  int lo[3], hi[3];
+  reduction_region(*f, interior, lo, hi);
+  const long nrows = (long)(hi[1] - lo[1]) * (hi[2] - lo[2]);
+  if (nrows <= 0 || hi[0] <= lo[0]) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_noalloc: empty region");
+  const long want = nrows < (long)num_sms() * 4 ? nrows : (long)num_sms() * 4;
+  if (want > NOALLOC_MAX_PARTIALS)
+    return fail(NEBO_ERR_INVALID,
+                "Nebo error in nebo_reduce_noalloc: the reduction needs %ld partial slots but the static scratch "
+                "holds %d",
+                want, NOALLOC_MAX_PARTIALS);
+  const int blocks = (int)want;
+  Acc* partials = nullptr;
+  if ((rc = noalloc_partials(&partials))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int sy = f->glob[0];
+  const long sz = (long)f->glob[0] * f->glob[1];
+  {
+    LaunchScope ls("reduce_rows", s);
+    if (f->dtype == NEBO_F64)
+      reduce_rows_kernel<double><<<blocks, RED_THREADS, 0, s>>>((const double*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                                hi[1] - lo[1], lo[2], nrows, op, partials);
+    else
+      reduce_rows_kernel<float><<<blocks, RED_THREADS, 0, s>>>((const float*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                               hi[1] - lo[1], lo[2], nrows, op, partials);
+  }
+  {
+    LaunchScope ls("reduce_final", s);
+    reduce_final_kernel<<<1, RED_THREADS, 0, s>>>(partials, blocks, op, d_result);
+  }
+  NEBO_LAUNCH_CHECK("nebo_reduce_noalloc");
+  return NEBO_OK;
+}
