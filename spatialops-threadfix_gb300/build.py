@@ -54,6 +54,46 @@ def _compile(src, obj, extra=()):
     return obj
 
 
+TESTS_CPP = os.path.join(REPO, "tests", "cpp")
+TESTS_BUILD = os.path.join(TESTS_CPP, "_build")
+# C++ programs written against the drop-in headers (include/spatialops): name -> (source, flags)
+PROGRAMS = {
+    "catalog_gpu_exact": ("catalog_gpu.cu", ["-DNEBO_EXACT_ARITHMETIC"]),
+    "catalog_gpu_fast": ("catalog_gpu.cu", []),
+}
+
+
+def _dropin_headers():
+    return glob.glob(os.path.join(INCLUDE, "spatialops", "**", "*.h"), recursive=True) + \
+        glob.glob(os.path.join(TESTS_CPP, "*.h")) + glob.glob(os.path.join(TESTS_CPP, "*.inc"))
+
+
+def _compile_program(name, src, flags):
+    exe = os.path.join(TESTS_BUILD, name)
+    cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", TESTS_CPP, *flags,
+           src, "-o", exe, "-L", BUILD, "-lnebo_gb300", "-Xlinker", "-rpath," + BUILD]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr[-4000:]}")
+    return exe
+
+
+def build_programs(verbose=False):
+    """Compile the drop-in C++ test programs (needs the library already linked)."""
+    os.makedirs(TESTS_BUILD, exist_ok=True)
+    deps = _dropin_headers() + glob.glob(os.path.join(INCLUDE, "*.h")) + [LIB]
+    jobs = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(PROGRAMS))) as ex:
+        for name, (src, flags) in PROGRAMS.items():
+            srcp = os.path.join(TESTS_CPP, src)
+            if _stale(os.path.join(TESTS_BUILD, name), [srcp, *deps, __file__]):
+                jobs.append(ex.submit(_compile_program, name, srcp, flags))
+        for j in jobs:
+            j.result()
+    if verbose:
+        print("built test programs in", TESTS_BUILD)
+
+
 def build_library(verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
@@ -79,4 +119,6 @@ def build_library(verbose=False, extra_flags=()):
 
 if __name__ == "__main__":
     build_library(verbose=True)
+    if "--programs" in sys.argv:
+        build_programs(verbose=True)
     sys.exit(0)
