@@ -145,19 +145,17 @@ class Deep:
         self.words = self.host_mask.to("cuda")
         self.out = N.Field("XVol", n, 1)
         self.filt = N.Field("XVol", n, 1)
-        self.red = torch.zeros(3, dtype=torch.float64, device="cuda")
+        self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
         self.cells = n ** 3
-        self.launches_per_step = 2 + 3 * 2
+        self.launches_per_step = 2 + 2
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
-        self.d2h_bytes = 3 * 8
-        self.host_red = torch.zeros(3, dtype=torch.float64).pin_memory()
+        self.d2h_bytes = 4 * 8
+        self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
 
     def step(self):
         N = self.N
         N.deep_chain(self.A, self.B, self.C, self.words, self.out, self.filt)
-        N.reduce_async(self.filt, "sum", False, self.red[0:1])
-        N.reduce_async(self.filt, "max", False, self.red[1:2])
-        N.reduce_async(self.filt, "norm", False, self.red[2:3])
+        N.reduce_all(self.filt, False, self.red)  # nebo_sum, nebo_max (and min), nebo_norm in one pass
 
     def step_e2e(self):
         for f, h in zip((self.A, self.B, self.C), self.host):

@@ -110,6 +110,11 @@ int nebo_reduce(const nebo_field* f, int op, int interior, double* result, nebo_
 int nebo_reduce_async(const nebo_field* f, int op, int interior, double* d_result,
                       nebo_stream_t stream);
 
+/* sum, max, min and norm of the same region in ONE pass (d_out4[0..3], device memory): each
+ * element costs two FP64 operations; max/min compare order-preserving integer keys (NaNs are
+ * skipped, as the reference's comparisons skip them). */
+int nebo_reduce_all(const nebo_field* f, int interior, double* d_out4, nebo_stream_t stream);
+
 /* Same reduction, same result as nebo_reduce_async, but it allocates nothing: no counterpart in
  * the reference.  For callers that must not enter the CUDA allocator at the call (a host
  * framework that reserved the device memory up front in its own pool, so another allocation

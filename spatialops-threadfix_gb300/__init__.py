@@ -71,6 +71,7 @@ SIGNATURES = [
     ("nebo_reduce", _I, [_FP, _I, _I, ctypes.POINTER(_D), _P]),
     ("nebo_reduce_async", _I, [_FP, _I, _I, _P, _P]),
     ("nebo_reduce_noalloc", _I, [_FP, _I, _I, _P, _P]),
+    ("nebo_reduce_all", _I, [_FP, _I, _P, _P]),
     ("nebo_heat_step", _I, [_FP, _FP, _FP, _D, ctypes.POINTER(_D), _P]),
     ("nebo_heat_run", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
     ("nebo_deep_chain", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _P]),
@@ -229,6 +230,12 @@ def reduce_async(f, op, interior, d_result, stream=None):
     d = f.desc()
     _check(lib().nebo_reduce_async(ctypes.byref(d), RED[op], int(interior), ctypes.c_void_p(d_result.data_ptr()),
                                    _stream(stream)))
+
+
+def reduce_all(f, interior, d_out4, stream=None):
+    """sum, max, min, norm of one field in a single pass into a device float64 tensor of 4."""
+    d = f.desc()
+    _check(lib().nebo_reduce_all(ctypes.byref(d), int(interior), ctypes.c_void_p(d_out4.data_ptr()), _stream(stream)))
 
 
 def heat_step(T, Tout, lam, dt, spacing=(1.0, 1.0, 1.0), stream=None):

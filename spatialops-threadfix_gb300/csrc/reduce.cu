@@ -7,6 +7,7 @@
 // FP32 fields are accumulated in FP64.  max/min use the reference's comparisons
 // ((r < v) ? v : r and (r > v) ? v : r), so they are exact.
 #include <cmath>
+#include <climits>
 #include <mutex>
 
 #include "common.cuh"
@@ -283,5 +284,148 @@ extern "C" int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, do
     reduce_final_kernel<<<1, RED_THREADS, 0, s>>>(partials, blocks, op, d_result);
   }
   NEBO_LAUNCH_CHECK("nebo_reduce_noalloc");
+  return NEBO_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// All four reductions in one pass over the field (nebo_sum, nebo_max, nebo_min, nebo_norm of
+// the same region), for callers that need several of them: the field is read once instead of
+// four times.  FP64 is the scarce unit on this GPU, so each element costs two FP64 operations
+// (one add for the sum, one fused multiply-add for the sum of squares); max and min compare
+// order-preserving 64-bit integer keys of the doubles on the integer pipe.  Per-thread partial
+// sums are plain (at most a few hundred terms each); partials are combined with Neumaier
+// compensation.  NaNs are skipped by max/min, as the reference's comparisons skip them; equal
+// zeros of opposite sign may come back with either sign.
+namespace nebo {
+namespace {
+
+struct Acc4 {
+  double s, sc, q, qc;  // sum and compensation, sum of squares and compensation
+  long long mx, mn;     // order-preserving keys of max and min
+};
+
+__device__ __forceinline__ long long order_key(double v) {
+  long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double from_key(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+__device__ __forceinline__ void comp_add(double& s, double& c, double v) {
+  const double t = s + v;
+  c += (fabs(s) >= fabs(v)) ? ((s - t) + v) : ((v - t) + s);
+  s = t;
+}
+__device__ __forceinline__ void merge4(Acc4& a, const Acc4& b) {
+  comp_add(a.s, a.sc, b.s);
+  a.sc += b.sc;
+  comp_add(a.q, a.qc, b.q);
+  a.qc += b.qc;
+  a.mx = a.mx > b.mx ? a.mx : b.mx;
+  a.mn = a.mn < b.mn ? a.mn : b.mn;
+}
+__device__ __forceinline__ Acc4 shfl_down4(const Acc4& a, int o) {
+  Acc4 b;
+  b.s = __shfl_down_sync(0xffffffffu, a.s, o);
+  b.sc = __shfl_down_sync(0xffffffffu, a.sc, o);
+  b.q = __shfl_down_sync(0xffffffffu, a.q, o);
+  b.qc = __shfl_down_sync(0xffffffffu, a.qc, o);
+  b.mx = __shfl_down_sync(0xffffffffu, a.mx, o);
+  b.mn = __shfl_down_sync(0xffffffffu, a.mn, o);
+  return b;
+}
+__device__ Acc4 block_reduce4(Acc4 a) {
+  __shared__ Acc4 sh[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) merge4(a, shfl_down4(a, o));
+  if (lane == 0) sh[wid] = a;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (wid == 0) {
+    if (lane < nw) {
+      a = sh[lane];
+    } else {
+      a.s = a.sc = a.q = a.qc = 0.0;
+      a.mx = LLONG_MIN;
+      a.mn = LLONG_MAX;
+    }
+    for (int o = 16; o > 0; o >>= 1) merge4(a, shfl_down4(a, o));
+  }
+  return a;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) reduce4_rows_kernel(const T* __restrict__ base, int sy, long sz, int x0,
+                                                                   int x1, int y0, int ny, int z0, long nrows,
+                                                                   Acc4* __restrict__ partials) {
+  double s = 0.0, q = 0.0;
+  long long mx = LLONG_MIN, mn = LLONG_MAX;
+  for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const int y = y0 + (int)(r % ny);
+    const int z = z0 + (int)(r / ny);
+    const T* row = base + (long)sy * y + sz * z;
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      const double v = (double)__ldg(row + x);
+      s += v;
+      q = fma(v, v, q);
+      if (v == v) {  // NaNs never win a comparison in the reference's fold
+        const long long k = order_key(v);
+        mx = k > mx ? k : mx;
+        mn = k < mn ? k : mn;
+      }
+    }
+  }
+  Acc4 a{s, 0.0, q, 0.0, mx, mn};
+  a = block_reduce4(a);
+  if (threadIdx.x == 0) partials[blockIdx.x] = a;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) reduce4_final_kernel(const Acc4* __restrict__ partials, int n,
+                                                                    double* __restrict__ out) {
+  Acc4 a{0.0, 0.0, 0.0, 0.0, LLONG_MIN, LLONG_MAX};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) merge4(a, partials[i]);
+  a = block_reduce4(a);
+  if (threadIdx.x == 0) {
+    out[0] = a.s + a.sc;
+    out[1] = a.mx == LLONG_MIN ? -INFINITY : from_key(a.mx);
+    out[2] = a.mn == LLONG_MAX ? INFINITY : from_key(a.mn);
+    out[3] = sqrt(a.q + a.qc);
+  }
+}
+
+}  // namespace
+}  // namespace nebo
+
+extern "C" int nebo_reduce_all(const nebo_field* f, int interior, double* d_out4, nebo_stream_t stream) {
+  int rc = check_reduce_args(f, NEBO_RED_SUM);
+  if (rc) return rc;
+  if (!d_out4) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_all: null result pointer");
+  int lo[3], hi[3];
+  reduction_region(*f, interior, lo, hi);
+  const long nrows = (long)(hi[1] - lo[1]) * (hi[2] - lo[2]);
+  if (nrows <= 0 || hi[0] <= lo[0]) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_all: empty region");
+  int blocks = (int)(nrows < (long)num_sms() * 4 ? nrows : (long)num_sms() * 4);
+  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  cudaStream_t s = (cudaStream_t)stream;
+  Acc4* partials = nullptr;
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&partials, sizeof(Acc4) * blocks, s));
+  const int sy = f->glob[0];
+  const long sz = (long)f->glob[0] * f->glob[1];
+  {
+    LaunchScope ls("reduce4_rows", s);
+    if (f->dtype == NEBO_F64)
+      reduce4_rows_kernel<double><<<blocks, RED_THREADS, 0, s>>>((const double*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                                 hi[1] - lo[1], lo[2], nrows, partials);
+    else
+      reduce4_rows_kernel<float><<<blocks, RED_THREADS, 0, s>>>((const float*)f->data, sy, sz, lo[0], hi[0], lo[1],
+                                                                hi[1] - lo[1], lo[2], nrows, partials);
+  }
+  {
+    LaunchScope ls("reduce4_final", s);
+    reduce4_final_kernel<<<1, RED_THREADS, 0, s>>>(partials, blocks, d_out4);
+  }
+  cudaError_t le = cudaGetLastError();
+  cudaFreeAsync(partials, s);
+  if (le != cudaSuccess) return cuda_fail(le, "nebo_reduce_all");
   return NEBO_OK;
 }
