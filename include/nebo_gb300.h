@@ -155,6 +155,31 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
                     const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
                     double dx, nebo_stream_t stream);
 
+/* ------------------------------------------------------------------ batched patches
+ * Many independent periodic heat-equation patches (one ghost layer, scalar lambda and dt per
+ * patch) advanced together: each time step is ONE persistent launch over a device patch table
+ * and a work list of (patch, tile, z-chunk) items; nebo_patchset_run captures the steps in a
+ * CUDA graph.  The reference advances such patches one `<<=` at a time from the caller's patch
+ * loop (one gpu_assign_kernel launch per expression and patch, spatialops/NeboLhs.h:29-41).
+ *   create:   shapes = 3 ints per patch (interior nx, ny, nz >= 2); allocates two arenas holding
+ *             every patch window (x fastest), returned by nebo_patchset_arena(ps, 0|1); the
+ *             element offset of each window comes from nebo_patchset_info.
+ *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest (clobbers
+ *             the arenas: call it before loading data).
+ *   run:      `steps` steps from arena `start`; *final_arena says where the result is.
+ * FP64 results are bit-identical to the reference's serial walk on a constant lambda field. */
+typedef struct nebo_patchset nebo_patchset;
+int nebo_patchset_create(nebo_patchset** ps, int npatch, const int32_t* shapes, const double* lam,
+                         const double* dt, int dtype);
+int nebo_patchset_destroy(nebo_patchset* ps);
+int nebo_patchset_info(const nebo_patchset* ps, int64_t* total_elems, int64_t* offsets,
+                       int32_t* log2_tile_x, int32_t* nitems);
+void* nebo_patchset_arena(const nebo_patchset* ps, int which);
+int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, nebo_stream_t stream);
+int nebo_patchset_autotune(nebo_patchset* ps, nebo_stream_t stream, int32_t* chosen_log2_tile_x);
+int nebo_patchset_run(nebo_patchset* ps, int start, int steps, int use_graph, int* final_arena,
+                      nebo_stream_t stream);
+
 /* ------------------------------------------------------------------ launch accounting
  * Every kernel launch of this library is counted; with profiling on, each launch (outside
  * graph capture) is also bracketed by CUDA events on its stream.  nebo_profile_report

@@ -75,6 +75,13 @@ SIGNATURES = [
     ("nebo_heat_step", _I, [_FP, _FP, _FP, _D, ctypes.POINTER(_D), _P]),
     ("nebo_heat_run", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
     ("nebo_deep_chain", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _P]),
+    ("nebo_patchset_create", _I, [ctypes.POINTER(_P), _I, _P, _P, _P, _I]),
+    ("nebo_patchset_destroy", _I, [_P]),
+    ("nebo_patchset_info", _I, [_P, _P, _P, _P, _P]),
+    ("nebo_patchset_arena", _P, [_P, _I]),
+    ("nebo_patchset_fill_ghosts", _I, [_P, _I, _P]),
+    ("nebo_patchset_autotune", _I, [_P, _P, _P]),
+    ("nebo_patchset_run", _I, [_P, _I, _I, _I, ctypes.POINTER(_I), _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
     ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
@@ -273,3 +280,74 @@ def profile_report(reset=True):
     buf = ctypes.create_string_buffer(1 << 16)
     _check(lib().nebo_profile_report(buf, len(buf), int(reset)))
     return json.loads(buf.value.decode())
+
+
+class PatchSet:
+    """Batched periodic heat patches (nebo_patchset_*): one persistent launch per step."""
+
+    def __init__(self, shapes, lam, dt, dtype="f64"):
+        self.shapes = np.ascontiguousarray(shapes, dtype=np.int32).reshape(-1, 3)
+        self.npatch = len(self.shapes)
+        self.lam = np.ascontiguousarray(lam, dtype=np.float64)
+        self.dt = np.ascontiguousarray(dt, dtype=np.float64)
+        self.dtype = F64 if dtype == "f64" else F32
+        self.esize = 8 if self.dtype == F64 else 4
+        h = ctypes.c_void_p()
+        _check(lib().nebo_patchset_create(ctypes.byref(h), self.npatch, ctypes.c_void_p(self.shapes.ctypes.data),
+                                          ctypes.c_void_p(self.lam.ctypes.data), ctypes.c_void_p(self.dt.ctypes.data),
+                                          self.dtype))
+        self.h = h
+        self._info()
+
+    def _info(self):
+        total = ctypes.c_int64()
+        self.offsets = np.zeros(self.npatch, dtype=np.int64)
+        self.log2tx = np.zeros(self.npatch, dtype=np.int32)
+        nitems = ctypes.c_int32()
+        _check(lib().nebo_patchset_info(self.h, ctypes.byref(total), ctypes.c_void_p(self.offsets.ctypes.data),
+                                        ctypes.c_void_p(self.log2tx.ctypes.data), ctypes.byref(nitems)))
+        self.total, self.nitems = total.value, nitems.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().nebo_patchset_destroy(self.h)
+        except Exception:
+            pass
+
+    def arena(self, which):
+        """The arena as a torch tensor view (no copy)."""
+        import torch
+
+        ptr = lib().nebo_patchset_arena(self.h, int(which))
+        nbytes = self.total * self.esize
+        cls = ctypes.c_double if self.dtype == F64 else ctypes.c_float
+        # wrap the raw device pointer through a CUDA array interface
+        class _CAI:
+            pass
+        obj = _CAI()
+        obj.__cuda_array_interface__ = {"shape": (self.total,), "typestr": "<f8" if self.dtype == F64 else "<f4",
+                                        "data": (ptr, False), "version": 3, "strides": None}
+        del cls, nbytes
+        return torch.as_tensor(obj, device="cuda")
+
+    def window(self, which, p):
+        nx, ny, nz = (int(v) for v in self.shapes[p])
+        n = (nx + 2) * (ny + 2) * (nz + 2)
+        o = int(self.offsets[p])
+        return self.arena(which)[o:o + n].view(nz + 2, ny + 2, nx + 2)
+
+    def fill_ghosts(self, which=0, stream=None):
+        _check(lib().nebo_patchset_fill_ghosts(self.h, int(which), _stream(stream)))
+
+    def autotune(self, stream=None):
+        out = np.zeros(self.npatch, dtype=np.int32)
+        _check(lib().nebo_patchset_autotune(self.h, _stream(stream), ctypes.c_void_p(out.ctypes.data)))
+        self._info()
+        return out
+
+    def run(self, steps, start=0, use_graph=True, stream=None):
+        fin = ctypes.c_int()
+        _check(lib().nebo_patchset_run(self.h, int(start), int(steps), int(use_graph), ctypes.byref(fin),
+                                       _stream(stream)))
+        return fin.value

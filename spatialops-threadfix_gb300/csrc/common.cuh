@@ -78,6 +78,9 @@ class LaunchScope {
   void* b_;
 };
 
+// Periodic ghost fill of one uniform-ghost patch (ghost.cu).
+int fill_periodic_any(const nebo_field* f, cudaStream_t s);
+
 inline int num_sms() {
   static int n = 0;
   if (!n) {

@@ -226,8 +226,6 @@ std::map<GraphKey, cudaGraphExec_t> g_graphs;
 
 }  // namespace
 
-int fill_periodic_any(const nebo_field* f, cudaStream_t s);  // ghost.cu
-
 }  // namespace nebo
 
 using namespace nebo;

@@ -1,0 +1,414 @@
+// Batched patches: many independent periodic heat-equation patches of uneven sizes advanced by
+// ONE persistent launch per step over a device patch table, with the steps captured in a CUDA
+// graph and the tile shape of each patch picked by a small autotuner.
+//
+// The reference advances patches one `<<=` at a time from the caller's patch loop (Uintah/
+// Wasatch-style; spatialops/NeboLhs.h:29-41 launches a 16x16 grid per expression), paying a
+// launch and a tail per patch and expression.  Here:
+//   * all patches live in one arena per buffer (FP64 or FP32), each a ghosted window, x fastest;
+//   * a work list enumerates (patch, x-tile, y-tile, z-chunk) items; a fixed grid of blocks
+//     (a multiple of the SM count) strides through it, so small and large patches share SMs;
+//   * tiles are TX x TY = 256 cells per plane with TX in {16, 32, 64} per patch (the autotuner
+//     times each candidate on the patches of each x-extent class and keeps the fastest);
+//   * each item is the fused heat step of nebo_heat_step: face fluxes computed once, high
+//     faces shared through shared memory, z-face carried in a register, and the new values
+//     written to the interior and to their periodic ghost images in the same pass.
+// Lambda is a scalar per patch, so each face costs (2 lambda) * (Tb - Ta): exactly twice the flux
+// the reference computes for a constant lambda field, (lam*1/2 + lam*1/2) * (Ta*(-1) + Tb*1),
+// and with the update scaled by dt/2 the FP64 results are bit-identical to the reference's
+// serial walk with such a field.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "common.cuh"
+
+struct nebo_patchset;  // opaque handle of the C ABI
+
+namespace nebo {
+namespace {
+
+constexpr int PT_THREADS = 256;
+constexpr int PT_MAX_TY = 16;   // TX = 16
+constexpr int PT_MAX_TX = 64;   // TY = 4
+
+struct PatchDev {
+  long long offset;  // element offset of the patch window in the arena
+  int nx, ny, nz;
+  int log2tx;        // tile x extent = 1 << log2tx
+  double lam2;       // 2*lambda
+  double hdt;        // dt/2
+};
+
+struct WorkItem {
+  int patch;
+  int x0, y0;
+  int z0, z1;
+};
+
+template <typename T>
+__device__ __forceinline__ T exact_sub(T a, T b);
+template <>
+__device__ __forceinline__ double exact_sub(double a, double b) { return __dsub_rn(a, b); }
+template <>
+__device__ __forceinline__ float exact_sub(float a, float b) { return a - b; }
+template <typename T>
+__device__ __forceinline__ T exact_add(T a, T b);
+template <>
+__device__ __forceinline__ double exact_add(double a, double b) { return __dadd_rn(a, b); }
+template <>
+__device__ __forceinline__ float exact_add(float a, float b) { return a + b; }
+template <typename T>
+__device__ __forceinline__ T exact_mul(T a, T b);
+template <>
+__device__ __forceinline__ double exact_mul(double a, double b) { return __dmul_rn(a, b); }
+template <>
+__device__ __forceinline__ float exact_mul(float a, float b) { return a * b; }
+
+template <typename T>
+__device__ __forceinline__ void store_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
+                                             T v) {
+  int xs[3], ys[3], zs[3];
+  int cx = 0, cy = 0, cz = 0;
+  xs[cx++] = x;
+  if (x == 0) xs[cx++] = nx;
+  if (x == nx - 1) xs[cx++] = -1;
+  ys[cy++] = y;
+  if (y == 0) ys[cy++] = ny;
+  if (y == ny - 1) ys[cy++] = -1;
+  zs[cz++] = z;
+  if (z == 0) zs[cz++] = nz;
+  if (z == nz - 1) zs[cz++] = -1;
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+}
+
+// One persistent launch = one time step of every patch.
+template <typename T>
+__global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev* __restrict__ patches,
+                                                                  const WorkItem* __restrict__ items, int nitems,
+                                                                  const T* __restrict__ src, T* __restrict__ dst) {
+  __shared__ T sfx[2][PT_MAX_TY * (PT_MAX_TX + 1) / 4 + 64];  // TY*(TX+1) <= 16*17, 8*33, 4*65
+  __shared__ T sfy[2][(PT_MAX_TY + 1) * 16 + 64];            // (TY+1)*TX <= 17*16, 9*32, 5*64
+  const int tid = threadIdx.x;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const WorkItem it = items[w];
+    const PatchDev P = patches[it.patch];
+    const int lx = P.log2tx, TX = 1 << lx, TY = PT_THREADS >> lx;
+    const int tx = tid & (TX - 1), ty = tid >> lx;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int sy = nx + 2;
+    const long sz = (long)(nx + 2) * (ny + 2);
+    const long interior = (long)1 + sy + sz;  // flat offset of interior (0,0,0)
+    const T* tin = src + P.offset + interior;
+    T* tout = dst + P.offset + interior;
+    const T l2 = (T)P.lam2, hdt = (T)P.hdt;
+    const int x = it.x0 + tx, y = it.y0 + ty;
+    const bool active = x < nx && y < ny;
+    const int xc = min(x, nx), yc = min(y, ny);
+    auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+    auto flux = [&](T ta, T tb) { return exact_mul(l2, exact_sub(tb, ta)); };
+    T tc = __ldg(tin + at(xc, yc, it.z0));
+    T fzlo = flux(__ldg(tin + at(xc, yc, it.z0 - 1)), tc);
+    for (int z = it.z0; z < it.z1; ++z) {
+      const int buf = z & 1;
+      const T tn = __ldg(tin + at(xc, yc, z + 1));
+      const T fzhi = flux(tc, tn);
+      const T fx = flux(__ldg(tin + at(xc - 1, yc, z)), tc);
+      const T fy = flux(__ldg(tin + at(xc, yc - 1, z)), tc);
+      sfx[buf][ty * (TX + 1) + tx] = fx;
+      sfy[buf][ty * TX + tx] = fy;
+      if (ty == 0) {  // +y halo faces of the tile
+        const int yh = it.y0 + TY;
+        if (yh <= ny && x <= nx) sfy[buf][TY * TX + tx] = flux(__ldg(tin + at(xc, yh - 1, z)), __ldg(tin + at(xc, yh, z)));
+      } else if (ty == 1 && tx < TY) {  // +x halo faces of the tile
+        const int xh = it.x0 + TX, yr = it.y0 + tx;
+        if (xh <= nx && yr < ny) sfx[buf][tx * (TX + 1) + TX] = flux(__ldg(tin + at(xh - 1, yr, z)), __ldg(tin + at(xh, yr, z)));
+      }
+      __syncthreads();
+      if (active) {
+        const T fxhi = sfx[buf][ty * (TX + 1) + tx + 1];
+        const T fyhi = sfy[buf][(ty + 1) * TX + tx];
+        const T s = exact_add(exact_add(exact_sub(fxhi, fx), exact_sub(fyhi, fy)), exact_sub(fzhi, fzlo));
+        store_images(tout, sy, sz, x, y, z, nx, ny, nz, exact_add(tc, exact_mul(hdt, s)));
+      }
+      tc = tn;
+      fzlo = fzhi;
+    }
+    __syncthreads();  // shared faces are reused by the next item
+  }
+}
+
+}  // namespace
+
+struct PatchSet {
+  int npatch = 0;
+  int dtype = NEBO_F64;
+  std::vector<int> shape;  // 3 per patch
+  std::vector<long long> offset;
+  std::vector<double> lam, dt;
+  std::vector<int> log2tx;
+  long long total = 0;  // elements per arena
+  void* arena[2] = {nullptr, nullptr};
+  PatchDev* d_patches = nullptr;
+  WorkItem* d_items = nullptr;
+  int nitems = 0;
+  int zchunk = 16;
+  int grid = 0;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, parity) -> graph
+  ~PatchSet() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(arena[0]);
+    cudaFree(arena[1]);
+    cudaFree(d_patches);
+    cudaFree(d_items);
+  }
+};
+
+namespace {
+
+std::vector<WorkItem> build_items(const PatchSet& ps, const std::vector<int>& which, int zchunk) {
+  std::vector<WorkItem> items;
+  for (int p : which) {
+    const int nx = ps.shape[3 * p], ny = ps.shape[3 * p + 1], nz = ps.shape[3 * p + 2];
+    const int TX = 1 << ps.log2tx[p], TY = PT_THREADS / TX;
+    for (int z0 = 0; z0 < nz; z0 += zchunk)
+      for (int y0 = 0; y0 < ny; y0 += TY)
+        for (int x0 = 0; x0 < nx; x0 += TX) items.push_back(WorkItem{p, x0, y0, z0, std::min(z0 + zchunk, nz)});
+  }
+  // largest z-extent items first so the strided assignment ends with short items
+  std::stable_sort(items.begin(), items.end(), [](const WorkItem& a, const WorkItem& b) { return (a.z1 - a.z0) > (b.z1 - b.z0); });
+  return items;
+}
+
+int upload_tables(PatchSet& ps, const std::vector<WorkItem>& items, cudaStream_t s) {
+  std::vector<PatchDev> pd(ps.npatch);
+  for (int p = 0; p < ps.npatch; ++p) {
+    pd[p].offset = ps.offset[p];
+    pd[p].nx = ps.shape[3 * p];
+    pd[p].ny = ps.shape[3 * p + 1];
+    pd[p].nz = ps.shape[3 * p + 2];
+    pd[p].log2tx = ps.log2tx[p];
+    pd[p].lam2 = ps.lam[p] + ps.lam[p];
+    pd[p].hdt = 0.5 * ps.dt[p];
+  }
+  if (!ps.d_patches) NEBO_CUDA_TRY(cudaMalloc((void**)&ps.d_patches, sizeof(PatchDev) * ps.npatch));
+  NEBO_CUDA_TRY(cudaMemcpyAsync(ps.d_patches, pd.data(), sizeof(PatchDev) * ps.npatch, cudaMemcpyHostToDevice, s));
+  cudaFree(ps.d_items);
+  ps.d_items = nullptr;
+  NEBO_CUDA_TRY(cudaMalloc((void**)&ps.d_items, sizeof(WorkItem) * std::max<size_t>(1, items.size())));
+  NEBO_CUDA_TRY(cudaMemcpyAsync(ps.d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, s));
+  NEBO_CUDA_TRY(cudaStreamSynchronize(s));
+  ps.nitems = (int)items.size();
+  for (auto& kv : ps.graphs) cudaGraphExecDestroy(kv.second);
+  ps.graphs.clear();
+  return NEBO_OK;
+}
+
+int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parity, cudaStream_t s) {
+  if (nitems == 0) return NEBO_OK;
+  LaunchScope ls(ps.dtype == NEBO_F64 ? "patches_step_f64" : "patches_step_f32", s);
+  const int grid = std::min(nitems, ps.grid);
+  if (ps.dtype == NEBO_F64)
+    patches_step_kernel<double><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
+                                                            (const double*)ps.arena[parity], (double*)ps.arena[parity ^ 1]);
+  else
+    patches_step_kernel<float><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, (const float*)ps.arena[parity],
+                                                           (float*)ps.arena[parity ^ 1]);
+  NEBO_LAUNCH_CHECK("nebo_patchset_run");
+  return NEBO_OK;
+}
+
+int default_log2tx(int nx) { return nx <= 16 ? 4 : (nx <= 40 ? 5 : 6); }
+
+}  // namespace
+}  // namespace nebo
+
+using namespace nebo;
+
+struct nebo_patchset : PatchSet {};
+
+extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32_t* shapes, const double* lam,
+                                    const double* dt, int dtype) {
+  if (!out || npatch <= 0 || !shapes || !lam || !dt)
+    return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: bad arguments");
+  if (dtype != NEBO_F64 && dtype != NEBO_F32) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: dtype");
+  *out = nullptr;
+  nebo_patchset* ps = new nebo_patchset();
+  ps->npatch = npatch;
+  ps->dtype = dtype;
+  ps->shape.assign(shapes, shapes + 3 * npatch);
+  ps->lam.assign(lam, lam + npatch);
+  ps->dt.assign(dt, dt + npatch);
+  ps->offset.resize(npatch);
+  ps->log2tx.resize(npatch);
+  long long off = 0;
+  for (int p = 0; p < npatch; ++p) {
+    const int nx = shapes[3 * p], ny = shapes[3 * p + 1], nz = shapes[3 * p + 2];
+    if (nx < 2 || ny < 2 || nz < 2) {
+      delete ps;
+      return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: patch %d has an edge below 2", p);
+    }
+    ps->offset[p] = off;
+    off += (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    off = (off + 31) & ~31LL;  // 256-byte aligned windows
+    ps->log2tx[p] = default_log2tx(nx);
+  }
+  ps->total = off;
+  const size_t bytes = (size_t)off * elem_size(dtype);
+  cudaError_t e = cudaMalloc(&ps->arena[0], bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&ps->arena[1], bytes);
+  if (e == cudaSuccess) e = cudaMemset(ps->arena[0], 0, bytes);
+  if (e == cudaSuccess) e = cudaMemset(ps->arena[1], 0, bytes);
+  if (e != cudaSuccess) {
+    delete ps;
+    return cuda_fail(e, "nebo_patchset_create");
+  }
+  ps->grid = num_sms() * 8;
+  std::vector<int> all(npatch);
+  for (int p = 0; p < npatch; ++p) all[p] = p;
+  int rc = upload_tables(*ps, build_items(*ps, all, ps->zchunk), 0);
+  if (rc) {
+    delete ps;
+    return rc;
+  }
+  *out = ps;
+  return NEBO_OK;
+}
+
+extern "C" int nebo_patchset_destroy(nebo_patchset* ps) {
+  delete ps;
+  return NEBO_OK;
+}
+
+extern "C" int nebo_patchset_info(const nebo_patchset* ps, int64_t* total_elems, int64_t* offsets, int32_t* log2tx,
+                                  int32_t* nitems) {
+  if (!ps) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_info: null handle");
+  if (total_elems) *total_elems = ps->total;
+  for (int p = 0; p < ps->npatch; ++p) {
+    if (offsets) offsets[p] = ps->offset[p];
+    if (log2tx) log2tx[p] = ps->log2tx[p];
+  }
+  if (nitems) *nitems = ps->nitems;
+  return NEBO_OK;
+}
+
+extern "C" void* nebo_patchset_arena(const nebo_patchset* ps, int which) {
+  return (ps && (which == 0 || which == 1)) ? ps->arena[which] : nullptr;
+}
+
+// Every patch's ghosts take their periodic images (run once after filling arena 0).
+extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, nebo_stream_t stream) {
+  if (!ps || (which != 0 && which != 1)) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_fill_ghosts");
+  for (int p = 0; p < ps->npatch; ++p) {
+    nebo_field f;
+    f.data = (char*)ps->arena[which] + ps->offset[p] * elem_size(ps->dtype);
+    for (int i = 0; i < 3; ++i) {
+      f.glob[i] = f.extent[i] = ps->shape[3 * p + i] + 2;
+      f.offset[i] = 0;
+      f.ghost_minus[i] = f.ghost_plus[i] = 1;
+      f.has_bc[i] = f.bc_extra[i] = 0;
+    }
+    f.dtype = ps->dtype;
+    int rc = nebo::fill_periodic_any(&f, (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  return NEBO_OK;
+}
+
+// Time each tile width on the patches of each x-extent class and keep the fastest.
+extern "C" int nebo_patchset_autotune(nebo_patchset* ps, nebo_stream_t stream, int32_t* chosen_log2tx) {
+  if (!ps) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_autotune: null handle");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::map<int, std::vector<int>> classes;  // class by nx bucket of 8
+  for (int p = 0; p < ps->npatch; ++p) classes[(ps->shape[3 * p] + 7) / 8].push_back(p);
+  cudaEvent_t a, b;
+  NEBO_CUDA_TRY(cudaEventCreate(&a));
+  NEBO_CUDA_TRY(cudaEventCreate(&b));
+  WorkItem* d_tmp = nullptr;
+  int rc = NEBO_OK;
+  for (auto& kv : classes) {
+    float best = 1e30f;
+    int bestl = default_log2tx(ps->shape[3 * kv.second[0]]);
+    for (int l = 4; l <= 6 && !rc; ++l) {
+      for (int p : kv.second) ps->log2tx[p] = l;
+      std::vector<WorkItem> items = build_items(*ps, kv.second, ps->zchunk);
+      cudaFree(d_tmp);
+      d_tmp = nullptr;
+      if (cudaMalloc((void**)&d_tmp, sizeof(WorkItem) * items.size()) != cudaSuccess) { rc = NEBO_ERR_ALLOC; break; }
+      cudaMemcpyAsync(d_tmp, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, s);
+      // patch table must carry the candidate tile width
+      std::vector<int> keep = ps->log2tx;
+      rc = upload_tables(*ps, std::vector<WorkItem>(), s);
+      if (rc) break;
+      float ms = 0.f;
+      for (int rep = 0; rep < 4 && !rc; ++rep) {
+        cudaEventRecord(a, s);
+        rc = launch_step(*ps, d_tmp, (int)items.size(), rep & 1, s);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, b);
+        if (rep > 0) ms += t;  // first launch warms up
+      }
+      if (ms < best) {
+        best = ms;
+        bestl = l;
+      }
+    }
+    for (int p : kv.second) ps->log2tx[p] = bestl;
+  }
+  cudaFree(d_tmp);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  std::vector<int> all(ps->npatch);
+  for (int p = 0; p < ps->npatch; ++p) all[p] = p;
+  rc = upload_tables(*ps, build_items(*ps, all, ps->zchunk), s);
+  if (rc) return rc;
+  if (chosen_log2tx)
+    for (int p = 0; p < ps->npatch; ++p) chosen_log2tx[p] = ps->log2tx[p];
+  // the timing runs overwrote the arenas: callers autotune before loading data
+  return NEBO_OK;
+}
+
+// steps time steps starting from arena `start`; returns (via *final) the arena holding the result.
+extern "C" int nebo_patchset_run(nebo_patchset* ps, int start, int steps, int use_graph, int* final_arena,
+                                 nebo_stream_t stream) {
+  if (!ps || (start != 0 && start != 1) || steps < 0) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_run");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (final_arena) *final_arena = (start + steps) & 1;
+  if (steps == 0) return NEBO_OK;
+  if (!use_graph) {
+    for (int k = 0; k < steps; ++k) {
+      int rc = launch_step(*ps, ps->d_items, ps->nitems, (start + k) & 1, s);
+      if (rc) return rc;
+    }
+    return NEBO_OK;
+  }
+  const std::pair<int, int> key(steps, start);
+  auto it = ps->graphs.find(key);
+  if (it == ps->graphs.end()) {
+    cudaStream_t cap;
+    NEBO_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    NEBO_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int rc = NEBO_OK;
+    for (int k = 0; k < steps && !rc; ++k) rc = launch_step(*ps, ps->d_items, ps->nitems, (start + k) & 1, cap);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "nebo_patchset_run capture");
+    cudaGraphExec_t exec;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "nebo_patchset_run instantiate");
+    it = ps->graphs.emplace(key, exec).first;
+  }
+  NEBO_CUDA_TRY(cudaGraphLaunch(it->second, s));
+  return NEBO_OK;
+}
