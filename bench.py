@@ -45,10 +45,14 @@ BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
     "heat": 8 * 3,                   # T, lambda read, T' written
     "heat32": 4 * 3,
     "patches": 8 * 2,    # T read, T' written (lambda is a scalar per patch)
-    "patches32": 4 * 2,
+    "patches32": 4 * 2 + 8 * 2,  # FP32 copy read+written, FP64 state read+written
+    # one RK stage: phi (stencil) + u,v,w,lambda read, state accumulation read/written
+    "transport": 8 * 5 + 8 + 8,            # FP64: phi, u, v, w, lam, acc read; out written
+    "transport32": 4 * 5 + 8 + 8 + 4,      # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
 }
 DOMINANT = {"deep": "deep_chain", "heat": "heat_step_f64", "heat32": "heat_step_f32",
-            "patches": "patches_step_f64", "patches32": "patches_step_f32"}
+            "patches": "patches_step_f64", "patches32": "patches_step_f32",
+            "transport": "transport_stage_f64", "transport32": "transport_stage_f32"}
 
 
 def measured_peak_hbm():
@@ -223,12 +227,12 @@ class Patches:
         ins = W.patch_inputs(shapes)
         self.ps = N.PatchSet(shapes, np.array([t[0] for t in ins]), np.array([t[2] for t in ins]), dtype)
         self.ps.autotune()
-        tdt = torch.float64 if dtype == "f64" else torch.float32
-        self.host = torch.zeros(self.ps.total, dtype=tdt).pin_memory()
+        self.host = torch.zeros(self.ps.total, dtype=torch.float64).pin_memory()
         for p, (_, T0, _) in enumerate(ins):
             o = int(self.ps.offsets[p])
             self.host[o:o + T0.size].copy_(torch.from_numpy(T0.reshape(-1)))
         self.ps.arena(0).copy_(self.host)
+        self.ps.fill_ghosts(0)
         self.cells = int(np.prod(shapes.astype(np.int64), axis=1).sum())
         self.launches_per_step = 1
         self.h2d_bytes = self.host.numel() * self.host.element_size()
@@ -246,12 +250,50 @@ class Patches:
 
     def step_e2e(self):
         self.ps.arena(0).copy_(self.host, non_blocking=True)
+        self.ps.fill_ghosts(0)
         self.parity = self.ps.run(1, start=0)
         self.red.copy_(self.ps.arena(self.parity)[:1].double(), non_blocking=True)
         self.host_red.copy_(self.red, non_blocking=True)
 
 
+class TransportWL:
+    """Scalar transport at n^3 + 2 ghosts; a step is one Heun RK2 step (two stage kernels)."""
+
+    def __init__(self, N, n, dtype):
+        import torch
+
+        from spatialops_gb300 import workloads as W
+
+        self.name = "transport" if dtype == "f64" else "transport32"
+        self.N, self.n = N, n
+        phi, u, v, w, lam, dt, nu = W.transport_inputs_device(n)
+        self.t = N.Transport(np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)),
+                             np.zeros((1, 1, 1)), n, dt, nu, dtype)
+        tdt = torch.float64 if dtype == "f64" else torch.float32
+        self.t.phi = phi
+        self.t.coef = [q.to(tdt).contiguous() for q in (u, v, w, lam)]
+        self.host = [phi.cpu().pin_memory()]
+        self.cells = n ** 3
+        self.launches_per_step = 2
+        self.h2d_bytes = self.host[0].numel() * 8
+        self.d2h_bytes = 8
+        self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
+        self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
+        self.phi_field = N.Field("SVol", n, 2, tensor=self.t.phi)
+
+    def step(self):
+        self.t.run(1)
+
+    def step_e2e(self):
+        self.t.phi.copy_(self.host[0], non_blocking=True)
+        self.t.run(1)
+        self.N.reduce_all(self.phi_field, True, self.red)  # FP64 reductions of the FP64 state
+        self.host_red.copy_(self.red, non_blocking=True)
+
+
 def make_workload(N, name, n):
+    if name in ("transport", "transport32"):
+        return TransportWL(N, n, "f64" if name == "transport" else "f32")
     if name in ("patches", "patches32"):
         return Patches(N, "f64" if name == "patches" else "f32")
     if name == "deep":
@@ -338,7 +380,8 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="deep", choices=["deep", "heat", "heat32", "patches", "patches32"])
+    ap.add_argument("--workload", default="deep", choices=["deep", "heat", "heat32", "patches", "patches32", "transport",
+                                                             "transport32"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -452,7 +495,7 @@ def main():
     line = {
         "metric": f"{W.name} cell-updates/s", "value": value, "unit": "Gcell-upd/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if W.name == "heat32" else "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if W.name.endswith("32") else "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": f"{W.name} {args.n}^3 + 1 ghost", "cells_per_step": W.cells,
                    "parallelism": f"replicas x{world}",

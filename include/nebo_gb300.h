@@ -161,9 +161,12 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
  * and a work list of (patch, tile, z-chunk) items; nebo_patchset_run captures the steps in a
  * CUDA graph.  The reference advances such patches one `<<=` at a time from the caller's patch
  * loop (one gpu_assign_kernel launch per expression and patch, spatialops/NeboLhs.h:29-41).
- *   create:   shapes = 3 ints per patch (interior nx, ny, nz >= 2); allocates two arenas holding
- *             every patch window (x fastest), returned by nebo_patchset_arena(ps, 0|1); the
- *             element offset of each window comes from nebo_patchset_info.
+ *   create:   shapes = 3 ints per patch (interior nx, ny, nz >= 2); allocates two FP64 state
+ *             arenas holding every patch window (x fastest), returned by nebo_patchset_arena(ps,
+ *             0|1); the element offset of each window comes from nebo_patchset_info.  dtype
+ *             NEBO_F32 adds FP32 copies that the stencil sweeps read and write (FP32 storage and
+ *             arithmetic on the sweeps, FP64 accumulation of the state).
+ *   fill_ghosts: periodic ghost images of an arena (and its FP32 copy); call after loading.
  *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest (clobbers
  *             the arenas: call it before loading data).
  *   run:      `steps` steps from arena `start`; *final_arena says where the result is.
@@ -179,6 +182,39 @@ int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, nebo_stream_t 
 int nebo_patchset_autotune(nebo_patchset* ps, nebo_stream_t stream, int32_t* chosen_log2_tile_x);
 int nebo_patchset_run(nebo_patchset* ps, int start, int steps, int use_graph, int* final_arena,
                       nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ scalar transport
+ * Heun RK2 steps of  d(phi)/dt = sum_d Grad_{d->S}( nu*Interp(lambda)*G4_d(phi)
+ *                                                  - u_d*cond(u_d > 0, phi[i-1])(phi[i]) )
+ * on an n^3 periodic SVol patch with two ghost layers (G4: 4th-order staggered gradient
+ * {1,-27,27,-1}/24 at (-2,-1,0,+1); unit spacing).  phi: FP64 state window, updated in place.
+ * u, v, w (XVol/YVol/ZVol face velocities) and lambda: windows of the same shape in `dtype`.
+ * dtype NEBO_F32: FP32 storage and stencil arithmetic, FP64 time accumulation (phi stays FP64);
+ * dtype NEBO_F64: everything FP64.  work: device scratch of nebo_transport_work_bytes bytes.
+ * Each RK stage is one kernel. */
+size_t nebo_transport_work_bytes(int n, int dtype);
+int nebo_transport_run(double* phi, const void* u, const void* v, const void* w, const void* lam,
+                       int n, int steps, double dt, double nu, int dtype, void* work,
+                       nebo_stream_t stream);
+
+/* ------------------------------------------------------------------ adjoint (differentiation)
+ * No counterpart in the reference (it has no differentiation).  Gradients of
+ *   J = 1/2 * sum_interior (T_N - T_target)^2,   T_{k+1} = nebo_heat_step(T_k, lambda, dt)
+ * (unit spacing, periodic, one ghost layer, FP64) with respect to T_0 and lambda.
+ * nebo_heat_adjoint_step: one reverse step -- Aout = A_{k+1} + dt*R(lambda, A_{k+1}) (the
+ *   heat operator is self-adjoint on the periodic grid; the ghost fill's transpose folds ghost
+ *   contributions onto interior images) and glam -= (dt/2)*sum of face (dT*dA) terms at T_k.
+ *   Inputs need periodic ghost images (T_k, A_{k+1}, lambda); Aout gets images.
+ * nebo_heat_gradient: forward sweep keeping every L-th state (L = checkpoint_every, or
+ *   ceil(sqrt(steps)) when <= 0), then the reverse sweep recomputing each segment from its
+ *   checkpoint: device memory ~ (steps/L + L) fields.  Writes gT0 = dJ/dT_0 (window with
+ *   images), glam = dJ/dlambda (interior; ghosts zero) and *J. */
+int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ain, const nebo_field* Aout,
+                           const nebo_field* lam, const nebo_field* glam, double dt,
+                           nebo_stream_t stream);
+int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget,
+                       int steps, double dt, int checkpoint_every, const nebo_field* gT0,
+                       const nebo_field* glam, double* J, nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ launch accounting
  * Every kernel launch of this library is counted; with profiling on, each launch (outside

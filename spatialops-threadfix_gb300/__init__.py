@@ -82,6 +82,10 @@ SIGNATURES = [
     ("nebo_patchset_fill_ghosts", _I, [_P, _I, _P]),
     ("nebo_patchset_autotune", _I, [_P, _P, _P]),
     ("nebo_patchset_run", _I, [_P, _I, _I, _I, ctypes.POINTER(_I), _P]),
+    ("nebo_transport_work_bytes", ctypes.c_size_t, [_I, _I]),
+    ("nebo_transport_run", _I, [_P, _P, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
+    ("nebo_heat_adjoint_step", _I, [_FP, _FP, _FP, _FP, _FP, _D, _P]),
+    ("nebo_heat_gradient", _I, [_FP, _FP, _FP, _I, _D, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
     ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
@@ -291,7 +295,7 @@ class PatchSet:
         self.lam = np.ascontiguousarray(lam, dtype=np.float64)
         self.dt = np.ascontiguousarray(dt, dtype=np.float64)
         self.dtype = F64 if dtype == "f64" else F32
-        self.esize = 8 if self.dtype == F64 else 4
+        self.esize = 8  # arenas hold the FP64 states in both modes
         h = ctypes.c_void_p()
         _check(lib().nebo_patchset_create(ctypes.byref(h), self.npatch, ctypes.c_void_p(self.shapes.ctypes.data),
                                           ctypes.c_void_p(self.lam.ctypes.data), ctypes.c_void_p(self.dt.ctypes.data),
@@ -326,7 +330,7 @@ class PatchSet:
         class _CAI:
             pass
         obj = _CAI()
-        obj.__cuda_array_interface__ = {"shape": (self.total,), "typestr": "<f8" if self.dtype == F64 else "<f4",
+        obj.__cuda_array_interface__ = {"shape": (self.total,), "typestr": "<f8",
                                         "data": (ptr, False), "version": 3, "strides": None}
         del cls, nbytes
         return torch.as_tensor(obj, device="cuda")
@@ -351,3 +355,42 @@ class PatchSet:
         _check(lib().nebo_patchset_run(self.h, int(start), int(steps), int(use_graph), ctypes.byref(fin),
                                        _stream(stream)))
         return fin.value
+
+
+class Transport:
+    """Scalar transport state on the GPU (nebo_transport_run): phi FP64, coefficients in dtype."""
+
+    def __init__(self, phi0, u, v, w, lam, n, dt, nu, dtype="f32"):
+        import torch
+
+        self.n, self.dt, self.nu = n, dt, nu
+        self.dtype = F64 if dtype == "f64" else F32
+        tdt = torch.float64 if self.dtype == F64 else torch.float32
+        self.phi = torch.from_numpy(np.ascontiguousarray(phi0)).to(device="cuda", dtype=torch.float64)
+        self.coef = [torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=tdt) for a in (u, v, w, lam)]
+        nb = lib().nebo_transport_work_bytes(int(n), self.dtype)
+        self.work = torch.empty(nb, dtype=torch.uint8, device="cuda")
+
+    def run(self, steps, stream=None):
+        c = [ctypes.c_void_p(t.data_ptr()) for t in self.coef]
+        _check(lib().nebo_transport_run(ctypes.c_void_p(self.phi.data_ptr()), c[0], c[1], c[2], c[3], int(self.n),
+                                        int(steps), float(self.dt), float(self.nu), self.dtype,
+                                        ctypes.c_void_p(self.work.data_ptr()), _stream(stream)))
+
+
+def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None):
+    """(J, dJ/dT0, dJ/dlambda) for J = 1/2 sum (T_N - T_target)^2 (fields: SVol, 1 ghost, FP64)."""
+    gT = Field(T0.loc, T0.n, T0.ghost)
+    gl = Field(T0.loc, T0.n, T0.ghost)
+    J = ctypes.c_double()
+    a, b, c, d, e = T0.desc(), lam.desc(), Ttarget.desc(), gT.desc(), gl.desc()
+    _check(lib().nebo_heat_gradient(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt),
+                                    int(checkpoint_every), ctypes.byref(d), ctypes.byref(e), ctypes.byref(J),
+                                    _stream(stream)))
+    return J.value, gT, gl
+
+
+def heat_adjoint_step(Tk, Ain, Aout, lam, glam, dt, stream=None):
+    a, b, c, d, e = Tk.desc(), Ain.desc(), Aout.desc(), lam.desc(), glam.desc()
+    _check(lib().nebo_heat_adjoint_step(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d),
+                                        ctypes.byref(e), float(dt), _stream(stream)))

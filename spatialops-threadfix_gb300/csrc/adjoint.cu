@@ -1,0 +1,273 @@
+// Adjoint of the fused heat step (no counterpart in the reference, which has no differentiation):
+// gradients of  J = 1/2 * sum_interior (T_N - T_target)^2  with respect to T_0 and lambda, for
+// T_{k+1} = T_k + dt * sum_d Div_d(Interp_d(lambda) * Grad_d(T_k)) on a periodic SVol patch with
+// one ghost layer and unit spacing (the forward step is nebo_heat_step's, bit-exact FP64).
+//
+// Reverse step (abar' = dJ/dT_{k+1}, both with periodic ghost images):
+//   abar[c]  = abar'[c] + dt * sum_d ( lf[c+s] (abar'[c+s]-abar'[c]) - lf[c] (abar'[c]-abar'[c-s]) )
+//              -- the forward operator applied to abar' (it is self-adjoint on the periodic
+//                 grid; the ghost fill's transpose folds ghost contributions onto their
+//                 interior images, which the periodic ghost reads express);
+//   glam[c] -= (dt/2) * sum_d ( (T[c]-T[c-s])(abar'[c]-abar'[c-s]) + (T[c+s]-T[c])(abar'[c+s]-abar'[c]) )
+//              -- lambda[c] enters the face coefficients lf[c] and lf[c+s] with weight 1/2.
+// One kernel per reverse step computes both, with every face quantity computed once and shared
+// through shared memory (x, y) or carried in a register (z), and writes abar's ghost images.
+//
+// Memory: sqrt(N) checkpointing.  The forward sweep keeps T at every L-th step (L = ceil(sqrt N));
+// the reverse sweep recomputes each segment's L states from its checkpoint into a segment buffer
+// and walks it backwards, so device memory grows like 2*sqrt(N) fields, not N.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace nebo {
+namespace {
+
+constexpr int BX = 32;
+constexpr int BY = 8;
+
+__device__ __forceinline__ void store_images1(double* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
+                                              double v) {
+  int xs[3], ys[3], zs[3];
+  int cx = 0, cy = 0, cz = 0;
+  xs[cx++] = x;
+  if (x == 0) xs[cx++] = nx;
+  if (x == nx - 1) xs[cx++] = -1;
+  ys[cy++] = y;
+  if (y == 0) ys[cy++] = ny;
+  if (y == ny - 1) ys[cy++] = -1;
+  zs[cz++] = z;
+  if (z == 0) zs[cz++] = nz;
+  if (z == nz - 1) zs[cz++] = -1;
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+}
+
+struct Face {
+  double fa;  // (lam_a + lam_b) * (abar_b - abar_a)
+  double p;   // (T_b - T_a) * (abar_b - abar_a)
+};
+
+__device__ __forceinline__ Face face(const double* T, const double* A, const double* L, long a, long b) {
+  const double da = A[b] - A[a];
+  Face f;
+  f.fa = (__ldg(L + a) + __ldg(L + b)) * da;
+  f.p = (__ldg(T + b) - __ldg(T + a)) * da;
+  return f;
+}
+
+__global__ void __launch_bounds__(BX* BY) heat_adjoint_kernel(const double* __restrict__ T, const double* __restrict__ Ain,
+                                                              double* __restrict__ Aout, const double* __restrict__ L,
+                                                              double* __restrict__ glam, int sy, long sz, int nx, int ny,
+                                                              int nz, int zchunk, double hdt) {
+  __shared__ Face sfx[2][BY][BX + 1];
+  __shared__ Face sfy[2][BY + 1][BX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, nz);
+  const bool active = x < nx && y < ny;
+  const int xc = min(x, nx), yc = min(y, ny);
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+  Face fzlo = face(T, Ain, L, at(xc, yc, z0 - 1), at(xc, yc, z0));
+  for (int z = z0; z < z1; ++z) {
+    const int buf = z & 1;
+    const long c = at(xc, yc, z);
+    const Face fzhi = face(T, Ain, L, c, c + sz);
+    const Face fx = face(T, Ain, L, c - 1, c);
+    const Face fy = face(T, Ain, L, c - sy, c);
+    sfx[buf][ty][tx] = fx;
+    sfy[buf][ty][tx] = fy;
+    if (ty == 0) {
+      const int yh = y0 + BY;
+      if (yh <= ny && x <= nx) sfy[buf][BY][tx] = face(T, Ain, L, at(xc, yh - 1, z), at(xc, yh, z));
+    } else if (ty == 1 && tx < BY) {
+      const int xh = x0 + BX, yr = y0 + tx;
+      if (xh <= nx && yr < ny) sfx[buf][tx][BX] = face(T, Ain, L, at(xh - 1, yr, z), at(xh, yr, z));
+    }
+    __syncthreads();
+    if (active) {
+      const Face fxhi = sfx[buf][ty][tx + 1], fyhi = sfy[buf][ty + 1][tx];
+      const double s = ((fxhi.fa - fx.fa) + (fyhi.fa - fy.fa)) + (fzhi.fa - fzlo.fa);
+      const double ps = ((fx.p + fxhi.p) + (fy.p + fyhi.p)) + (fzlo.p + fzhi.p);
+      store_images1(Aout, sy, sz, x, y, z, nx, ny, nz, Ain[c] + hdt * s);
+      glam[c] -= hdt * ps;
+    }
+    fzlo = fzhi;
+  }
+}
+
+// abar_N = T_N - T_target on the interior (+ images); per-block partial sums of (T_N - T_target)^2.
+__global__ void loss_seed_kernel(const double* __restrict__ T, const double* __restrict__ Tt, double* __restrict__ A,
+                                 int sy, long sz, int nx, int ny, int nz, double* __restrict__ partial) {
+  double acc = 0.0;
+  const long total = (long)nx * ny * nz;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+    const long c = (long)x + (long)sy * y + sz * z;
+    const double d = T[c] - Tt[c];
+    acc = fma(d, d, acc);
+    store_images1(A, sy, sz, x, y, z, nx, ny, nz, d);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) t += sh[i];
+    partial[blockIdx.x] = t;
+  }
+}
+
+}  // namespace
+
+int heat_step_dispatch(const nebo_field* T, const nebo_field* To, const nebo_field* L, double dt, const double sp[3],
+                       cudaStream_t s);  // heat.cu
+
+}  // namespace nebo
+
+using namespace nebo;
+
+// One reverse step (exposed for tests): Aout, glam from T_k, A_{k+1}; all windows one ghost
+// layer, same shape; A_{k+1} and T_k must hold periodic ghost images (lam too).
+extern "C" int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ain, const nebo_field* Aout,
+                                      const nebo_field* lam, const nebo_field* glam, double dt, nebo_stream_t stream) {
+  const nebo_field* fs[5] = {Tk, Ain, Aout, lam, glam};
+  for (int i = 0; i < 5; ++i) {
+    int rc = check_field(fs[i], "nebo_heat_adjoint_step");
+    if (rc) return rc;
+    if (fs[i]->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_heat_adjoint_step: FP64 only");
+    if ((rc = check_periodic_patch(fs[i], 1, "nebo_heat_adjoint_step"))) return rc;
+    if (i && (rc = check_same_layout(Tk, fs[i], "nebo_heat_adjoint_step"))) return rc;
+  }
+  int n[3];
+  interior_extent(*Tk, n);
+  const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
+                     vl = make_view<double>(*lam), vg = make_view<double>(*glam);
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
+  chunks = chunks < 1 ? 1 : (chunks > (n[2] + 7) / 8 ? (n[2] + 7) / 8 : chunks);
+  const int zchunk = (n[2] + chunks - 1) / chunks;
+  chunks = (n[2] + zchunk - 1) / zchunk;
+  cudaStream_t s = (cudaStream_t)stream;
+  LaunchScope ls("heat_adjoint_step", s);
+  heat_adjoint_kernel<<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(vt.base, va.base, vo.base, vl.base, vg.base,
+                                                                        vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
+  NEBO_LAUNCH_CHECK("nebo_heat_adjoint_step");
+  return NEBO_OK;
+}
+
+namespace {
+int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const nebo_field* T0, const nebo_field* lam,
+                  const nebo_field* Ttarget, int steps, double dt, const nebo_field* gT0, const nebo_field* glam,
+                  double* J, nebo_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = cells * sizeof(double);
+  auto buf = [&](size_t i) { return pool + i * cells; };
+  double* partial = pool + (size_t)nbuf * cells;
+  auto field_at = [&](double* p) {
+    nebo_field f = *T0;
+    f.data = p;
+    return f;
+  };
+  const double unit[3] = {1.0, 1.0, 1.0};
+  int rc = NEBO_OK;
+  nebo_field lamf = *lam;
+  // lambda's ghosts must be periodic images (they are read at boundary faces)
+  if ((rc = fill_periodic_any(&lamf, s))) return rc;
+  // forward sweep with checkpoints
+  NEBO_CUDA_TRY(cudaMemcpyAsync(buf(0), T0->data, bytes, cudaMemcpyDeviceToDevice, s));
+  {
+    nebo_field c0 = field_at(buf(0));
+    if ((rc = fill_periodic_any(&c0, s))) return rc;
+  }
+  {
+    double* tmp = buf(nbuf - 1);
+    double* cur = buf(0);
+    for (int k = 0; k < steps && !rc; ++k) {
+      double* nxt = ((k + 1) % L == 0 && (k + 1) / L < nck) ? buf((k + 1) / L) : (cur == tmp ? buf(nbuf - 2) : tmp);
+      nebo_field a = field_at(cur), b = field_at(nxt);
+      rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
+      cur = nxt;
+    }
+    if (rc) return rc;
+    // seed: abar_N = T_N - T_target, J
+    double* A0 = buf(nck + L);
+    double* A1 = buf(nck + L + 1);
+    const View<double> vt = make_view<double>(field_at(cur));
+    const View<double> vtt = make_view<double>(*Ttarget);
+    const View<double> va = make_view<double>(field_at(A0));
+    int n[3];
+    interior_extent(*T0, n);
+    {
+      LaunchScope ls("loss_seed", s);
+      loss_seed_kernel<<<256, 256, 0, s>>>(vt.base, vtt.base, va.base, vt.sy, vt.sz, n[0], n[1], n[2], partial);
+    }
+    NEBO_CUDA_TRY(cudaGetLastError());
+    double hp[256];
+    NEBO_CUDA_TRY(cudaMemcpyAsync(hp, partial, sizeof(hp), cudaMemcpyDeviceToHost, s));
+    NEBO_CUDA_TRY(cudaMemsetAsync(glam->data, 0, bytes, s));
+    // reverse sweep, segment by segment
+    double* Ain = A0;
+    double* Aout = A1;
+    for (int seg = nck - 1; seg >= 0 && !rc; --seg) {
+      const int k0 = seg * L, k1 = (k0 + L < steps) ? k0 + L : steps;  // states k0 .. k1-1
+      // recompute states k0+1 .. k1-1 into the segment buffers (state k0 is the checkpoint)
+      for (int k = k0; k + 1 < k1 && !rc; ++k) {
+        nebo_field a = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
+        nebo_field b = field_at(buf(nck + (k - k0)));
+        rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
+      }
+      for (int k = k1 - 1; k >= k0 && !rc; --k) {
+        nebo_field tk = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
+        nebo_field ai = field_at(Ain), ao = field_at(Aout);
+        rc = nebo_heat_adjoint_step(&tk, &ai, &ao, &lamf, glam, dt, stream);
+        double* t = Ain;
+        Ain = Aout;
+        Aout = t;
+      }
+    }
+    if (rc) return rc;
+    NEBO_CUDA_TRY(cudaMemcpyAsync(gT0->data, Ain, bytes, cudaMemcpyDeviceToDevice, s));
+    NEBO_CUDA_TRY(cudaStreamSynchronize(s));
+    if (J) {
+      double t = 0.0;
+      for (int i = 0; i < 256; ++i) t += hp[i];
+      *J = 0.5 * t;
+    }
+  }
+  return rc;
+}
+}  // namespace
+
+// Full gradient with sqrt(N) checkpointing.  T0, lam, Ttarget: windows (1 ghost, periodic patch);
+// gT0, glam: outputs (windows; interiors written, glam overwritten); J: host result.
+// checkpoint_every <= 0 selects ceil(sqrt(steps)).
+extern "C" int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
+                                  double dt, int checkpoint_every, const nebo_field* gT0, const nebo_field* glam,
+                                  double* J, nebo_stream_t stream) {
+  const nebo_field* fs[5] = {T0, lam, Ttarget, gT0, glam};
+  for (int i = 0; i < 5; ++i) {
+    int rc = check_field(fs[i], "nebo_heat_gradient");
+    if (rc) return rc;
+    if (fs[i]->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_heat_gradient: FP64 only");
+    if ((rc = check_periodic_patch(fs[i], 1, "nebo_heat_gradient"))) return rc;
+    if (i && (rc = check_same_layout(T0, fs[i], "nebo_heat_gradient"))) return rc;
+  }
+  if (steps < 1) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_heat_gradient: steps < 1");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
+  const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
+  const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
+  const size_t bytes = cells * sizeof(double);
+  // device memory: nck checkpoints + L segment states + 2 adjoint buffers + 1 forward temp
+  const size_t nbuf = (size_t)nck + (size_t)L + 3;
+  double* pool = nullptr;
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&pool, nbuf * bytes + 1024 * sizeof(double), s));
+  const int rc = gradient_impl(pool, cells, nck, L, (int)nbuf, T0, lam, Ttarget, steps, dt, gT0, glam, J, stream);
+  cudaFreeAsync(pool, s);
+  return rc;
+}

@@ -226,6 +226,12 @@ std::map<GraphKey, cudaGraphExec_t> g_graphs;
 
 }  // namespace
 
+// Launch one heat step with no argument checks (callers inside the library have checked).
+int heat_step_dispatch(const nebo_field* T, const nebo_field* To, const nebo_field* L, double dt, const double sp[3],
+                       cudaStream_t s) {
+  return heat_step_any(T, To, L, dt, sp, s);
+}
+
 }  // namespace nebo
 
 using namespace nebo;

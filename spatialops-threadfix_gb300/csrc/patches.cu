@@ -5,7 +5,9 @@
 // The reference advances patches one `<<=` at a time from the caller's patch loop (Uintah/
 // Wasatch-style; spatialops/NeboLhs.h:29-41 launches a 16x16 grid per expression), paying a
 // launch and a tail per patch and expression.  Here:
-//   * all patches live in one arena per buffer (FP64 or FP32), each a ghosted window, x fastest;
+//   * all patches live in one arena per buffer, each a ghosted window, x fastest: the FP64 states,
+//     plus, in FP32 mode, FP32 copies that the stencil sweeps read (the state itself is still
+//     accumulated in FP64, so rounding to FP32 never compounds from step to step);
 //   * a work list enumerates (patch, x-tile, y-tile, z-chunk) items; a fixed grid of blocks
 //     (a multiple of the SM count) strides through it, so small and large patches share SMs;
 //   * tiles are TX x TY = 256 cells per plane with TX in {16, 32, 64} per patch (the autotuner
@@ -85,10 +87,15 @@ __device__ __forceinline__ void store_images(T* base, int sy, long sz, int x, in
 }
 
 // One persistent launch = one time step of every patch.
-template <typename T>
+// FP64 mode (ACC = false, T = double): src/dst are the FP64 states.
+// FP32 mode (ACC = true, T = float): src/dst are FP32 stencil copies; the time-integrated state
+// is accumulated in FP64 (acc_src -> acc_dst), and both the copy and the state get ghost images.
+template <typename T, bool ACC>
 __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev* __restrict__ patches,
                                                                   const WorkItem* __restrict__ items, int nitems,
-                                                                  const T* __restrict__ src, T* __restrict__ dst) {
+                                                                  const T* __restrict__ src, T* __restrict__ dst,
+                                                                  const double* __restrict__ acc_src,
+                                                                  double* __restrict__ acc_dst) {
   __shared__ T sfx[2][PT_MAX_TY * (PT_MAX_TX + 1) / 4 + 64];  // TY*(TX+1) <= 16*17, 8*33, 4*65
   __shared__ T sfy[2][(PT_MAX_TY + 1) * 16 + 64];            // (TY+1)*TX <= 17*16, 9*32, 5*64
   const int tid = threadIdx.x;
@@ -131,7 +138,14 @@ __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev
         const T fxhi = sfx[buf][ty * (TX + 1) + tx + 1];
         const T fyhi = sfy[buf][(ty + 1) * TX + tx];
         const T s = exact_add(exact_add(exact_sub(fxhi, fx), exact_sub(fyhi, fy)), exact_sub(fzhi, fzlo));
-        store_images(tout, sy, sz, x, y, z, nx, ny, nz, exact_add(tc, exact_mul(hdt, s)));
+        if (ACC) {
+          const long c = P.offset + interior + at(x, y, z);
+          const double v = acc_src[c] + P.hdt * (double)s;
+          store_images(acc_dst + P.offset + interior, sy, sz, x, y, z, nx, ny, nz, v);
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, (T)v);
+        } else {
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, exact_add(tc, exact_mul(hdt, s)));
+        }
       }
       tc = tn;
       fzlo = fzhi;
@@ -150,7 +164,8 @@ struct PatchSet {
   std::vector<double> lam, dt;
   std::vector<int> log2tx;
   long long total = 0;  // elements per arena
-  void* arena[2] = {nullptr, nullptr};
+  void* arena[2] = {nullptr, nullptr};    // FP64 states
+  float* arena32[2] = {nullptr, nullptr};  // FP32 stencil copies (FP32 mode)
   PatchDev* d_patches = nullptr;
   WorkItem* d_items = nullptr;
   int nitems = 0;
@@ -161,6 +176,8 @@ struct PatchSet {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     cudaFree(arena[0]);
     cudaFree(arena[1]);
+    cudaFree(arena32[0]);
+    cudaFree(arena32[1]);
     cudaFree(d_patches);
     cudaFree(d_items);
   }
@@ -211,16 +228,22 @@ int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parit
   LaunchScope ls(ps.dtype == NEBO_F64 ? "patches_step_f64" : "patches_step_f32", s);
   const int grid = std::min(nitems, ps.grid);
   if (ps.dtype == NEBO_F64)
-    patches_step_kernel<double><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
-                                                            (const double*)ps.arena[parity], (double*)ps.arena[parity ^ 1]);
+    patches_step_kernel<double, false><<<grid, PT_THREADS, 0, s>>>(
+        ps.d_patches, items, nitems, (const double*)ps.arena[parity], (double*)ps.arena[parity ^ 1], nullptr, nullptr);
   else
-    patches_step_kernel<float><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, (const float*)ps.arena[parity],
-                                                           (float*)ps.arena[parity ^ 1]);
+    patches_step_kernel<float, true><<<grid, PT_THREADS, 0, s>>>(
+        ps.d_patches, items, nitems, ps.arena32[parity], ps.arena32[parity ^ 1], (const double*)ps.arena[parity],
+        (double*)ps.arena[parity ^ 1]);
   NEBO_LAUNCH_CHECK("nebo_patchset_run");
   return NEBO_OK;
 }
 
 int default_log2tx(int nx) { return nx <= 16 ? 4 : (nx <= 40 ? 5 : 6); }
+
+__global__ void patches_cast_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
 
 }  // namespace
 }  // namespace nebo
@@ -256,11 +279,18 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
     ps->log2tx[p] = default_log2tx(nx);
   }
   ps->total = off;
-  const size_t bytes = (size_t)off * elem_size(dtype);
+  const size_t bytes = (size_t)off * sizeof(double);
   cudaError_t e = cudaMalloc(&ps->arena[0], bytes);
   if (e == cudaSuccess) e = cudaMalloc(&ps->arena[1], bytes);
   if (e == cudaSuccess) e = cudaMemset(ps->arena[0], 0, bytes);
   if (e == cudaSuccess) e = cudaMemset(ps->arena[1], 0, bytes);
+  if (dtype == NEBO_F32) {
+    const size_t b32 = (size_t)off * sizeof(float);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena32[0], b32);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena32[1], b32);
+    if (e == cudaSuccess) e = cudaMemset(ps->arena32[0], 0, b32);
+    if (e == cudaSuccess) e = cudaMemset(ps->arena32[1], 0, b32);
+  }
   if (e != cudaSuccess) {
     delete ps;
     return cuda_fail(e, "nebo_patchset_create");
@@ -303,16 +333,22 @@ extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, neb
   if (!ps || (which != 0 && which != 1)) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_fill_ghosts");
   for (int p = 0; p < ps->npatch; ++p) {
     nebo_field f;
-    f.data = (char*)ps->arena[which] + ps->offset[p] * elem_size(ps->dtype);
+    f.data = (double*)ps->arena[which] + ps->offset[p];
     for (int i = 0; i < 3; ++i) {
       f.glob[i] = f.extent[i] = ps->shape[3 * p + i] + 2;
       f.offset[i] = 0;
       f.ghost_minus[i] = f.ghost_plus[i] = 1;
       f.has_bc[i] = f.bc_extra[i] = 0;
     }
-    f.dtype = ps->dtype;
+    f.dtype = NEBO_F64;
     int rc = nebo::fill_periodic_any(&f, (cudaStream_t)stream);
     if (rc) return rc;
+  }
+  if (ps->dtype == NEBO_F32) {  // the FP32 stencil copy of the state
+    LaunchScope ls("patches_cast_f32", (cudaStream_t)stream);
+    patches_cast_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>((const double*)ps->arena[which],
+                                                                         ps->arena32[which], (size_t)ps->total);
+    NEBO_LAUNCH_CHECK("nebo_patchset_fill_ghosts");
   }
   return NEBO_OK;
 }

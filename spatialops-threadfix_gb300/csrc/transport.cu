@@ -1,0 +1,276 @@
+// Variable-coefficient scalar transport on a staggered mesh, Heun's RK2, periodic, two ghost
+// layers:  per direction d, on the faces of the SVol cells (XVol/YVol/ZVol locations),
+//   F_d = nu * Interp(lambda) * G4_d(phi) - u_d * cond(u_d > 0, phi[i-1])(phi[i])
+//   rhs = Grad_{X->S}(F_x) + Grad_{Y->S}(F_y) + Grad_{Z->S}(F_z)
+// with G4 the 4th-order staggered gradient {1, -27, 27, -1}/24 at points (-2,-1,0,+1), the
+// upwind value chosen by cond on the face velocity, Interp {1/2,1/2} at (-1,0) and the
+// divergence {-1, +1} at (0,+1) (user NeboStencilBuilder stencils of the reference's API,
+// spatialops/NeboStencilBuilder.h:85-152; the Nebo form is in oracle/ref/ref_driver.cpp).
+//
+// Precision modes (one template):
+//   FP32 storage: phi, u, v, w, lambda are float; the stencil arithmetic is float; the time
+//                 state is accumulated in an FP64 field (phi64), and a float copy of the state
+//                 is written for the next stencil sweep.  Reductions read phi64.
+//   FP64 storage: everything double (the plain path the FP32 form is measured against).
+// Each stage is ONE kernel: face fluxes computed once per face (low faces by each thread, high
+// faces through shared memory or carried in z), RK combination fused, periodic ghost images of
+// the stencil copy written in the same pass.
+#include "common.cuh"
+
+namespace nebo {
+namespace {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int G = 2;
+
+template <typename T>
+struct TrArgs {
+  const T* phi;      // stencil source (ghosts valid)
+  const double* acc; // FP64 state the stage advances from (phi64 for stage 1, phi1_64 for stage 2)
+  const double* base;  // stage 2: phi_n (FP64); unused in stage 1
+  double* out64;     // FP64 result (may alias the stencil copy in FP64 mode)
+  T* outS;           // stencil copy of the result with periodic images (FP32 mode), or nullptr
+  const T* u;
+  const T* v;
+  const T* w;
+  const T* lam;
+  int n, sy;
+  long sz;
+  T nu, q0, q1, q2, q3;  // nu and the G4 coefficients
+  double dt;
+};
+
+template <typename T>
+__device__ __forceinline__ T face_flux(const TrArgs<T>& a, long f, long s, const T* vel) {
+  const T* p = a.phi;
+  const T il = (__ldg(a.lam + f - s) + __ldg(a.lam + f)) * T(0.5);
+  const T g4 = ((__ldg(p + f - 2 * s) * a.q0 + __ldg(p + f - s) * a.q1) + __ldg(p + f) * a.q2) + __ldg(p + f + s) * a.q3;
+  const T uf = __ldg(vel + f);
+  const T up = (uf > T(0)) ? __ldg(p + f - s) : __ldg(p + f);
+  return a.nu * il * g4 - uf * up;
+}
+
+template <typename T>
+__device__ __forceinline__ void store_images2(T* base, int sy, long sz, int x, int y, int z, int n, T v) {
+  int xs[3], ys[3], zs[3];
+  int cx = 0, cy = 0, cz = 0;
+  xs[cx++] = x;
+  if (x < G) xs[cx++] = x + n;
+  if (x >= n - G) xs[cx++] = x - n;
+  ys[cy++] = y;
+  if (y < G) ys[cy++] = y + n;
+  if (y >= n - G) ys[cy++] = y - n;
+  zs[cz++] = z;
+  if (z < G) zs[cz++] = z + n;
+  if (z >= n - G) zs[cz++] = z - n;
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+}
+
+template <typename T, bool SECOND>
+__global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, int zchunk) {
+  __shared__ T sfx[2][TY][TX + 1];
+  __shared__ T sfy[2][TY + 1][TX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int n = a.n;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, n);
+  const bool active = x < n && y < n;
+  const int xc = min(x, n), yc = min(y, n);  // column/row n is a ghost: valid memory
+  const int sy = a.sy;
+  const long sz = a.sz;
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+  T fzlo = face_flux(a, at(xc, yc, z0), sz, a.w);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = z & 1;
+    const long c = at(xc, yc, z);
+    const T fzhi = face_flux(a, c + sz, sz, a.w);
+    const T fx = face_flux(a, c, 1, a.u);
+    const T fy = face_flux(a, c, sy, a.v);
+    sfx[buf][ty][tx] = fx;
+    sfy[buf][ty][tx] = fy;
+    if (ty == 0) {
+      const int yh = y0 + TY;
+      if (yh <= n && x <= n) sfy[buf][TY][tx] = face_flux(a, at(xc, yh, z), sy, a.v);
+    } else if (ty == 1 && tx < TY) {
+      const int xh = x0 + TX, yr = y0 + tx;
+      if (xh <= n && yr < n) sfx[buf][tx][TX] = face_flux(a, at(xh, yr, z), 1, a.u);
+    }
+    __syncthreads();
+    if (active) {
+      const T rhs = ((sfx[buf][ty][tx + 1] - fx) + (sfy[buf][ty + 1][tx] - fy)) + (fzhi - fzlo);
+      double r;
+      if (!SECOND)
+        r = a.acc[c] + a.dt * (double)rhs;
+      else
+        r = 0.5 * a.base[c] + 0.5 * (a.acc[c] + a.dt * (double)rhs);
+      if (a.outS) {
+        a.out64[c] = r;
+        store_images2(a.outS, sy, sz, x, y, z, n, (T)r);
+      } else {
+        store_images2(reinterpret_cast<T*>(a.out64), sy, sz, x, y, z, n, (T)r);
+      }
+    }
+    fzlo = fzhi;
+  }
+}
+
+__global__ void cast_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int cast_f64_to_f32(const double* a, float* b, size_t n, cudaStream_t s) {
+  LaunchScope ls("cast_f64_f32", s);
+  cast_f64_f32_kernel<<<num_sms() * 8, 256, 0, s>>>(a, b, n);
+  NEBO_LAUNCH_CHECK("nebo_transport_run (cast)");
+  return NEBO_OK;
+}
+
+template <typename T>
+int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
+  const int n = a.n;
+  const int gxb = (n + TX - 1) / TX, gyb = (n + TY - 1) / TY;
+  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
+  chunks = chunks < 1 ? 1 : (chunks > (n + 7) / 8 ? (n + 7) / 8 : chunks);
+  const int zchunk = (n + chunks - 1) / chunks;
+  chunks = (n + zchunk - 1) / zchunk;
+  dim3 grid(gxb, gyb, chunks), block(TX, TY);
+  LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
+  if (second)
+    transport_stage_kernel<T, true><<<grid, block, 0, s>>>(a, zchunk);
+  else
+    transport_stage_kernel<T, false><<<grid, block, 0, s>>>(a, zchunk);
+  NEBO_LAUNCH_CHECK("nebo_transport_run");
+  return NEBO_OK;
+}
+
+}  // namespace
+}  // namespace nebo
+
+using namespace nebo;
+
+// phi: state (FP64 window, 2 ghosts) in/out.  u, v, w, lam: windows of the storage dtype.
+// work: caller-provided device scratch of nebo_transport_work_bytes(n, dtype) bytes.
+extern "C" size_t nebo_transport_work_bytes(int n, int dtype) {
+  const size_t cells = (size_t)(n + 2 * G) * (n + 2 * G) * (n + 2 * G);
+  return cells * (2 * sizeof(double) + (dtype == NEBO_F32 ? 2 * sizeof(float) : 0)) + 1024;
+}
+
+extern "C" int nebo_transport_run(double* phi, const void* u, const void* v, const void* w, const void* lam, int n,
+                                  int steps, double dt, double nu, int dtype, void* work, nebo_stream_t stream) {
+  if (!phi || !u || !v || !w || !lam || !work || n < 2 * G || steps < 0)
+    return fail(NEBO_ERR_INVALID, "Nebo error in nebo_transport_run: bad arguments");
+  if (dtype != NEBO_F64 && dtype != NEBO_F32) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_transport_run: dtype");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int gl = n + 2 * G;
+  const size_t cells = (size_t)gl * gl * gl;
+  const long sy = gl, sz = (long)gl * gl;
+  const long interior = G + sy * G + sz * G;
+  char* wp = static_cast<char*>(work);
+  wp = (char*)(((uintptr_t)wp + 255) & ~(uintptr_t)255);
+  double* phi1 = reinterpret_cast<double*>(wp);  // stage-1 state (FP64)
+  double* phin = phi1 + cells;                   // stage-2 state (FP64)
+  nebo_field f;
+  for (int i = 0; i < 3; ++i) {
+    f.glob[i] = f.extent[i] = gl;
+    f.offset[i] = 0;
+    f.ghost_minus[i] = f.ghost_plus[i] = G;
+    f.has_bc[i] = f.bc_extra[i] = 0;
+  }
+  int rc;
+  if (dtype == NEBO_F64) {
+    f.dtype = NEBO_F64;
+    f.data = phi;
+    if ((rc = fill_periodic_any(&f, s))) return rc;
+    for (const void* q : {u, v, w, lam}) {
+      f.data = const_cast<void*>(q);
+      if ((rc = fill_periodic_any(&f, s))) return rc;
+    }
+    TrArgs<double> a{};
+    a.u = (const double*)u + interior;
+    a.v = (const double*)v + interior;
+    a.w = (const double*)w + interior;
+    a.lam = (const double*)lam + interior;
+    a.n = n;
+    a.sy = (int)sy;
+    a.sz = sz;
+    a.nu = nu;
+    const double h = 1.0 / 24.0;
+    a.q0 = h;
+    a.q1 = -27.0 * h;
+    a.q2 = 27.0 * h;
+    a.q3 = -h;
+    a.dt = dt;
+    double* cur = phi;
+    for (int k = 0; k < steps; ++k) {
+      // stage 1: phi1 = cur + dt R(cur)
+      a.phi = cur + interior;
+      a.acc = cur + interior;
+      a.out64 = phi1 + interior;
+      a.outS = nullptr;
+      if ((rc = transport_launch(a, false, s))) return rc;
+      // stage 2: phin = cur/2 + (phi1 + dt R(phi1))/2
+      a.phi = phi1 + interior;
+      a.acc = phi1 + interior;
+      a.base = cur + interior;
+      a.out64 = (cur == phi ? phin : phi) + interior;
+      if ((rc = transport_launch(a, true, s))) return rc;
+      cur = (cur == phi) ? phin : phi;
+    }
+    if (cur != phi) NEBO_CUDA_TRY(cudaMemcpyAsync(phi, cur, cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return NEBO_OK;
+  }
+  // FP32 storage: float stencil copies + FP64 accumulators
+  float* s0 = reinterpret_cast<float*>(phin + cells);
+  float* s1 = s0 + cells;
+  f.dtype = NEBO_F32;
+  for (const void* q : {u, v, w, lam}) {
+    f.data = const_cast<void*>(q);
+    if ((rc = fill_periodic_any(&f, s))) return rc;
+  }
+  f.dtype = NEBO_F64;
+  f.data = phi;
+  if ((rc = fill_periodic_any(&f, s))) return rc;
+  if ((rc = cast_f64_to_f32(phi, s0, cells, s))) return rc;
+  TrArgs<float> a{};
+  a.u = (const float*)u + interior;
+  a.v = (const float*)v + interior;
+  a.w = (const float*)w + interior;
+  a.lam = (const float*)lam + interior;
+  a.n = n;
+  a.sy = (int)sy;
+  a.sz = sz;
+  a.nu = (float)nu;
+  const float h = 1.0f / 24.0f;
+  a.q0 = h;
+  a.q1 = -27.0f * h;
+  a.q2 = 27.0f * h;
+  a.q3 = -h;
+  a.dt = dt;
+  double* cur = phi;
+  for (int k = 0; k < steps; ++k) {
+    a.phi = s0 + interior;
+    a.acc = cur + interior;
+    a.out64 = phi1 + interior;
+    a.outS = s1;
+    a.outS += interior;
+    if ((rc = transport_launch(a, false, s))) return rc;
+    a.phi = s1 + interior;
+    a.acc = phi1 + interior;
+    a.base = cur + interior;
+    double* nxt = (cur == phi) ? phin : phi;
+    a.out64 = nxt + interior;
+    a.outS = s0 + interior;
+    if ((rc = transport_launch(a, true, s))) return rc;
+    cur = nxt;
+  }
+  if (cur != phi) NEBO_CUDA_TRY(cudaMemcpyAsync(phi, cur, cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // the FP64 state's ghosts: periodic images of the result
+  f.dtype = NEBO_F64;
+  f.data = phi;
+  return fill_periodic_any(&f, s);
+}

@@ -149,3 +149,39 @@ def transport_inputs(n, seed=10, modes=4, nu=0.05):
     dt = 0.4  # CFL 0.4 with |u| <= 1 and unit spacing
     return (np.ascontiguousarray(phi), np.ascontiguousarray(u), np.ascontiguousarray(v),
             np.ascontiguousarray(w), np.ascontiguousarray(lam), dt, nu)
+
+
+def transport_inputs_device(n, seed=10, modes=4, nu=0.05, device="cuda"):
+    """transport_inputs built with torch on the GPU (same construction; for the full-size runs,
+    where numpy on the host would take minutes).  Returns torch float64 tensors."""
+    import torch
+
+    g = 2
+    rng = np.random.default_rng(seed)
+    ax = torch.arange(-g, n + g, dtype=torch.float64, device=device)
+    zz, yy, xx = torch.meshgrid(ax, ax, ax, indexing="ij")
+    A = [torch.zeros_like(xx) for _ in range(3)]
+    for _ in range(modes):
+        k = rng.integers(1, 4, size=3) * rng.choice([-1, 1], size=3)
+        amp = rng.normal(size=3)
+        ph = rng.uniform(0, 2 * np.pi)
+        arg = (2 * np.pi / n) * (float(k[0]) * xx + float(k[1]) * yy + float(k[2]) * zz) + ph
+        s = torch.sin(arg)
+        for d in range(3):
+            A[d] += float(amp[d]) * s
+        del arg, s
+    Ax, Ay, Az = A
+
+    def dfwd(f, axis):
+        return torch.roll(f, -1, dims=axis) - f
+
+    u = dfwd(Az, 1) - dfwd(Ay, 0)
+    v = dfwd(Ax, 0) - dfwd(Az, 2)
+    w = dfwd(Ay, 2) - dfwd(Ax, 1)
+    del A, Ax, Ay, Az
+    umax = max(float(u.abs().max()), float(v.abs().max()), float(w.abs().max()))
+    u, v, w = u / umax, v / umax, w / umax
+    lam = torch.from_numpy(rng.uniform(0.5, 1.5, size=(n + 2 * g,) * 3)).to(device)
+    r2 = ((xx + 0.5 - n / 2.0) ** 2 + (yy + 0.5 - n / 2.0) ** 2 + (zz + 0.5 - n / 2.0) ** 2)
+    phi = torch.exp(-r2 / (2.0 * (n / 8.0) ** 2))
+    return phi.contiguous(), u.contiguous(), v.contiguous(), w.contiguous(), lam.contiguous(), 0.4, nu

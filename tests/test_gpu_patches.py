@@ -15,8 +15,11 @@ def _setup(shapes, dtype, autotune):
     dt = np.array([t[2] for t in ins])
     ps = N.PatchSet(shapes, lam, dt, dtype)
     chosen = ps.autotune() if autotune else None
+    import torch
+
     for p, (_, T0, _) in enumerate(ins):
-        ps.window(0, p).copy_(__import__("torch").from_numpy(T0).to(ps.window(0, p).dtype))
+        ps.window(0, p).copy_(torch.from_numpy(T0))
+    ps.fill_ghosts(0)
     return ps, ins, chosen
 
 
@@ -50,12 +53,13 @@ def test_patches_autotune_keeps_results():
 
 
 def test_patches_fp32_error_vs_fp64_oracle():
+    # FP32 stencil sweeps, FP64 state accumulation: <= 1e-5 relative after 200 steps
     rng = np.random.default_rng(5)
     shapes = rng.integers(8, 40, size=(10, 3)).astype(np.int32)
     ps, ins, _ = _setup(shapes, "f32", autotune=True)
-    fin = ps.run(40)
+    fin = ps.run(200)
     for p in range(len(shapes)):
-        ref = _oracle(shapes[p], ins[p][0], ins[p][1], ins[p][2], 40)
+        ref = _oracle(shapes[p], ins[p][0], ins[p][1], ins[p][2], 200)
         got = ps.window(fin, p).cpu().numpy().astype(np.float64)
         err = np.abs(got - ref).max() / np.abs(ref).max()
         assert err <= 1e-5, (p, err)

@@ -1,0 +1,123 @@
+"""Scalar transport (FP64 and FP32-storage forms) and the heat adjoint on the GPU."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_dsl as O
+import spatialops_gb300 as N
+from spatialops_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def test_transport_fp64_vs_reference_golden():
+    z = np.load(os.path.join(GOLD, "transport.npz"))
+    n = int(z["n"])
+    t = N.Transport(z["phi0"], z["u"], z["v"], z["w"], z["lam"], n, float(z["dt"]), float(z["nu"]), dtype="f64")
+    t.run(int(z["steps"]))
+    assert _rel(t.phi.cpu().numpy(), z["f:phi"]) <= 1e-13
+
+
+@pytest.mark.parametrize("n,steps", [(24, 6), (37, 3)])
+def test_transport_fp64_vs_oracle(n, steps):
+    phi, u, v, w, lam, dt, nu = W.transport_inputs(n)
+    t = N.Transport(phi, u, v, w, lam, n, dt, nu, dtype="f64")
+    t.run(steps)
+    ref = O.transport_run(phi, u, v, w, lam, n, steps, dt, nu)
+    assert _rel(t.phi.cpu().numpy(), ref) <= 1e-13
+
+
+def test_transport_fp32_storage_error_vs_fp64_oracle():
+    n, steps = 32, 20
+    phi, u, v, w, lam, dt, nu = W.transport_inputs(n)
+    t = N.Transport(phi, u, v, w, lam, n, dt, nu, dtype="f32")
+    t.run(steps)
+    ref = O.transport_run(phi, u, v, w, lam, n, steps, dt, nu)
+    assert _rel(t.phi.cpu().numpy(), ref) <= 1e-5
+
+
+def test_transport_velocity_is_divergence_free():
+    n = 16
+    _, u, v, w, _, _, _ = W.transport_inputs(n)
+    g = 2
+    i = slice(g, g + n)
+    div = (u[i, i, g + 1:g + n + 1] - u[i, i, i]) + (v[i, g + 1:g + n + 1, i] - v[i, i, i]) + \
+        (w[g + 1:g + n + 1, i, i] - w[i, i, i])
+    assert np.abs(div).max() < 1e-12
+
+
+# ---------------------------------------------------------------------------- adjoint
+def _setup(n, steps, seed=8):
+    lam, T0, dt, lam_t = W.adjoint_inputs(n, seed)
+    Ttarget = O.heat_run(lam_t, T0, n, steps, dt)
+    return lam, T0, dt, Ttarget
+
+
+def _gpu_grad(lam, T0, Tt, steps, dt, every=0):
+    F = lambda a: N.Field.from_numpy("SVol", a, 1)
+    J, gT, gl = N.heat_gradient(F(T0), F(lam), F(Tt), steps, dt, every)
+    return J, gT.numpy(), gl.numpy()
+
+
+@pytest.mark.parametrize("every", [0, 1, 4, 50])
+def test_adjoint_matches_oracle_adjoint(every):
+    n, steps = (10, 9, 8), 13
+    lam, T0, dt, Tt = _setup(n, steps)
+    J, gT, gl = _gpu_grad(lam, T0, Tt, steps, dt, every)
+    TN = O.heat_run(lam, T0, n, steps, dt)
+    r = np.zeros_like(TN)
+    r[1:-1, 1:-1, 1:-1] = (TN - Tt)[1:-1, 1:-1, 1:-1]
+    ref_gT, ref_gl = O.heat_adjoint(T0, lam, r, n, steps, dt)
+    I = (slice(1, -1),) * 3
+    assert abs(J - 0.5 * float((r[I] ** 2).sum())) <= 1e-12 * max(J, 1e-300)
+    assert _rel(gT[I], ref_gT[I]) <= 1e-12
+    assert _rel(gl[I], ref_gl[I]) <= 1e-12
+
+
+def test_adjoint_dense_jacobian_8cubed():
+    """dJ/dT0 = Jac^T r with the dense Jacobian of the (linear) map T0 -> T_N built column by column."""
+    n, steps = (8, 8, 8), 10
+    lam, T0, dt, Tt = _setup(n, steps)
+    J, gT, _ = _gpu_grad(lam, T0, Tt, steps, dt)
+    I = (slice(1, -1),) * 3
+    TN = O.heat_run(lam, T0, n, steps, dt)
+    r = (TN - Tt)[I].reshape(-1)
+    jac = np.zeros((512, 512))
+    for col in range(512):
+        e = np.zeros_like(T0)
+        e[I] = np.eye(1, 512, col).reshape(8, 8, 8)
+        O.fill_periodic(e, 1)
+        jac[:, col] = O.heat_run(lam, e, n, steps, dt)[I].reshape(-1)
+    ref = jac.T @ r
+    assert np.abs(gT[I].reshape(-1) - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("which", ["lam", "T0"])
+def test_adjoint_vs_central_finite_differences(which):
+    n, steps = (24, 20, 16), 40
+    lam, T0, dt, Tt = _setup(n, steps)
+    J, gT, gl = _gpu_grad(lam, T0, Tt, steps, dt)
+    I = (slice(1, -1),) * 3
+    rng = np.random.default_rng(9)
+    F = lambda a: N.Field.from_numpy("SVol", a, 1)
+    for _ in range(4):
+        d = np.zeros_like(T0)
+        d[I] = rng.normal(size=d[I].shape)
+        O.fill_periodic(d, 1)
+        eps = 1e-6
+        if which == "lam":
+            Jp = N.heat_gradient(F(T0), F(lam + eps * d), F(Tt), steps, dt)[0]
+            Jm = N.heat_gradient(F(T0), F(lam - eps * d), F(Tt), steps, dt)[0]
+            g = float((gl[I] * d[I]).sum())
+        else:
+            Jp = N.heat_gradient(F(T0 + eps * d), F(lam), F(Tt), steps, dt)[0]
+            Jm = N.heat_gradient(F(T0 - eps * d), F(lam), F(Tt), steps, dt)[0]
+            g = float((gT[I] * d[I]).sum())
+        fd = (Jp - Jm) / (2 * eps)
+        assert abs(fd - g) <= 1e-6 * abs(g), (fd, g)
