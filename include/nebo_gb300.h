@@ -41,7 +41,7 @@ enum nebo_status_code {
   NEBO_ERR_NO_DEVICE = 7
 };
 
-enum nebo_dtype { NEBO_F64 = 0, NEBO_F32 = 1 };
+enum nebo_dtype { NEBO_F64 = 0, NEBO_F32 = 1, NEBO_F32X2 = 2 /* two-float state (patchsets only) */ };
 
 enum nebo_reduction { NEBO_RED_SUM = 0, NEBO_RED_MAX = 1, NEBO_RED_MIN = 2, NEBO_RED_NORM = 3 };
 
@@ -166,7 +166,12 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
  *             0|1); the element offset of each window comes from nebo_patchset_info.  dtype
  *             NEBO_F32 adds FP32 copies that the stencil sweeps read and write (FP32 storage and
  *             arithmetic on the sweeps, FP64 accumulation of the state).
- *   fill_ghosts: periodic ghost images of an arena (and its FP32 copy); call after loading.
+ *             dtype NEBO_F32X2 keeps the state as two floats (hi + lo, ~48-bit significand) and
+ *             runs the sweep in FP32 arithmetic only (no FP64 operation); results reach the FP64
+ *             arena through nebo_patchset_sync.
+ *   fill_ghosts: periodic ghost images of an FP64 arena, then its FP32 / two-float working copy;
+ *             call after loading the FP64 arena.
+ *   sync:     after run, make the FP64 arena `which` hold the state (FP32X2: hi + lo).
  *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest (clobbers
  *             the arenas: call it before loading data).
  *   run:      `steps` steps from arena `start`; *final_arena says where the result is.
@@ -179,6 +184,7 @@ int nebo_patchset_info(const nebo_patchset* ps, int64_t* total_elems, int64_t* o
                        int32_t* log2_tile_x, int32_t* nitems);
 void* nebo_patchset_arena(const nebo_patchset* ps, int which);
 int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, nebo_stream_t stream);
+int nebo_patchset_sync(const nebo_patchset* ps, int which, nebo_stream_t stream);
 int nebo_patchset_autotune(nebo_patchset* ps, nebo_stream_t stream, int32_t* chosen_log2_tile_x);
 int nebo_patchset_run(nebo_patchset* ps, int start, int steps, int use_graph, int* final_arena,
                       nebo_stream_t stream);

@@ -19,7 +19,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnebo_gb300.so")
 
-F64, F32 = 0, 1
+F64, F32, F32X2 = 0, 1, 2
 RED = {"sum": 0, "max": 1, "min": 2, "norm": 3}
 
 # location type -> (offset, BCExtra), spatialops/structured/FVStaggeredLocationTypes.h:63-126
@@ -80,6 +80,7 @@ SIGNATURES = [
     ("nebo_patchset_info", _I, [_P, _P, _P, _P, _P]),
     ("nebo_patchset_arena", _P, [_P, _I]),
     ("nebo_patchset_fill_ghosts", _I, [_P, _I, _P]),
+    ("nebo_patchset_sync", _I, [_P, _I, _P]),
     ("nebo_patchset_autotune", _I, [_P, _P, _P]),
     ("nebo_patchset_run", _I, [_P, _I, _I, _I, ctypes.POINTER(_I), _P]),
     ("nebo_transport_work_bytes", ctypes.c_size_t, [_I, _I]),
@@ -294,8 +295,8 @@ class PatchSet:
         self.npatch = len(self.shapes)
         self.lam = np.ascontiguousarray(lam, dtype=np.float64)
         self.dt = np.ascontiguousarray(dt, dtype=np.float64)
-        self.dtype = F64 if dtype == "f64" else F32
-        self.esize = 8  # arenas hold the FP64 states in both modes
+        self.dtype = {"f64": F64, "f32": F32, "f32x2": F32X2}[dtype]
+        self.esize = 8  # the visible arenas hold FP64 states in every mode
         h = ctypes.c_void_p()
         _check(lib().nebo_patchset_create(ctypes.byref(h), self.npatch, ctypes.c_void_p(self.shapes.ctypes.data),
                                           ctypes.c_void_p(self.lam.ctypes.data), ctypes.c_void_p(self.dt.ctypes.data),
@@ -355,6 +356,10 @@ class PatchSet:
         _check(lib().nebo_patchset_run(self.h, int(start), int(steps), int(use_graph), ctypes.byref(fin),
                                        _stream(stream)))
         return fin.value
+
+    def sync(self, which, stream=None):
+        """Make FP64 arena `which` hold the state (needed after run in the two-float mode)."""
+        _check(lib().nebo_patchset_sync(self.h, int(which), _stream(stream)))
 
 
 class Transport:

@@ -31,6 +31,7 @@ namespace nebo {
 namespace {
 
 constexpr int PT_THREADS = 256;
+constexpr int PF = 4;  // z planes prefetched ahead per thread
 constexpr int PT_MAX_TY = 16;   // TX = 16
 constexpr int PT_MAX_TX = 64;   // TY = 4
 
@@ -48,24 +49,50 @@ struct WorkItem {
   int z0, z1;
 };
 
-template <typename T>
-__device__ __forceinline__ T exact_sub(T a, T b);
-template <>
-__device__ __forceinline__ double exact_sub(double a, double b) { return __dsub_rn(a, b); }
-template <>
-__device__ __forceinline__ float exact_sub(float a, float b) { return a - b; }
-template <typename T>
-__device__ __forceinline__ T exact_add(T a, T b);
-template <>
-__device__ __forceinline__ double exact_add(double a, double b) { return __dadd_rn(a, b); }
-template <>
-__device__ __forceinline__ float exact_add(float a, float b) { return a + b; }
-template <typename T>
-__device__ __forceinline__ T exact_mul(T a, T b);
-template <>
-__device__ __forceinline__ double exact_mul(double a, double b) { return __dmul_rn(a, b); }
-template <>
-__device__ __forceinline__ float exact_mul(float a, float b) { return a * b; }
+// Storage and arithmetic of the three precision modes.
+//   PMODE_F64   value = double, fluxes double, round-to-nearest FP64 ops (bit-exact form)
+//   PMODE_F32   value = float copy read by the stencil; flux arithmetic float; the state is
+//               accumulated in FP64 (acc_src -> acc_dst)
+//   PMODE_F32X2 value = float2 (hi, lo): the state as an unevaluated sum of two floats (~48-bit
+//               significand); differences (hb-ha)+(lb-la), fluxes and the update in float, the
+//               update added with an error-free two-sum.  No FP64 operation on the sweep.
+enum { PMODE_F64 = 0, PMODE_F32 = 1, PMODE_F32X2 = 2 };
+
+template <int M> struct PM;
+template <> struct PM<PMODE_F64> {
+  typedef double S;
+  typedef double F;
+  static __device__ __forceinline__ F diff(S a, S b) { return __dsub_rn(b, a); }
+  static __device__ __forceinline__ F add(F a, F b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ F sub(F a, F b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ F mul(F a, F b) { return __dmul_rn(a, b); }
+};
+template <> struct PM<PMODE_F32> {
+  typedef float S;
+  typedef float F;
+  static __device__ __forceinline__ F diff(S a, S b) { return b - a; }
+  static __device__ __forceinline__ F add(F a, F b) { return a + b; }
+  static __device__ __forceinline__ F sub(F a, F b) { return a - b; }
+  static __device__ __forceinline__ F mul(F a, F b) { return a * b; }
+};
+template <> struct PM<PMODE_F32X2> {
+  typedef float2 S;
+  typedef float F;
+  static __device__ __forceinline__ F diff(S a, S b) { return (b.x - a.x) + (b.y - a.y); }
+  static __device__ __forceinline__ F add(F a, F b) { return a + b; }
+  static __device__ __forceinline__ F sub(F a, F b) { return a - b; }
+  static __device__ __forceinline__ F mul(F a, F b) { return a * b; }
+};
+
+// (hi, lo) + inc with Knuth's two-sum, renormalised (Dekker's fast two-sum)
+__device__ __forceinline__ float2 ff_add(float2 v, float inc) {
+  const float s = __fadd_rn(v.x, inc);
+  const float bb = __fsub_rn(s, v.x);
+  const float e = __fadd_rn(__fsub_rn(v.x, __fsub_rn(s, bb)), __fsub_rn(inc, bb));
+  const float lo = __fadd_rn(v.y, e);
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
 
 template <typename T>
 __device__ __forceinline__ void store_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
@@ -86,18 +113,21 @@ __device__ __forceinline__ void store_images(T* base, int sy, long sz, int x, in
       for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
 }
 
-// One persistent launch = one time step of every patch.
-// FP64 mode (ACC = false, T = double): src/dst are the FP64 states.
-// FP32 mode (ACC = true, T = float): src/dst are FP32 stencil copies; the time-integrated state
-// is accumulated in FP64 (acc_src -> acc_dst), and both the copy and the state get ghost images.
-template <typename T, bool ACC>
+template <typename S>
+__device__ __forceinline__ S ldg_s(const S* p) { return __ldg(p); }
+
+// One persistent launch = one time step of every patch (mode M, see PM above).
+template <int M>
 __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev* __restrict__ patches,
                                                                   const WorkItem* __restrict__ items, int nitems,
-                                                                  const T* __restrict__ src, T* __restrict__ dst,
+                                                                  const typename PM<M>::S* __restrict__ src,
+                                                                  typename PM<M>::S* __restrict__ dst,
                                                                   const double* __restrict__ acc_src,
                                                                   double* __restrict__ acc_dst) {
-  __shared__ T sfx[2][PT_MAX_TY * (PT_MAX_TX + 1) / 4 + 64];  // TY*(TX+1) <= 16*17, 8*33, 4*65
-  __shared__ T sfy[2][(PT_MAX_TY + 1) * 16 + 64];            // (TY+1)*TX <= 17*16, 9*32, 5*64
+  typedef typename PM<M>::S S;
+  typedef typename PM<M>::F F;
+  __shared__ F sfx[2][PT_MAX_TY * (PT_MAX_TX + 1) / 4 + 64];  // TY*(TX+1) <= 16*17, 8*33, 4*65
+  __shared__ F sfy[2][(PT_MAX_TY + 1) * 16 + 64];            // (TY+1)*TX <= 17*16, 9*32, 5*64
   const int tid = threadIdx.x;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const WorkItem it = items[w];
@@ -108,43 +138,53 @@ __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev
     const int sy = nx + 2;
     const long sz = (long)(nx + 2) * (ny + 2);
     const long interior = (long)1 + sy + sz;  // flat offset of interior (0,0,0)
-    const T* tin = src + P.offset + interior;
-    T* tout = dst + P.offset + interior;
-    const T l2 = (T)P.lam2, hdt = (T)P.hdt;
+    const S* tin = src + P.offset + interior;
+    S* tout = dst + P.offset + interior;
+    const F l2 = (F)P.lam2, hdt = (F)P.hdt;
     const int x = it.x0 + tx, y = it.y0 + ty;
     const bool active = x < nx && y < ny;
     const int xc = min(x, nx), yc = min(y, ny);
     auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
-    auto flux = [&](T ta, T tb) { return exact_mul(l2, exact_sub(tb, ta)); };
-    T tc = __ldg(tin + at(xc, yc, it.z0));
-    T fzlo = flux(__ldg(tin + at(xc, yc, it.z0 - 1)), tc);
+    auto flux = [&](S ta, S tb) { return PM<M>::mul(l2, PM<M>::diff(ta, tb)); };
+    S tc = ldg_s(tin + at(xc, yc, it.z0));
+    F fzlo = flux(ldg_s(tin + at(xc, yc, it.z0 - 1)), tc);
+    // register queue of the next PF planes (loads issued PF planes ahead of use; clamped to
+    // the +z ghost plane, which exists)
+    S q[PF];
+#pragma unroll
+    for (int i = 0; i < PF; ++i) q[i] = ldg_s(tin + at(xc, yc, min(it.z0 + 1 + i, nz)));
     for (int z = it.z0; z < it.z1; ++z) {
       const int buf = z & 1;
-      const T tn = __ldg(tin + at(xc, yc, z + 1));
-      const T fzhi = flux(tc, tn);
-      const T fx = flux(__ldg(tin + at(xc - 1, yc, z)), tc);
-      const T fy = flux(__ldg(tin + at(xc, yc - 1, z)), tc);
+      const S tn = q[0];
+#pragma unroll
+      for (int i = 0; i < PF - 1; ++i) q[i] = q[i + 1];
+      q[PF - 1] = ldg_s(tin + at(xc, yc, min(z + 1 + PF, nz)));
+      const F fzhi = flux(tc, tn);
+      const F fx = flux(ldg_s(tin + at(xc - 1, yc, z)), tc);
+      const F fy = flux(ldg_s(tin + at(xc, yc - 1, z)), tc);
       sfx[buf][ty * (TX + 1) + tx] = fx;
       sfy[buf][ty * TX + tx] = fy;
       if (ty == 0) {  // +y halo faces of the tile
         const int yh = it.y0 + TY;
-        if (yh <= ny && x <= nx) sfy[buf][TY * TX + tx] = flux(__ldg(tin + at(xc, yh - 1, z)), __ldg(tin + at(xc, yh, z)));
+        if (yh <= ny && x <= nx) sfy[buf][TY * TX + tx] = flux(ldg_s(tin + at(xc, yh - 1, z)), ldg_s(tin + at(xc, yh, z)));
       } else if (ty == 1 && tx < TY) {  // +x halo faces of the tile
         const int xh = it.x0 + TX, yr = it.y0 + tx;
-        if (xh <= nx && yr < ny) sfx[buf][tx * (TX + 1) + TX] = flux(__ldg(tin + at(xh - 1, yr, z)), __ldg(tin + at(xh, yr, z)));
+        if (xh <= nx && yr < ny) sfx[buf][tx * (TX + 1) + TX] = flux(ldg_s(tin + at(xh - 1, yr, z)), ldg_s(tin + at(xh, yr, z)));
       }
       __syncthreads();
       if (active) {
-        const T fxhi = sfx[buf][ty * (TX + 1) + tx + 1];
-        const T fyhi = sfy[buf][(ty + 1) * TX + tx];
-        const T s = exact_add(exact_add(exact_sub(fxhi, fx), exact_sub(fyhi, fy)), exact_sub(fzhi, fzlo));
-        if (ACC) {
+        const F fxhi = sfx[buf][ty * (TX + 1) + tx + 1];
+        const F fyhi = sfy[buf][(ty + 1) * TX + tx];
+        const F s = PM<M>::add(PM<M>::add(PM<M>::sub(fxhi, fx), PM<M>::sub(fyhi, fy)), PM<M>::sub(fzhi, fzlo));
+        if constexpr (M == PMODE_F64) {
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, __dadd_rn(tc, __dmul_rn(hdt, s)));
+        } else if constexpr (M == PMODE_F32) {
           const long c = P.offset + interior + at(x, y, z);
           const double v = acc_src[c] + P.hdt * (double)s;
           store_images(acc_dst + P.offset + interior, sy, sz, x, y, z, nx, ny, nz, v);
-          store_images(tout, sy, sz, x, y, z, nx, ny, nz, (T)v);
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, (float)v);
         } else {
-          store_images(tout, sy, sz, x, y, z, nx, ny, nz, exact_add(tc, exact_mul(hdt, s)));
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, ff_add(tc, hdt * s));
         }
       }
       tc = tn;
@@ -166,6 +206,7 @@ struct PatchSet {
   long long total = 0;  // elements per arena
   void* arena[2] = {nullptr, nullptr};    // FP64 states
   float* arena32[2] = {nullptr, nullptr};  // FP32 stencil copies (FP32 mode)
+  float2* arena2[2] = {nullptr, nullptr};  // two-float states (FP32X2 mode)
   PatchDev* d_patches = nullptr;
   WorkItem* d_items = nullptr;
   int nitems = 0;
@@ -178,6 +219,8 @@ struct PatchSet {
     cudaFree(arena[1]);
     cudaFree(arena32[0]);
     cudaFree(arena32[1]);
+    cudaFree(arena2[0]);
+    cudaFree(arena2[1]);
     cudaFree(d_patches);
     cudaFree(d_items);
   }
@@ -225,15 +268,18 @@ int upload_tables(PatchSet& ps, const std::vector<WorkItem>& items, cudaStream_t
 
 int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parity, cudaStream_t s) {
   if (nitems == 0) return NEBO_OK;
-  LaunchScope ls(ps.dtype == NEBO_F64 ? "patches_step_f64" : "patches_step_f32", s);
+  LaunchScope ls(ps.dtype == NEBO_F64 ? "patches_step_f64" : (ps.dtype == NEBO_F32 ? "patches_step_f32" : "patches_step_f32x2"), s);
   const int grid = std::min(nitems, ps.grid);
   if (ps.dtype == NEBO_F64)
-    patches_step_kernel<double, false><<<grid, PT_THREADS, 0, s>>>(
+    patches_step_kernel<PMODE_F64><<<grid, PT_THREADS, 0, s>>>(
         ps.d_patches, items, nitems, (const double*)ps.arena[parity], (double*)ps.arena[parity ^ 1], nullptr, nullptr);
-  else
-    patches_step_kernel<float, true><<<grid, PT_THREADS, 0, s>>>(
+  else if (ps.dtype == NEBO_F32)
+    patches_step_kernel<PMODE_F32><<<grid, PT_THREADS, 0, s>>>(
         ps.d_patches, items, nitems, ps.arena32[parity], ps.arena32[parity ^ 1], (const double*)ps.arena[parity],
         (double*)ps.arena[parity ^ 1]);
+  else
+    patches_step_kernel<PMODE_F32X2><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, ps.arena2[parity],
+                                                                 ps.arena2[parity ^ 1], nullptr, nullptr);
   NEBO_LAUNCH_CHECK("nebo_patchset_run");
   return NEBO_OK;
 }
@@ -243,6 +289,16 @@ int default_log2tx(int nx) { return nx <= 16 ? 4 : (nx <= 40 ? 5 : 6); }
 __global__ void patches_cast_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
+}
+__global__ void patches_split_kernel(const double* __restrict__ a, float2* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float hi = (float)a[i];
+    b[i] = make_float2(hi, (float)(a[i] - (double)hi));
+  }
+}
+__global__ void patches_join_kernel(const float2* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i].x + (double)a[i].y;
 }
 
 }  // namespace
@@ -256,7 +312,8 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
                                     const double* dt, int dtype) {
   if (!out || npatch <= 0 || !shapes || !lam || !dt)
     return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: bad arguments");
-  if (dtype != NEBO_F64 && dtype != NEBO_F32) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: dtype");
+  if (dtype != NEBO_F64 && dtype != NEBO_F32 && dtype != NEBO_F32X2)
+    return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_create: dtype");
   *out = nullptr;
   nebo_patchset* ps = new nebo_patchset();
   ps->npatch = npatch;
@@ -284,6 +341,13 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
   if (e == cudaSuccess) e = cudaMalloc(&ps->arena[1], bytes);
   if (e == cudaSuccess) e = cudaMemset(ps->arena[0], 0, bytes);
   if (e == cudaSuccess) e = cudaMemset(ps->arena[1], 0, bytes);
+  if (dtype == NEBO_F32X2) {
+    const size_t b2 = (size_t)off * sizeof(float2);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena2[0], b2);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena2[1], b2);
+    if (e == cudaSuccess) e = cudaMemset(ps->arena2[0], 0, b2);
+    if (e == cudaSuccess) e = cudaMemset(ps->arena2[1], 0, b2);
+  }
   if (dtype == NEBO_F32) {
     const size_t b32 = (size_t)off * sizeof(float);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena32[0], b32);
@@ -349,7 +413,24 @@ extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, neb
     patches_cast_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>((const double*)ps->arena[which],
                                                                          ps->arena32[which], (size_t)ps->total);
     NEBO_LAUNCH_CHECK("nebo_patchset_fill_ghosts");
+  } else if (ps->dtype == NEBO_F32X2) {  // split each double into (hi, lo) floats
+    LaunchScope ls("patches_split_f32x2", (cudaStream_t)stream);
+    patches_split_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>((const double*)ps->arena[which],
+                                                                          ps->arena2[which], (size_t)ps->total);
+    NEBO_LAUNCH_CHECK("nebo_patchset_fill_ghosts");
   }
+  return NEBO_OK;
+}
+
+// Bring the state of arena `which` into its FP64 arena (FP32X2 mode joins hi + lo; the other
+// modes already keep the FP64 state there).
+extern "C" int nebo_patchset_sync(const nebo_patchset* ps, int which, nebo_stream_t stream) {
+  if (!ps || (which != 0 && which != 1)) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_sync");
+  if (ps->dtype != NEBO_F32X2) return NEBO_OK;
+  LaunchScope ls("patches_join_f32x2", (cudaStream_t)stream);
+  patches_join_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena2[which], (double*)ps->arena[which],
+                                                                       (size_t)ps->total);
+  NEBO_LAUNCH_CHECK("nebo_patchset_sync");
   return NEBO_OK;
 }
 
