@@ -69,6 +69,11 @@ __device__ __forceinline__ void store_images2(T* base, int sy, long sz, int x, i
       for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
 }
 
+// Ask L2 to fetch the line holding p (no register, no wait): planes are requested PFZ steps of
+// the z march before the kernel reads them, so DRAM latency overlaps the current plane's work.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+constexpr int PFZ = 6;
+
 template <typename T, bool SECOND>
 __global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, int zchunk) {
   __shared__ T sfx[2][TY][TX + 1];
@@ -87,6 +92,20 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, in
   for (int z = z0; z < z1; ++z) {
     const int buf = z & 1;
     const long c = at(xc, yc, z);
+    {
+      // the planes this column reads first at step z + PFZ (clamped inside the window)
+      const int zp = min(z + PFZ, n + 1);
+      const long cp = at(xc, yc, zp);
+      prefetch_l2(a.phi + cp);
+      prefetch_l2(a.lam + cp);
+      prefetch_l2(a.u + cp);
+      prefetch_l2(a.v + cp);
+      prefetch_l2(a.w + cp);
+      if (zp < n) {
+        prefetch_l2(a.acc + cp);
+        if (SECOND) prefetch_l2(a.base + cp);
+      }
+    }
     const T fzhi = face_flux(a, c + sz, sz, a.w);
     const T fx = face_flux(a, c, 1, a.u);
     const T fy = face_flux(a, c, sy, a.v);
