@@ -155,6 +155,11 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
                     const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
                     double dx, nebo_stream_t stream);
 
+/* Element-wise FP64 exp (fn 0) or sin (fn 1) with the table-driven functions nebo_deep_chain
+ * uses (Tang's table method for exp; a sin/cos(k pi/64) table with short Taylor polynomials for
+ * sin): about half the FP64 instructions of general-purpose versions, within 2 ulp. */
+int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream);
+
 /* ------------------------------------------------------------------ batched patches
  * Many independent periodic heat-equation patches (one ghost layer, scalar lambda and dt per
  * patch) advanced together: each time step is ONE persistent launch over a device patch table

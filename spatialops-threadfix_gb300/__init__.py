@@ -87,6 +87,7 @@ SIGNATURES = [
     ("nebo_transport_run", _I, [_P, _P, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
     ("nebo_heat_adjoint_step", _I, [_FP, _FP, _FP, _FP, _FP, _D, _P]),
     ("nebo_heat_gradient", _I, [_FP, _FP, _FP, _I, _D, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
+    ("nebo_fastmath_eval", _I, [_I, _P, _P, ctypes.c_size_t, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
     ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
@@ -399,3 +400,13 @@ def heat_adjoint_step(Tk, Ain, Aout, lam, glam, dt, stream=None):
     a, b, c, d, e = Tk.desc(), Ain.desc(), Aout.desc(), lam.desc(), glam.desc()
     _check(lib().nebo_heat_adjoint_step(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d),
                                         ctypes.byref(e), float(dt), _stream(stream)))
+
+
+def fastmath_eval(fn, x, stream=None):
+    """Element-wise table-driven FP64 exp ("exp") or sin ("sin") of a CUDA float64 tensor."""
+    import torch
+
+    y = torch.empty_like(x)
+    _check(lib().nebo_fastmath_eval({"exp": 0, "sin": 1}[fn], ctypes.c_void_p(x.data_ptr()),
+                                    ctypes.c_void_p(y.data_ptr()), x.numel(), _stream(stream)))
+    return y

@@ -31,7 +31,6 @@ namespace {
 
 constexpr int BX = 32;
 constexpr int BY = 8;
-constexpr int PF = 4;  // z planes prefetched ahead per thread
 
 struct ExactD {
   static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
@@ -106,30 +105,10 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
   T lc = __ldg(lam + at(xc, yc, z0));
   T fzlo = face_flux<T, A, MODE>(__ldg(lam + at(xc, yc, z0 - 1)), lc, __ldg(tin + at(xc, yc, z0 - 1)), tc, p.c0[2],
                                  p.c1[2]);
-  // register queue of the next PF planes of this column: each HBM load is issued PF planes
-  // before it is used, so PF loads per thread are in flight (planes past nz+... clamp to the
-  // +z ghost plane, which exists; those values are never used)
-  T qt[PF], ql[PF];
-#pragma unroll
-  for (int i = 0; i < PF; ++i) {
-    const int zz = min(z0 + 1 + i, nz);
-    qt[i] = __ldg(tin + at(xc, yc, zz));
-    ql[i] = __ldg(lam + at(xc, yc, zz));
-  }
   for (int z = z0; z < z1; ++z) {
     const int buf = z & 1;
-    const T tn = qt[0];
-    const T ln = ql[0];
-#pragma unroll
-    for (int i = 0; i < PF - 1; ++i) {
-      qt[i] = qt[i + 1];
-      ql[i] = ql[i + 1];
-    }
-    {
-      const int zz = min(z + 1 + PF, nz);
-      qt[PF - 1] = __ldg(tin + at(xc, yc, zz));
-      ql[PF - 1] = __ldg(lam + at(xc, yc, zz));
-    }
+    const T tn = __ldg(tin + at(xc, yc, z + 1));
+    const T ln = __ldg(lam + at(xc, yc, z + 1));
     const T fzhi = face_flux<T, A, MODE>(lc, ln, tc, tn, p.c0[2], p.c1[2]);
     const T fx = face_flux<T, A, MODE>(__ldg(lam + at(xc - 1, yc, z)), lc, __ldg(tin + at(xc - 1, yc, z)), tc, p.c0[0],
                                        p.c1[0]);

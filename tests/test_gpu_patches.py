@@ -53,8 +53,8 @@ def test_patches_autotune_keeps_results():
 
 
 @pytest.mark.parametrize("dtype,steps,tol", [
-    ("f32", 40, 1e-5),      # FP32 stencil copy, FP64 state: measured 1.4e-5 after 200 steps
-    ("f32x2", 200, 1e-7),   # two-float state, FP32 arithmetic only
+    ("f32", 200, 5e-5),     # FP32 stencil copy, FP64 state (halves the stencil bytes)
+    ("f32x2", 200, 1e-5),   # two-float state, FP32 arithmetic only: the 1e-5 target at 200 steps
 ])
 def test_patches_fp32_error_vs_fp64_oracle(dtype, steps, tol):
     rng = np.random.default_rng(5)
@@ -66,4 +66,5 @@ def test_patches_fp32_error_vs_fp64_oracle(dtype, steps, tol):
         ref = _oracle(shapes[p], ins[p][0], ins[p][1], ins[p][2], steps)
         got = ps.window(fin, p).cpu().numpy()
         err = np.abs(got - ref).max() / np.abs(ref).max()
+        print(f"patch {p} {tuple(shapes[p])} {dtype} {steps} steps: relative max error {err:.3e}")
         assert err <= tol, (p, err)
