@@ -45,13 +45,13 @@ BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
     "heat": 8 * 3,                   # T, lambda read, T' written
     "heat32": 4 * 3,
     "patches": 8 * 2,    # T read, T' written (lambda is a scalar per patch)
-    "patches32": 8 * 2,  # two-float state (hi, lo) read and written
+    "patches32": 4 * 2,  # FP32 state read and written
     # one RK stage: phi (stencil) + u,v,w,lambda read, state accumulation read/written
     "transport": 8 * 5 + 8 + 8,            # FP64: phi, u, v, w, lam, acc read; out written
     "transport32": 4 * 5 + 8 + 8 + 4,      # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
 }
 DOMINANT = {"deep": "deep_chain", "heat": "heat_step_f64", "heat32": "heat_step_f32",
-            "patches": "patches_step_f64", "patches32": "patches_step_f32x2",
+            "patches": "patches_step_f64", "patches32": "patches_step_f32",
             "transport": "transport_stage_f64", "transport32": "transport_stage_f32"}
 
 
@@ -221,7 +221,7 @@ class Patches:
 
         from spatialops_gb300 import workloads as W
 
-        self.name = "patches" if dtype == "f64" else "patches32"  # patches32: two-float FP32 state
+        self.name = "patches" if dtype == "f64" else "patches32"  # patches32: FP32 storage
         self.N = N
         shapes = W.patch_shapes(count)
         ins = W.patch_inputs(shapes)
@@ -296,7 +296,7 @@ def make_workload(N, name, n):
     if name in ("transport", "transport32"):
         return TransportWL(N, n, "f64" if name == "transport" else "f32")
     if name in ("patches", "patches32"):
-        return Patches(N, "f64" if name == "patches" else "f32x2")
+        return Patches(N, "f64" if name == "patches" else "f32")
     if name == "deep":
         return Deep(N, n)
     if name == "heat":

@@ -169,14 +169,13 @@ int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream
  *   create:   shapes = 3 ints per patch (interior nx, ny, nz >= 2); allocates two FP64 state
  *             arenas holding every patch window (x fastest), returned by nebo_patchset_arena(ps,
  *             0|1); the element offset of each window comes from nebo_patchset_info.  dtype
- *             NEBO_F32 adds FP32 copies that the stencil sweeps read and write (FP32 storage and
- *             arithmetic on the sweeps, FP64 accumulation of the state).
- *             dtype NEBO_F32X2 keeps the state as two floats (hi + lo, ~48-bit significand) and
- *             runs the sweep in FP32 arithmetic only (no FP64 operation); results reach the FP64
- *             arena through nebo_patchset_sync.
+ *             NEBO_F32 keeps the working state in FP32 (storage and arithmetic: half the bytes);
+ *             NEBO_F32X2 keeps it as two floats (hi + lo, ~48-bit significand) with FP32
+ *             arithmetic only.  In both, results reach the FP64 arena through nebo_patchset_sync.
  *   fill_ghosts: periodic ghost images of an FP64 arena, then its FP32 / two-float working copy;
  *             call after loading the FP64 arena.
- *   sync:     after run, make the FP64 arena `which` hold the state (FP32X2: hi + lo).
+ *   sync:     after run, make the FP64 arena `which` hold the state (FP32: widened, FP32X2:
+ *             hi + lo).
  *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest (clobbers
  *             the arenas: call it before loading data).
  *   run:      `steps` steps from arena `start`; *final_arena says where the result is.

@@ -29,20 +29,16 @@ constexpr int BY = 8;
 
 __device__ __forceinline__ void store_images1(double* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
                                               double v) {
-  int xs[3], ys[3], zs[3];
-  int cx = 0, cy = 0, cz = 0;
-  xs[cx++] = x;
-  if (x == 0) xs[cx++] = nx;
-  if (x == nx - 1) xs[cx++] = -1;
-  ys[cy++] = y;
-  if (y == 0) ys[cy++] = ny;
-  if (y == ny - 1) ys[cy++] = -1;
-  zs[cz++] = z;
-  if (z == 0) zs[cz++] = nz;
-  if (z == nz - 1) zs[cz++] = -1;
-  for (int k = 0; k < cz; ++k)
-    for (int j = 0; j < cy; ++j)
-      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+  base[(long)x + (long)sy * y + sz * z] = v;
+  if (x != 0 && x != nx - 1 && y != 0 && y != ny - 1 && z != 0 && z != nz - 1) return;
+  // a boundary cell: also write its periodic ghost images (up to 7 more cells; n >= 2 per axis)
+  const int ax = x == 0 ? nx : -1, ay = y == 0 ? ny : -1, az = z == 0 ? nz : -1;
+  const int m = (x == 0 || x == nx - 1) | ((y == 0 || y == ny - 1) << 1) | ((z == 0 || z == nz - 1) << 2);
+  for (int b = 1; b < 8; ++b) {
+    if (b & ~m) continue;
+    const int xx = (b & 1) ? ax : x, yy = (b & 2) ? ay : y, zz = (b & 4) ? az : z;
+    base[(long)xx + (long)sy * yy + sz * zz] = v;
+  }
 }
 
 struct Face {

@@ -69,20 +69,16 @@ __device__ __forceinline__ T face_flux(T la, T lb, T ta, T tb, T c0, T c1) {
 template <typename T>
 __device__ __forceinline__ void store_with_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny,
                                                   int nz, T v) {
-  int xs[3], ys[3], zs[3];
-  int cx = 0, cy = 0, cz = 0;
-  xs[cx++] = x;
-  if (x == 0) xs[cx++] = nx;
-  if (x == nx - 1) xs[cx++] = -1;
-  ys[cy++] = y;
-  if (y == 0) ys[cy++] = ny;
-  if (y == ny - 1) ys[cy++] = -1;
-  zs[cz++] = z;
-  if (z == 0) zs[cz++] = nz;
-  if (z == nz - 1) zs[cz++] = -1;
-  for (int k = 0; k < cz; ++k)
-    for (int j = 0; j < cy; ++j)
-      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+  base[(long)x + (long)sy * y + sz * z] = v;
+  if (x != 0 && x != nx - 1 && y != 0 && y != ny - 1 && z != 0 && z != nz - 1) return;
+  // a boundary cell: also write its periodic ghost images (up to 7 more cells; n >= 2 per axis)
+  const int ax = x == 0 ? nx : -1, ay = y == 0 ? ny : -1, az = z == 0 ? nz : -1;
+  const int m = (x == 0 || x == nx - 1) | ((y == 0 || y == ny - 1) << 1) | ((z == 0 || z == nz - 1) << 2);
+  for (int b = 1; b < 8; ++b) {
+    if (b & ~m) continue;
+    const int xx = (b & 1) ? ax : x, yy = (b & 2) ? ay : y, zz = (b & 4) ? az : z;
+    base[(long)xx + (long)sy * yy + sz * zz] = v;
+  }
 }
 
 template <typename T, class A, int MODE>
@@ -157,6 +153,79 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
   }
 }
 
+
+// FP32 heat step with an asynchronous plane pipeline.  FP32 arithmetic is nearly free on this
+// GPU, so the kernel is bound by how many bytes it keeps in flight: each block streams planes
+// of T and lambda (its 32x8 tile plus a one-cell halo) into a ring of NS shared-memory stages
+// with cp.async, NS-2 planes ahead of the plane it computes, using no registers for the loads
+// in flight.  Each thread then evaluates its cell's six face fluxes straight from shared
+// memory (recomputing a shared face costs three FP32 operations, cheaper than exchanging it).
+constexpr int NS = 5;              // pipeline stages (planes resident or in flight)
+constexpr int HX = BX + 2, HY = BY + 2;
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__global__ void __launch_bounds__(BX* BY) heat_step_f32_async_kernel(const float* __restrict__ tin,
+                                                                      float* __restrict__ tout,
+                                                                      const float* __restrict__ lam, int sy, long sz,
+                                                                      int nx, int ny, int nz, int zchunk, float w0,
+                                                                      float w1, float w2) {
+  __shared__ float sT[NS][HY][HX];
+  __shared__ float sL[NS][HY][HX];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int z0 = blockIdx.z * zchunk;
+  const int z1 = min(z0 + zchunk, nz);
+  // copy plane p (interior z index, -1..nz) of both fields into stage p % NS; tile cells past the
+  // +ghost column/row clamp to it (they exist and are never used)
+  auto issue = [&](int p) {
+    const int st = ((p % NS) + NS) % NS;
+    for (int k = tid; k < HX * HY; k += BX * BY) {
+      const int r = k / HX, c = k - r * HX;
+      const int gx = min(x0 - 1 + c, nx), gy = min(y0 - 1 + r, ny);
+      const long off = (long)gx + (long)sy * gy + sz * p;
+      cp_async4(&sT[st][r][c], tin + off);
+      cp_async4(&sL[st][r][c], lam + off);
+    }
+  };
+  // prologue: planes z0-1 .. z0+NS-3 (NS-1 groups)
+  for (int i = 0; i < NS - 1; ++i) {
+    const int p = z0 - 1 + i;
+    if (p <= z1) issue(p);
+    cp_async_commit();
+  }
+  const int x = x0 + tx, y = y0 + ty;
+  const bool active = x < nx && y < ny;
+  for (int z = z0; z < z1; ++z) {
+    cp_async_wait<NS - 3>();  // planes up to z+1 have landed (this thread's copies)
+    __syncthreads();          // ... and everyone's
+    if (active) {
+      const int sm = (((z - 1) % NS) + NS) % NS, s0 = z % NS, sp = (z + 1) % NS;
+      const int r = ty + 1, c = tx + 1;
+      const float t = sT[s0][r][c], l = sL[s0][r][c];
+      const float fxl = (sL[s0][r][c - 1] + l) * (t - sT[s0][r][c - 1]);
+      const float fxh = (l + sL[s0][r][c + 1]) * (sT[s0][r][c + 1] - t);
+      const float fyl = (sL[s0][r - 1][c] + l) * (t - sT[s0][r - 1][c]);
+      const float fyh = (l + sL[s0][r + 1][c]) * (sT[s0][r + 1][c] - t);
+      const float fzl = (sL[sm][r][c] + l) * (t - sT[sm][r][c]);
+      const float fzh = (l + sL[sp][r][c]) * (sT[sp][r][c] - t);
+      const float v = t + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fzl);
+      store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
+    }
+    __syncthreads();  // stage of plane z-1 is free
+    const int p = z - 1 + NS;
+    if (p <= z1) issue(p);
+    cp_async_commit();
+  }
+  cp_async_wait<0>();
+}
+
 int check_heat(const nebo_field* T, const nebo_field* To, const nebo_field* L, const char* what) {
   int rc;
   if ((rc = check_field(T, what)) || (rc = check_field(To, what)) || (rc = check_field(L, what))) return rc;
@@ -199,8 +268,8 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
                                                                               vin.sz, n[0], n[1], n[2], zchunk, p);
   } else {
     LaunchScope ls("heat_step_f32", s);
-    heat_step_kernel<float, FastF, MODE_WEIGHTED><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz,
-                                                                         n[0], n[1], n[2], zchunk, p);
+    heat_step_f32_async_kernel<<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz, n[0], n[1], n[2],
+                                                      zchunk, p.w[0], p.w[1], p.w[2]);
   }
   NEBO_LAUNCH_CHECK("nebo_heat_step");
   return NEBO_OK;

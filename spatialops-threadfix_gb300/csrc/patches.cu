@@ -5,9 +5,8 @@
 // The reference advances patches one `<<=` at a time from the caller's patch loop (Uintah/
 // Wasatch-style; spatialops/NeboLhs.h:29-41 launches a 16x16 grid per expression), paying a
 // launch and a tail per patch and expression.  Here:
-//   * all patches live in one arena per buffer, each a ghosted window, x fastest: the FP64 states,
-//     plus, in FP32 mode, FP32 copies that the stencil sweeps read (the state itself is still
-//     accumulated in FP64, so rounding to FP32 never compounds from step to step);
+//   * all patches live in one arena per buffer, each a ghosted window, x fastest: FP64 states,
+//     or FP32 states (half the bytes), or two-float states (FP32 arithmetic, ~48-bit state);
 //   * a work list enumerates (patch, x-tile, y-tile, z-chunk) items; a fixed grid of blocks
 //     (a multiple of the SM count) strides through it, so small and large patches share SMs;
 //   * tiles are TX x TY = 256 cells per plane with TX in {16, 32, 64} per patch (the autotuner
@@ -51,8 +50,7 @@ struct WorkItem {
 
 // Storage and arithmetic of the three precision modes.
 //   PMODE_F64   value = double, fluxes double, round-to-nearest FP64 ops (bit-exact form)
-//   PMODE_F32   value = float copy read by the stencil; flux arithmetic float; the state is
-//               accumulated in FP64 (acc_src -> acc_dst)
+//   PMODE_F32   value = float: FP32 storage and arithmetic (half the bytes of FP64)
 //   PMODE_F32X2 value = float2 (hi, lo): the state as an unevaluated sum of two floats (~48-bit
 //               significand); differences (hb-ha)+(lb-la), fluxes and the update in float, the
 //               update added with an error-free two-sum.  No FP64 operation on the sweep.
@@ -97,20 +95,16 @@ __device__ __forceinline__ float2 ff_add(float2 v, float inc) {
 template <typename T>
 __device__ __forceinline__ void store_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
                                              T v) {
-  int xs[3], ys[3], zs[3];
-  int cx = 0, cy = 0, cz = 0;
-  xs[cx++] = x;
-  if (x == 0) xs[cx++] = nx;
-  if (x == nx - 1) xs[cx++] = -1;
-  ys[cy++] = y;
-  if (y == 0) ys[cy++] = ny;
-  if (y == ny - 1) ys[cy++] = -1;
-  zs[cz++] = z;
-  if (z == 0) zs[cz++] = nz;
-  if (z == nz - 1) zs[cz++] = -1;
-  for (int k = 0; k < cz; ++k)
-    for (int j = 0; j < cy; ++j)
-      for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+  base[(long)x + (long)sy * y + sz * z] = v;
+  if (x != 0 && x != nx - 1 && y != 0 && y != ny - 1 && z != 0 && z != nz - 1) return;
+  // a boundary cell: also write its periodic ghost images (up to 7 more cells; n >= 2 per axis)
+  const int ax = x == 0 ? nx : -1, ay = y == 0 ? ny : -1, az = z == 0 ? nz : -1;
+  const int m = (x == 0 || x == nx - 1) | ((y == 0 || y == ny - 1) << 1) | ((z == 0 || z == nz - 1) << 2);
+  for (int b = 1; b < 8; ++b) {
+    if (b & ~m) continue;
+    const int xx = (b & 1) ? ax : x, yy = (b & 2) ? ay : y, zz = (b & 4) ? az : z;
+    base[(long)xx + (long)sy * yy + sz * zz] = v;
+  }
 }
 
 template <typename S>
@@ -121,9 +115,7 @@ template <int M>
 __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev* __restrict__ patches,
                                                                   const WorkItem* __restrict__ items, int nitems,
                                                                   const typename PM<M>::S* __restrict__ src,
-                                                                  typename PM<M>::S* __restrict__ dst,
-                                                                  const double* __restrict__ acc_src,
-                                                                  double* __restrict__ acc_dst) {
+                                                                  typename PM<M>::S* __restrict__ dst) {
   typedef typename PM<M>::S S;
   typedef typename PM<M>::F F;
   __shared__ F sfx[2][PT_MAX_TY * (PT_MAX_TX + 1) / 4 + 64];  // TY*(TX+1) <= 16*17, 8*33, 4*65
@@ -179,10 +171,7 @@ __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev
         if constexpr (M == PMODE_F64) {
           store_images(tout, sy, sz, x, y, z, nx, ny, nz, __dadd_rn(tc, __dmul_rn(hdt, s)));
         } else if constexpr (M == PMODE_F32) {
-          const long c = P.offset + interior + at(x, y, z);
-          const double v = acc_src[c] + P.hdt * (double)s;
-          store_images(acc_dst + P.offset + interior, sy, sz, x, y, z, nx, ny, nz, v);
-          store_images(tout, sy, sz, x, y, z, nx, ny, nz, (float)v);
+          store_images(tout, sy, sz, x, y, z, nx, ny, nz, tc + hdt * s);
         } else {
           store_images(tout, sy, sz, x, y, z, nx, ny, nz, ff_add(tc, hdt * s));
         }
@@ -205,7 +194,7 @@ struct PatchSet {
   std::vector<int> log2tx;
   long long total = 0;  // elements per arena
   void* arena[2] = {nullptr, nullptr};    // FP64 states
-  float* arena32[2] = {nullptr, nullptr};  // FP32 stencil copies (FP32 mode)
+  float* arena32[2] = {nullptr, nullptr};  // FP32 states (FP32 mode)
   float2* arena2[2] = {nullptr, nullptr};  // two-float states (FP32X2 mode)
   PatchDev* d_patches = nullptr;
   WorkItem* d_items = nullptr;
@@ -271,15 +260,15 @@ int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parit
   LaunchScope ls(ps.dtype == NEBO_F64 ? "patches_step_f64" : (ps.dtype == NEBO_F32 ? "patches_step_f32" : "patches_step_f32x2"), s);
   const int grid = std::min(nitems, ps.grid);
   if (ps.dtype == NEBO_F64)
-    patches_step_kernel<PMODE_F64><<<grid, PT_THREADS, 0, s>>>(
-        ps.d_patches, items, nitems, (const double*)ps.arena[parity], (double*)ps.arena[parity ^ 1], nullptr, nullptr);
+    patches_step_kernel<PMODE_F64><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
+                                                               (const double*)ps.arena[parity],
+                                                               (double*)ps.arena[parity ^ 1]);
   else if (ps.dtype == NEBO_F32)
-    patches_step_kernel<PMODE_F32><<<grid, PT_THREADS, 0, s>>>(
-        ps.d_patches, items, nitems, ps.arena32[parity], ps.arena32[parity ^ 1], (const double*)ps.arena[parity],
-        (double*)ps.arena[parity ^ 1]);
+    patches_step_kernel<PMODE_F32><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, ps.arena32[parity],
+                                                               ps.arena32[parity ^ 1]);
   else
     patches_step_kernel<PMODE_F32X2><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, ps.arena2[parity],
-                                                                 ps.arena2[parity ^ 1], nullptr, nullptr);
+                                                                 ps.arena2[parity ^ 1]);
   NEBO_LAUNCH_CHECK("nebo_patchset_run");
   return NEBO_OK;
 }
@@ -295,6 +284,10 @@ __global__ void patches_split_kernel(const double* __restrict__ a, float2* __res
     const float hi = (float)a[i];
     b[i] = make_float2(hi, (float)(a[i] - (double)hi));
   }
+}
+__global__ void patches_widen_kernel(const float* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
 }
 __global__ void patches_join_kernel(const float2* __restrict__ a, double* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -408,7 +401,7 @@ extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, neb
     int rc = nebo::fill_periodic_any(&f, (cudaStream_t)stream);
     if (rc) return rc;
   }
-  if (ps->dtype == NEBO_F32) {  // the FP32 stencil copy of the state
+  if (ps->dtype == NEBO_F32) {  // the FP32 working state
     LaunchScope ls("patches_cast_f32", (cudaStream_t)stream);
     patches_cast_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>((const double*)ps->arena[which],
                                                                          ps->arena32[which], (size_t)ps->total);
@@ -422,14 +415,18 @@ extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, neb
   return NEBO_OK;
 }
 
-// Bring the state of arena `which` into its FP64 arena (FP32X2 mode joins hi + lo; the other
-// modes already keep the FP64 state there).
+// Bring the state of arena `which` into its FP64 arena (FP32 mode widens, FP32X2 joins hi + lo;
+// FP64 mode already keeps its state there).
 extern "C" int nebo_patchset_sync(const nebo_patchset* ps, int which, nebo_stream_t stream) {
   if (!ps || (which != 0 && which != 1)) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_patchset_sync");
-  if (ps->dtype != NEBO_F32X2) return NEBO_OK;
-  LaunchScope ls("patches_join_f32x2", (cudaStream_t)stream);
-  patches_join_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena2[which], (double*)ps->arena[which],
-                                                                       (size_t)ps->total);
+  if (ps->dtype == NEBO_F64) return NEBO_OK;
+  LaunchScope ls("patches_to_f64", (cudaStream_t)stream);
+  if (ps->dtype == NEBO_F32X2)
+    patches_join_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena2[which], (double*)ps->arena[which],
+                                                                         (size_t)ps->total);
+  else
+    patches_widen_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena32[which],
+                                                                          (double*)ps->arena[which], (size_t)ps->total);
   NEBO_LAUNCH_CHECK("nebo_patchset_sync");
   return NEBO_OK;
 }

@@ -58,8 +58,8 @@ int check_periodic_patch(const nebo_field* f, int g, const char* what) {
       return fail(NEBO_ERR_INVALID, "Nebo error in %s: periodic patch cannot carry BC cells", what);
     if (f->offset[i] != 0 || f->extent[i] != f->glob[i])
       return fail(NEBO_ERR_INVALID, "Nebo error in %s: window must cover the allocation", what);
-    if (f->extent[i] - 2 * g < g)
-      return fail(NEBO_ERR_INVALID, "Nebo error in %s: interior smaller than the ghost depth", what);
+    if (f->extent[i] - 2 * g < (g > 2 ? g : 2))
+      return fail(NEBO_ERR_INVALID, "Nebo error in %s: periodic interior needs at least max(2, ghosts) cells", what);
   }
   return NEBO_OK;
 }

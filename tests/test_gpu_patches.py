@@ -53,8 +53,8 @@ def test_patches_autotune_keeps_results():
 
 
 @pytest.mark.parametrize("dtype,steps,tol", [
-    ("f32", 200, 5e-5),     # FP32 stencil copy, FP64 state (halves the stencil bytes)
-    ("f32x2", 200, 1e-5),   # two-float state, FP32 arithmetic only: the 1e-5 target at 200 steps
+    ("f32", 200, 1e-5),     # FP32 storage and arithmetic: the batched FP32 form (half the bytes)
+    ("f32x2", 200, 1e-6),   # two-float state, FP32 arithmetic only
 ])
 def test_patches_fp32_error_vs_fp64_oracle(dtype, steps, tol):
     rng = np.random.default_rng(5)
