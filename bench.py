@@ -160,16 +160,50 @@ class Deep:
         self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
 
     def step(self):
+        self._chain(self.A, self.B, self.C, self.words)
+
+    def _chain(self, A, B, C, words):
         N = self.N
-        N.deep_chain(self.A, self.B, self.C, self.words, self.out, self.filt)
+        N.deep_chain(A, B, C, words, self.out, self.filt)
         N.reduce_all(self.filt, False, self.red)  # nebo_sum, nebo_max (and min), nebo_norm in one pass
 
+    # e2e: every step uploads its inputs (a, b, c, mask words) from pinned host memory and reads
+    # its reductions back.  The uploads run on a copy stream into two alternating device input
+    # sets, so step k+1's upload overlaps step k's kernels; each upload still happens inside the
+    # timed region, after the start event.
+    def e2e_begin(self, start_event):
+        import torch
+
+        N, n = self.N, self.n
+        if not hasattr(self, "sets"):
+            self.sets = [(self.A, self.B, self.C, self.words),
+                         (N.Field("SVol", n, 1), N.Field("XVol", n, 1), N.Field("XVol", n, 1),
+                          torch.empty_like(self.words))]
+            self.copy_stream = torch.cuda.Stream()
+            self.ready = [torch.cuda.Event(), torch.cuda.Event()]
+            self.free = [torch.cuda.Event(), torch.cuda.Event()]
+        self.copy_stream.wait_event(start_event)
+        self.k = 0
+
     def step_e2e(self):
-        for f, h in zip((self.A, self.B, self.C), self.host):
-            f.tensor.copy_(h, non_blocking=True)
-        self.words.copy_(self.host_mask, non_blocking=True)
-        self.step()
+        import torch
+
+        i = self.k % 2
+        A, B, C, words = self.sets[i]
+        cur = torch.cuda.current_stream()
+        cs = self.copy_stream
+        with torch.cuda.stream(cs):
+            if self.k >= 2:
+                cs.wait_event(self.free[i])  # step k-2 is done reading this set
+            for f, h in zip((A, B, C), self.host):
+                f.tensor.copy_(h, non_blocking=True)
+            words.copy_(self.host_mask, non_blocking=True)
+            self.ready[i].record(cs)
+        cur.wait_event(self.ready[i])
+        self._chain(A, B, C, words)
+        self.free[i].record(cur)
         self.host_red.copy_(self.red, non_blocking=True)
+        self.k += 1
 
 
 class Heat:
@@ -451,10 +485,16 @@ def main():
 
     # e2e: host buffers, copies inside the timed region
     e_steps = max(3, min(args.steps, 50))
+    if hasattr(W, "e2e_begin"):
+        warm = torch.cuda.Event()
+        warm.record(stream)
+        W.e2e_begin(warm)
     for _ in range(2):
         W.step_e2e()
     barrier()
     e0.record(stream)
+    if hasattr(W, "e2e_begin"):
+        W.e2e_begin(e0)
     for _ in range(e_steps):
         W.step_e2e()
     e1.record(stream)
@@ -502,7 +542,9 @@ def main():
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (129 MB); no flush between steps"},
         "e2e": {"value": e2e_value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": W.h2d_bytes,
-                "d2h_bytes_per_step": W.d2h_bytes, "steps": e_steps},
+                "d2h_bytes_per_step": W.d2h_bytes, "steps": e_steps,
+                "copies": ("uploads on a copy stream into 2 alternating input sets, overlapping the previous "
+                           "step's kernels" if hasattr(W, "e2e_begin") else "serial with the kernels")},
         "gpu_launches": int(launches),
         "roofline": roof,
         "cpu_baseline": cpu,

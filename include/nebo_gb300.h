@@ -155,9 +155,11 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
                     const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
                     double dx, nebo_stream_t stream);
 
-/* Element-wise FP64 exp (fn 0) or sin (fn 1) with the table-driven functions nebo_deep_chain
- * uses (Tang's table method for exp; a sin/cos(k pi/64) table with short Taylor polynomials for
- * sin): about half the FP64 instructions of general-purpose versions, within 2 ulp. */
+/* Element-wise FP64 exp (fn 0) or sin (fn 1) with the functions nebo_deep_chain uses: the
+ * argument reduction in FP64 (three instructions), the table lookup (Tang's 2^(j/64) for exp,
+ * sin/cos(k pi/64) for sin) and the polynomials in 64-bit fixed point on the integer pipe.
+ * Within one ulp of the exact result for |x| < 708 (exp) and |x| < 2^20 (sin); other arguments
+ * use CUDA's exp and sin. */
 int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ batched patches

@@ -8,8 +8,8 @@
 // recomputing the inner interpolant twice; here the chain collapses to one 4-point stencil on a,
 //   I(G(I(a)))[i] = (g1/4) * ((a[i+1] - a[i-1]) + (a[i] - a[i-2])),
 // a reassociation of the same sum (FP64 error a few ulp of max|a|, inside the 1e-13 relative
-// bound).  exp and sin are the table-driven FP64 functions of fp64_fast.cuh (about half the FP64
-// instructions of the general-purpose ones; at most 2 ulp from CUDA's exp and sin).
+// bound).  exp and sin are the integer-pipe functions of fp64_int.cuh: FP64 only for the argument
+// reduction, 64-bit fixed point for the polynomials (within one ulp; at most 2 ulp from CUDA's).
 //
 // Write regions follow calculate_actual_ghost (NeboBasic.h:61-100): with one ghost layer the
 // chain's x ghost is -1, so `out` is written on x in [1, n) and y, z in [-1, n+1); the filter's
@@ -18,7 +18,7 @@
 // Kernel 1 is bound by FP64 issue (exp + sin); kernel 2 sums the 27 points separably
 // (x, then y from shared memory, then z from a register queue while marching in z).
 #include "common.cuh"
-#include "fp64_fast.cuh"
+#include "fp64_int.cuh"
 
 namespace nebo {
 namespace {
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256) deep_out_kernel(const double* __restrict_
       v = 0.0;
     } else {
       const double igi = q * ((__ldg(a + i + 1) - __ldg(a + i - 1)) + (__ldg(a + i) - __ldg(a + i - 2)));
-      v = fma(igi, fastmath::exp_fast(__ldg(b + i)), fastmath::sin_fast(__ldg(c + i)));
+      v = fma(igi, fixmath::exp_i(__ldg(b + i)), fixmath::sin_i(__ldg(c + i)));
     }
     out[i] = v;
   }
@@ -111,7 +111,7 @@ extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const n
   int rc = check_deep(a, b, c, out, filt);
   if (rc) return rc;
   if (!mask_words) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_deep_chain: null mask");
-  if (fastmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_deep_chain: math tables upload");
+  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_deep_chain: math tables upload");
   int n[3];
   interior_extent(*a, n);
   cudaStream_t s = (cudaStream_t)stream;
@@ -149,19 +149,19 @@ extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const n
   return NEBO_OK;
 }
 
-// Element-wise FP64 exp / sin of the table-driven functions (fn 0: exp, 1: sin).
+// Element-wise FP64 exp / sin of the integer-pipe functions (fn 0: exp, 1: sin).
 namespace nebo {
 namespace {
 __global__ void fastmath_kernel(int fn, const double* __restrict__ x, double* __restrict__ y, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    y[i] = fn == 0 ? fastmath::exp_fast(x[i]) : fastmath::sin_fast(x[i]);
+    y[i] = fn == 0 ? fixmath::exp_i(x[i]) : fixmath::sin_i(x[i]);
 }
 }  // namespace
 }  // namespace nebo
 
 extern "C" int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream) {
   if ((fn != 0 && fn != 1) || (n && (!x || !y))) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_fastmath_eval");
-  if (fastmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_fastmath_eval: math tables upload");
+  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_fastmath_eval: math tables upload");
   if (!n) return NEBO_OK;
   cudaStream_t s = (cudaStream_t)stream;
   LaunchScope ls("fastmath_eval", s);

@@ -66,12 +66,10 @@ __device__ __forceinline__ T face_flux(T la, T lb, T ta, T tb, T c0, T c1) {
   }
 }
 
+// The periodic ghost images of boundary cell (x,y,z) (up to 7 cells; n >= 2 per axis).
 template <typename T>
-__device__ __forceinline__ void store_with_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny,
+__device__ __forceinline__ void store_images_only(T* base, int sy, long sz, int x, int y, int z, int nx, int ny,
                                                   int nz, T v) {
-  base[(long)x + (long)sy * y + sz * z] = v;
-  if (x != 0 && x != nx - 1 && y != 0 && y != ny - 1 && z != 0 && z != nz - 1) return;
-  // a boundary cell: also write its periodic ghost images (up to 7 more cells; n >= 2 per axis)
   const int ax = x == 0 ? nx : -1, ay = y == 0 ? ny : -1, az = z == 0 ? nz : -1;
   const int m = (x == 0 || x == nx - 1) | ((y == 0 || y == ny - 1) << 1) | ((z == 0 || z == nz - 1) << 2);
   for (int b = 1; b < 8; ++b) {
@@ -79,6 +77,14 @@ __device__ __forceinline__ void store_with_images(T* base, int sy, long sz, int 
     const int xx = (b & 1) ? ax : x, yy = (b & 2) ? ay : y, zz = (b & 4) ? az : z;
     base[(long)xx + (long)sy * yy + sz * zz] = v;
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_with_images(T* base, int sy, long sz, int x, int y, int z, int nx, int ny,
+                                                  int nz, T v) {
+  base[(long)x + (long)sy * y + sz * z] = v;
+  if (x != 0 && x != nx - 1 && y != 0 && y != ny - 1 && z != 0 && z != nz - 1) return;
+  store_images_only(base, sy, sz, x, y, z, nx, ny, nz, v);
 }
 
 template <typename T, class A, int MODE>
@@ -157,71 +163,107 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
 // FP32 heat step with an asynchronous plane pipeline.  FP32 arithmetic is nearly free on this
 // GPU, so the kernel is bound by how many bytes it keeps in flight: each block streams planes
 // of T and lambda (its 32x8 tile plus a one-cell halo) into a ring of NS shared-memory stages
-// with cp.async, NS-2 planes ahead of the plane it computes, using no registers for the loads
-// in flight.  Each thread then evaluates its cell's six face fluxes straight from shared
+// with cp.async, up to NS-3 planes ahead of the plane it computes, using no registers for the
+// loads in flight.  Each thread then evaluates its cell's six face fluxes straight from shared
 // memory (recomputing a shared face costs three FP32 operations, cheaper than exchanging it).
-constexpr int NS = 5;              // pipeline stages (planes resident or in flight)
+//
+// Ring schedule: the prologue issues planes z0-1 .. z0+NS-3 (one commit group each); iteration z
+// waits until at most NS-4 groups are pending (so planes up to z+1 have landed), syncs the block,
+// issues plane z+NS-2 into the stage of plane z-2 (last read in iteration z-1, before the sync),
+// then computes from the stages of planes z-1, z, z+1.
+constexpr int NS = 8;              // pipeline stages (planes resident or in flight)
 constexpr int HX = BX + 2, HY = BY + 2;
 
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
                : "memory");
 }
+__device__ __forceinline__ void cp_async4_s(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-__global__ void __launch_bounds__(BX* BY) heat_step_f32_async_kernel(const float* __restrict__ tin,
+__global__ void __launch_bounds__(BX* BY, 8) heat_step_f32_async_kernel(const float* __restrict__ tin,
                                                                       float* __restrict__ tout,
                                                                       const float* __restrict__ lam, int sy, long sz,
                                                                       int nx, int ny, int nz, int zchunk, float w0,
                                                                       float w1, float w2) {
-  __shared__ float sT[NS][HY][HX];
-  __shared__ float sL[NS][HY][HX];
+  constexpr int PLANE = HX * HY;                            // floats per stage and field
+  constexpr int NCOPY = (PLANE + BX * BY - 1) / (BX * BY);  // copy slots per thread
+  __shared__ __align__(16) float sT[NS * PLANE];
+  __shared__ __align__(16) float sL[NS * PLANE];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
   const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
   const int z0 = blockIdx.z * zchunk;
   const int z1 = min(z0 + zchunk, nz);
-  // copy plane p (interior z index, -1..nz) of both fields into stage p % NS; tile cells past the
-  // +ghost column/row clamp to it (they exist and are never used)
-  auto issue = [&](int p) {
-    const int st = ((p % NS) + NS) % NS;
-    for (int k = tid; k < HX * HY; k += BX * BY) {
-      const int r = k / HX, c = k - r * HX;
-      const int gx = min(x0 - 1 + c, nx), gy = min(y0 - 1 + r, ny);
-      const long off = (long)gx + (long)sy * gy + sz * p;
-      cp_async4(&sT[st][r][c], tin + off);
-      cp_async4(&sL[st][r][c], lam + off);
+  // this thread's copy slots: tile cell k = tid + j*BX*BY of the (HY x HX) halo tile; cells past
+  // the +ghost column/row clamp to it (they exist and are never used)
+  int goff[NCOPY];  // within a plane (a plane holds fewer than 2^31 cells)
+  uint32_t soff[NCOPY];
+#pragma unroll
+  for (int j = 0; j < NCOPY; ++j) {
+    const int k = min(tid + j * BX * BY, PLANE - 1);
+    const int r = k / HX, c = k - r * HX;
+    goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
+    soff[j] = (uint32_t)(k * sizeof(float));
+  }
+  const uint32_t sT0 = (uint32_t)__cvta_generic_to_shared(sT), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
+  auto issue = [&](int p) {  // plane p (interior z index, -1..nz) into stage p % NS
+    if (p > z1) return;
+    const uint32_t st = (uint32_t)((p + NS) % NS) * (PLANE * sizeof(float));
+    const float* tp = tin + sz * p;
+    const float* lp = lam + sz * p;
+#pragma unroll
+    for (int j = 0; j < NCOPY; ++j) {
+      if (j == NCOPY - 1 && tid + j * BX * BY >= PLANE) break;
+      cp_async4_s(sT0 + st + soff[j], tp + goff[j]);
+      cp_async4_s(sL0 + st + soff[j], lp + goff[j]);
     }
   };
-  // prologue: planes z0-1 .. z0+NS-3 (NS-1 groups)
+#pragma unroll 1
   for (int i = 0; i < NS - 1; ++i) {
-    const int p = z0 - 1 + i;
-    if (p <= z1) issue(p);
+    issue(z0 - 1 + i);
     cp_async_commit();
   }
   const int x = x0 + tx, y = y0 + ty;
   const bool active = x < nx && y < ny;
-  for (int z = z0; z < z1; ++z) {
-    cp_async_wait<NS - 3>();  // planes up to z+1 have landed (this thread's copies)
-    __syncthreads();          // ... and everyone's
-    if (active) {
-      const int sm = (((z - 1) % NS) + NS) % NS, s0 = z % NS, sp = (z + 1) % NS;
-      const int r = ty + 1, c = tx + 1;
-      const float t = sT[s0][r][c], l = sL[s0][r][c];
-      const float fxl = (sL[s0][r][c - 1] + l) * (t - sT[s0][r][c - 1]);
-      const float fxh = (l + sL[s0][r][c + 1]) * (sT[s0][r][c + 1] - t);
-      const float fyl = (sL[s0][r - 1][c] + l) * (t - sT[s0][r - 1][c]);
-      const float fyh = (l + sL[s0][r + 1][c]) * (sT[s0][r + 1][c] - t);
-      const float fzl = (sL[sm][r][c] + l) * (t - sT[sm][r][c]);
-      const float fzh = (l + sL[sp][r][c]) * (sT[sp][r][c] - t);
-      const float v = t + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fzl);
-      store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
-    }
-    __syncthreads();  // stage of plane z-1 is free
-    const int p = z - 1 + NS;
-    if (p <= z1) issue(p);
+  const bool edge_xy = x == 0 || x == nx - 1 || y == 0 || y == ny - 1;
+  const int ci = (ty + 1) * HX + tx + 1;  // this cell in a stage
+  float tc = 0.f, lc = 0.f, fzl = 0.f;
+  float* out = tout + (long)x + (long)sy * y + sz * z0;
+#pragma unroll 1
+  for (int z = z0; z < z1; ++z, out += sz) {
+    cp_async_wait<NS - 4>();  // planes up to z+1 have landed (this thread's copies)
+    __syncthreads();          // ... and everyone's; plane z-2's stage is no longer read
+    issue(z + NS - 2);
     cp_async_commit();
+    const float* T0 = sT + ((z + NS) % NS) * PLANE;
+    const float* L0 = sL + ((z + NS) % NS) * PLANE;
+    const float* Tp = sT + ((z + 1) % NS) * PLANE;
+    const float* Lp = sL + ((z + 1) % NS) * PLANE;
+    if (z == z0) {  // first plane of the chunk: centre and low z face from the stages
+      const float* Tm = sT + ((z - 1 + NS) % NS) * PLANE;
+      const float* Lm = sL + ((z - 1 + NS) % NS) * PLANE;
+      tc = T0[ci];
+      lc = L0[ci];
+      fzl = (Lm[ci] + lc) * (tc - Tm[ci]);
+    }
+    const float tn = Tp[ci], ln = Lp[ci];
+    const float fzh = (lc + ln) * (tn - tc);
+    if (active) {
+      const float fxl = (L0[ci - 1] + lc) * (tc - T0[ci - 1]);
+      const float fxh = (lc + L0[ci + 1]) * (T0[ci + 1] - tc);
+      const float fyl = (L0[ci - HX] + lc) * (tc - T0[ci - HX]);
+      const float fyh = (lc + L0[ci + HX]) * (T0[ci + HX] - tc);
+      const float v = tc + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fzl);
+      *out = v;
+      if (edge_xy || z == 0 || z == nz - 1) store_images_only(tout, sy, sz, x, y, z, nx, ny, nz, v);
+    }
+    tc = tn;
+    lc = ln;
+    fzl = fzh;
   }
   cp_async_wait<0>();
 }
@@ -267,9 +309,21 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
       heat_step_kernel<double, ExactD, MODE_REFERENCE><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                               vin.sz, n[0], n[1], n[2], zchunk, p);
   } else {
+    // one full wave: as many z chunks as the resident blocks allow (each chunk re-reads two
+    // halo planes and fills the ring once, so more chunks than slots only cost)
+    static int per_sm = 0;
+    if (!per_sm) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat_step_f32_async_kernel, BX * BY, 0) !=
+              cudaSuccess ||
+          per_sm < 1)
+        per_sm = 1;
+    }
+    int ch = max(1, min(num_sms() * per_sm / (gxb * gyb), (n[2] + 7) / 8));
+    const int zc = (n[2] + ch - 1) / ch;
+    ch = (n[2] + zc - 1) / zc;
     LaunchScope ls("heat_step_f32", s);
-    heat_step_f32_async_kernel<<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz, n[0], n[1], n[2],
-                                                      zchunk, p.w[0], p.w[1], p.w[2]);
+    heat_step_f32_async_kernel<<<dim3(gxb, gyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz, n[0],
+                                                                    n[1], n[2], zc, p.w[0], p.w[1], p.w[2]);
   }
   NEBO_LAUNCH_CHECK("nebo_heat_step");
   return NEBO_OK;

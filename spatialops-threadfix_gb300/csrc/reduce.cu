@@ -1,8 +1,9 @@
 // Reductions nebo_sum / nebo_max / nebo_min / nebo_norm (and _interior) over one field
 // (spatialops/NeboReductions.h:45-240).  The reference folds serially on the CPU; here a
 // two-pass, deterministic tree runs on the device:
-//   pass 1: one block per slice of rows, x-contiguous loads, per-thread Neumaier-compensated
-//           FP64 sums (or max/min), warp shuffles, one partial per block;
+//   pass 1: a warp per row, 8 independent loads per lane, pairwise sums of each batch folded
+//           into per-thread Neumaier-compensated FP64 sums (or max/min), warp shuffles, one
+//           partial per block;
 //   pass 2: one block combines the partials in a fixed order.
 // FP32 fields are accumulated in FP64.  max/min use the reference's comparisons
 // ((r < v) ? v : r and (r > v) ? v : r), so they are exact.
@@ -73,27 +74,63 @@ __device__ Acc block_reduce(Acc a, int op) {
   return a;
 }
 
+// Every element of the region's rows, a warp per row (rows strided over all warps of the grid),
+// each lane issuing 8 independent loads before it uses them; f8(v[8]) gets each full batch of 8
+// (lanes 32 apart), f1(v) each element of the row tails.
+template <typename T, class F8, class F1>
+__device__ __forceinline__ void walk_rows(const T* __restrict__ base, int sy, long sz, int x0, int x1, int y0, int ny,
+                                          int z0, int nrows, F8&& f8, F1&& f1) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < nrows; r += nwarps) {
+    const int z = r / ny, y = r - z * ny;
+    const T* row = base + (long)sy * (y0 + y) + sz * (z0 + z);
+    int x = x0 + lane;
+    for (; x + 7 * 32 < x1; x += 8 * 32) {
+      double v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = (double)__ldg(row + x + 32 * i);
+      f8(v);
+    }
+    for (; x < x1; x += 32) f1((double)__ldg(row + x));
+  }
+}
+
+// Sum of 8 in pairs (7 FP64 adds), and of their squares (4 multiplies folded into 4 FMAs).
+__device__ __forceinline__ double sum8(const double* v) {
+  return ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+}
+__device__ __forceinline__ double sumsq8(const double* v) {
+  const double a = fma(v[0], v[0], v[1] * v[1]), b = fma(v[2], v[2], v[3] * v[3]);
+  const double c = fma(v[4], v[4], v[5] * v[5]), d = fma(v[6], v[6], v[7] * v[7]);
+  return (a + b) + (c + d);
+}
+
+// Pass 1 of one reduction: each thread folds its batches (pairwise within a batch, then into a
+// Neumaier-compensated running sum; max/min with the reference's comparisons).
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) reduce_rows_kernel(const T* __restrict__ base, int sy, long sz, int x0,
                                                                   int x1, int y0, int ny, int z0, long nrows, int op,
                                                                   Acc* __restrict__ partials) {
   Acc a = identity(op);
-  for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
-    const int y = y0 + (int)(r % ny);
-    const int z = z0 + (int)(r / ny);
-    const T* row = base + (long)sy * y + sz * z;
-    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-      const double v = (double)__ldg(row + x);
-      if (op == NEBO_RED_MAX)
-        a.s = (a.s < v) ? v : a.s;
-      else if (op == NEBO_RED_MIN)
-        a.s = (a.s > v) ? v : a.s;
-      else if (op == NEBO_RED_NORM)
-        two_sum_add(a, v * v);
-      else
-        two_sum_add(a, v);
-    }
-  }
+  auto one = [&](double v) {
+    if (op == NEBO_RED_MAX)
+      a.s = (a.s < v) ? v : a.s;
+    else if (op == NEBO_RED_MIN)
+      a.s = (a.s > v) ? v : a.s;
+    else
+      two_sum_add(a, op == NEBO_RED_NORM ? v * v : v);
+  };
+  walk_rows(base, sy, sz, x0, x1, y0, ny, z0, (int)nrows,
+            [&](const double* v) {
+              if (op == NEBO_RED_SUM)
+                two_sum_add(a, sum8(v));
+              else if (op == NEBO_RED_NORM)
+                two_sum_add(a, sumsq8(v));
+              else
+                for (int i = 0; i < 8; ++i) one(v[i]);
+            },
+            one);
   a = block_reduce(a, op);
   if (threadIdx.x == 0) partials[blockIdx.x] = a;
 }
@@ -304,10 +341,6 @@ struct Acc4 {
   long long mx, mn;     // order-preserving keys of max and min
 };
 
-__device__ __forceinline__ long long order_key(double v) {
-  long long b = __double_as_longlong(v);
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
 __device__ __forceinline__ double from_key(long long k) {
   return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
 }
@@ -360,21 +393,26 @@ __global__ void __launch_bounds__(RED_THREADS) reduce4_rows_kernel(const T* __re
                                                                    Acc4* __restrict__ partials) {
   double s = 0.0, q = 0.0;
   long long mx = LLONG_MIN, mn = LLONG_MAX;
-  for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
-    const int y = y0 + (int)(r % ny);
-    const int z = z0 + (int)(r / ny);
-    const T* row = base + (long)sy * y + sz * z;
-    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-      const double v = (double)__ldg(row + x);
-      s += v;
-      q = fma(v, v, q);
-      if (v == v) {  // NaNs never win a comparison in the reference's fold
-        const long long k = order_key(v);
-        mx = k > mx ? k : mx;
-        mn = k < mn ? k : mn;
-      }
+  auto keys = [&](double v) {
+    const long long b = __double_as_longlong(v);
+    if ((b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) {  // not NaN: NaNs never win a comparison
+      const long long k = b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+      mx = k > mx ? k : mx;
+      mn = k < mn ? k : mn;
     }
-  }
+  };
+  walk_rows(base, sy, sz, x0, x1, y0, ny, z0, (int)nrows,
+            [&](const double* v) {
+              s += sum8(v);
+              q += sumsq8(v);
+#pragma unroll
+              for (int i = 0; i < 8; ++i) keys(v[i]);
+            },
+            [&](double v) {
+              s += v;
+              q = fma(v, v, q);
+              keys(v);
+            });
   Acc4 a{s, 0.0, q, 0.0, mx, mn};
   a = block_reduce4(a);
   if (threadIdx.x == 0) partials[blockIdx.x] = a;

@@ -1,0 +1,40 @@
+"""The integer-pipe exp and sin of the deep chain, compiled for the host (same source, same
+fixed-point arithmetic) and compared with long double expl / sinl: the algorithm's error bound
+is checked on the CPU, the GPU build against CUDA's functions in test_gpu_fastmath.py."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda"):
+        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
+            return os.path.join(d, "include")
+    return None
+
+
+@pytest.fixture(scope="module")
+def results(tmp_path_factory):
+    inc = _cuda_include()
+    if shutil.which("g++") is None or inc is None or np.finfo(np.longdouble).nmant < 63:
+        pytest.skip("needs g++, the CUDA headers and a long double with a 64-bit significand or more")
+    exe = str(tmp_path_factory.mktemp("fixmath") / "fixmath_host")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", inc, os.path.join(HERE, "cpp", "fixmath_host.cpp"), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe, "100000"], check=True, capture_output=True, text=True).stdout
+    return {ln.split()[0]: float(ln.split()[1]) for ln in out.splitlines() if ln.strip()}
+
+
+@pytest.mark.parametrize("name", ["exp_unit", "exp_full", "exp_tiny", "sin_unit", "sin_100", "sin_1e5", "sin_tiny",
+                                  "sin_2p20", "sin_near_jpi"])
+def test_within_one_ulp(results, name):
+    assert results[name] <= 1.0, (name, results[name])
+
+
+def test_exp_nearly_correctly_rounded(results):
+    assert max(results["exp_unit"], results["exp_full"], results["exp_tiny"]) <= 0.52
