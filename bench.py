@@ -154,7 +154,7 @@ class Deep:
         self.filt = N.Field("XVol", n, 1)
         self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
         self.cells = n ** 3
-        self.launches_per_step = 2 + 2
+        self.launches_per_step = 4  # chain, filter + reductions, ghost-shell reductions, final
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
         self.d2h_bytes = 4 * 8
         self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
@@ -163,9 +163,8 @@ class Deep:
         self._chain(self.A, self.B, self.C, self.words)
 
     def _chain(self, A, B, C, words):
-        N = self.N
-        N.deep_chain(A, B, C, words, self.out, self.filt)
-        N.reduce_all(self.filt, False, self.red)  # nebo_sum, nebo_max (and min), nebo_norm in one pass
+        # nebo_sum, nebo_max (and min), nebo_norm of filt folded into the filter kernel
+        self.N.deep_chain(A, B, C, words, self.out, self.filt, reductions=self.red)
 
     # e2e: every step uploads its inputs (a, b, c, mask words) from pinned host memory and reads
     # its reductions back.  The uploads run on a copy stream into two alternating device input

@@ -155,11 +155,20 @@ int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* 
                     const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
                     double dx, nebo_stream_t stream);
 
+/* nebo_deep_chain followed by nebo_sum, nebo_max, nebo_min and nebo_norm of filt
+ * (spatialops/NeboReductions.h:114-240; interior != 0: the _interior variants), with the
+ * reductions folded into the filter kernel as it writes filt (valid ghost cells of filt, which
+ * the filter does not write, are reduced by a small extra pass).  d_out4 (device, 4 doubles)
+ * receives {sum, max, min, norm} as nebo_reduce_all gives them; nothing is synchronised. */
+int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, const nebo_field* c,
+                           const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
+                           double dx, int interior, double* d_out4, nebo_stream_t stream);
+
 /* Element-wise FP64 exp (fn 0) or sin (fn 1) with the functions nebo_deep_chain uses: the
- * argument reduction in FP64 (three instructions), the table lookup (Tang's 2^(j/64) for exp,
- * sin/cos(k pi/64) for sin) and the polynomials in 64-bit fixed point on the integer pipe.
- * Within one ulp of the exact result for |x| < 708 (exp) and |x| < 2^20 (sin); other arguments
- * use CUDA's exp and sin. */
+ * argument reduction's one exact product in FP64, the rest in FP32, 32-bit and 64-bit fixed
+ * point (Tang's 2^(j/256) table for exp; sin/cos(k pi/256) for sin).  Within 0.52 ulp (exp,
+ * |x| < 708) and about 1.1 ulp (sin, |x| < 2^20) of the exact result; other arguments use
+ * CUDA's exp and sin. */
 int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ batched patches

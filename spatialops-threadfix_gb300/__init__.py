@@ -75,6 +75,7 @@ SIGNATURES = [
     ("nebo_heat_step", _I, [_FP, _FP, _FP, _D, ctypes.POINTER(_D), _P]),
     ("nebo_heat_run", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
     ("nebo_deep_chain", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _P]),
+    ("nebo_deep_chain_reduce", _I, [_FP, _FP, _FP, _P, _FP, _FP, _D, _I, _P, _P]),
     ("nebo_patchset_create", _I, [ctypes.POINTER(_P), _I, _P, _P, _P, _I]),
     ("nebo_patchset_destroy", _I, [_P]),
     ("nebo_patchset_info", _I, [_P, _P, _P, _P, _P]),
@@ -264,11 +265,21 @@ def heat_run(T, Ttmp, lam, steps, dt, spacing=(1.0, 1.0, 1.0), use_graph=True, s
                                int(use_graph), _stream(stream)))
 
 
-def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None):
+def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None, reductions=None, interior=False):
+    """out <<= cond(mask,0)(Interp(Grad(Interp(a)))*exp(b)+sin(c)); filt <<= BoxFilter(out).
+
+    reductions: optional float64 CUDA tensor of 4 that receives {sum, max, min, norm} of filt
+    (valid ghosts included unless interior), folded into the filter kernel."""
     da, db, dc, do, df = a.desc(), b.desc(), c.desc(), out.desc(), filt.desc()
-    _check(lib().nebo_deep_chain(ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
-                                 ctypes.c_void_p(words.data_ptr()), ctypes.byref(do), ctypes.byref(df), float(dx),
-                                 _stream(stream)))
+    if reductions is None:
+        _check(lib().nebo_deep_chain(ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                     ctypes.c_void_p(words.data_ptr()), ctypes.byref(do), ctypes.byref(df), float(dx),
+                                     _stream(stream)))
+        return
+    _check(lib().nebo_deep_chain_reduce(ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                        ctypes.c_void_p(words.data_ptr()), ctypes.byref(do), ctypes.byref(df),
+                                        float(dx), int(interior), ctypes.c_void_p(reductions.data_ptr()),
+                                        _stream(stream)))
 
 
 def kernel_launch_count():

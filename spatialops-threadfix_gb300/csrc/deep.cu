@@ -17,8 +17,11 @@
 //
 // Kernel 1 is bound by FP64 issue (exp + sin); kernel 2 sums the 27 points separably
 // (x, then y from shared memory, then z from a register queue while marching in z).
+#include <algorithm>
+
 #include "common.cuh"
 #include "fp64_int.cuh"
+#include "reduce4.cuh"
 
 namespace nebo {
 namespace {
@@ -32,7 +35,7 @@ __global__ void __launch_bounds__(256) deep_out_kernel(const double* __restrict_
                                                        int nx, int ny, int nz, double q) {
   // region: x in [1, nx), y in [-1, ny+1), z in [-1, nz+1)
   const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = -1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int y = -1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   if (x >= nx || y > ny) return;
   for (int z = -1 + (int)blockIdx.z; z <= nz; z += gridDim.z) {
     const long i = (long)x + (long)sy * y + sz * z;
@@ -48,39 +51,114 @@ __global__ void __launch_bounds__(256) deep_out_kernel(const double* __restrict_
   }
 }
 
-// filt[x,y,z] = (sum over the 27 neighbours of out) / 27 on the interior.
+__device__ __forceinline__ void cp_async8(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int FNS = 6;  // filter ring stages
+
+// filt[x,y,z] = (sum over the 27 neighbours of out) / 27 on the interior, and with RED the
+// four reductions of the values written (one Acc4 partial per block).
+// Planes of `out` (the tile plus a one-cell halo) stream through a ring of FNS shared-memory
+// stages with cp.async.  Ring schedule: plane p (-1..nz) lives in stage (p+1) % FNS; the
+// prologue issues planes z0-1 .. z0+FNS-3; iteration p waits until plane p has landed (at most
+// FNS-2 groups pending), syncs, issues plane p+FNS-1 into the stage of plane p-1 (consumed in
+// iteration p-1, before the sync), then sums plane p: x-sums of 3 into `rows`, a sync, y-sums of
+// 3 from `rows`; the 2-D sums of planes p-2, p-1, p give the output of plane p-1.
+template <bool RED>
 __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
-                                                            int sy, long sz, int nx, int ny, int nz, int zchunk) {
-  __shared__ double plane[FY + 2][FX + 2];  // one z plane of src with x/y halo
-  __shared__ double rows[FY + 2][FX];       // x-sums of 3
-  const int tx = threadIdx.x, ty = threadIdx.y;
+                                                            int sy, long sz, int nx, int ny, int nz, int zchunk,
+                                                            Acc4* __restrict__ partials) {
+  constexpr int PW = FX + 2, PH = FY + 2, PLANE = PW * PH;
+  constexpr int NCOPY = (PLANE + FX * FY - 1) / (FX * FY);
+  __shared__ __align__(16) double ring[FNS * PLANE];
+  __shared__ double rows[PH * FX];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
   const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
   const int x = x0 + tx, y = y0 + ty;
   const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, nz);
-  const int tid = ty * FX + tx;
-  double s_prev = 0.0, s_cur = 0.0;  // 2D 9-point sums of planes z-1 and z
-  for (int zz = z0 - 1; zz <= z1; ++zz) {
-    // stage plane zz rows y0-1 .. y0+FY, cols x0-1 .. x0+FX (clamped to the ghosted window)
-    for (int k = tid; k < (FY + 2) * (FX + 2); k += FX * FY) {
-      const int r = k / (FX + 2), cidx = k % (FX + 2);
-      const int gx_ = min(x0 - 1 + cidx, nx), gy_ = min(y0 - 1 + r, ny);
-      plane[r][cidx] = __ldg(src + (long)gx_ + (long)sy * gy_ + sz * zz);
+  int goff[NCOPY];  // within a plane (fewer than 2^31 cells)
+  uint32_t soff[NCOPY];
+#pragma unroll
+  for (int j = 0; j < NCOPY; ++j) {
+    const int k = min(tid + j * FX * FY, PLANE - 1);
+    const int r = k / PW, c = k - r * PW;
+    goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
+    soff[j] = (uint32_t)(k * sizeof(double));
+  }
+  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(ring);
+  auto issue = [&](int p) {
+    if (p > z1) return;
+    const uint32_t st = ring0 + (uint32_t)((p + 1) % FNS) * (PLANE * sizeof(double));
+    const double* sp = src + sz * p;
+#pragma unroll
+    for (int j = 0; j < NCOPY; ++j) {
+      if (j == NCOPY - 1 && tid + j * FX * FY >= PLANE) break;
+      cp_async8(st + soff[j], sp + goff[j]);
+    }
+  };
+#pragma unroll 1
+  for (int i = 0; i < FNS - 1; ++i) {
+    issue(z0 - 1 + i);
+    cp_async_commit();
+  }
+  const bool active = x < nx && y < ny;
+  double s_prev = 0.0, s_cur = 0.0;  // 2-D 9-point sums of planes p-2 and p-1
+  Acc4 acc = acc4_identity();
+  double* out = dst + (long)x + (long)sy * y + sz * (z0 - 1);
+#pragma unroll 1
+  for (int p = z0 - 1; p <= z1; ++p, out += sz) {
+    cp_async_wait<FNS - 2>();
+    __syncthreads();
+    issue(p + FNS - 1);
+    cp_async_commit();
+    const double* pl = ring + ((p + 1) % FNS) * PLANE;
+    for (int k = tid; k < PH * FX; k += FX * FY) {
+      const int r = k / FX, c = k % FX;
+      rows[k] = (pl[r * PW + c] + pl[r * PW + c + 1]) + pl[r * PW + c + 2];
     }
     __syncthreads();
-    for (int k = tid; k < (FY + 2) * FX; k += FX * FY) {
-      const int r = k / FX, cidx = k % FX;
-      rows[r][cidx] = (plane[r][cidx] + plane[r][cidx + 1]) + plane[r][cidx + 2];
-    }
-    __syncthreads();
-    const double s2 = (rows[ty][tx] + rows[ty + 1][tx]) + rows[ty + 2][tx];
-    if (zz >= z0 + 1 && x < nx && y < ny) {
-      // plane zz-1 is complete: s_prev (zz-2), s_cur (zz-1), s2 (zz)
-      dst[(long)x + (long)sy * y + sz * (zz - 1)] = ((s_prev + s_cur) + s2) * (1.0 / 27.0);
+    const double s2 = (rows[ty * FX + tx] + rows[(ty + 1) * FX + tx]) + rows[(ty + 2) * FX + tx];
+    if (p >= z0 + 1 && active) {
+      const double v = ((s_prev + s_cur) + s2) * (1.0 / 27.0);
+      out[-sz] = v;  // plane p-1
+      if (RED) acc4_add(acc, v);
     }
     s_prev = s_cur;
     s_cur = s2;
-    __syncthreads();
   }
+  cp_async_wait<0>();
+  if (RED) {
+    acc = block_reduce4(acc);
+    if (tid == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = acc;
+  }
+}
+
+// The four reductions over the cells of box [lo, hi) that are not in the box [ilo, ihi) (glob
+// coordinates): the valid ghost cells of `filt`, which the filter does not write but
+// nebo_sum/max/min/norm include.  A warp per (y, z) row.
+__global__ void __launch_bounds__(256) shell_reduce_kernel(const double* __restrict__ base, int gx, long gxy, int lx,
+                                                           int hx, int ly, int hy, int lz, int hz, int ix0, int ix1,
+                                                           int iy0, int iy1, int iz0, int iz1,
+                                                           Acc4* __restrict__ partials) {
+  Acc4 acc = acc4_identity();
+  const int lane = threadIdx.x & 31;
+  const int nyr = hy - ly, nrows = nyr * (hz - lz);
+  for (int r = blockIdx.x * 8 + (threadIdx.x >> 5); r < nrows; r += gridDim.x * 8) {
+    const int z = lz + r / nyr, y = ly + r % nyr;
+    const double* row = base + (long)gx * y + gxy * z;
+    if (z >= iz0 && z < iz1 && y >= iy0 && y < iy1) {
+      for (int xx = lx + lane; xx < ix0; xx += 32) acc4_add(acc, __ldg(row + xx));
+      for (int xx = ix1 + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+    } else {
+      for (int xx = lx + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+    }
+  }
+  acc = block_reduce4(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
 int check_deep(const nebo_field* a, const nebo_field* b, const nebo_field* c, const nebo_field* out,
@@ -105,16 +183,20 @@ int check_deep(const nebo_field* a, const nebo_field* b, const nebo_field* c, co
 
 using namespace nebo;
 
-extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* c,
-                               const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt, double dx,
-                               nebo_stream_t stream) {
+namespace nebo {
+void reduction_region(const nebo_field& f, int interior, int lo[3], int hi[3]);
+namespace {
+
+int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, const uint32_t* mask_words,
+              const nebo_field* out, const nebo_field* filt, double dx, bool reduce, int interior, double* d_out4,
+              cudaStream_t s, const char* what) {
   int rc = check_deep(a, b, c, out, filt);
   if (rc) return rc;
-  if (!mask_words) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_deep_chain: null mask");
-  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_deep_chain: math tables upload");
+  if (!mask_words) return fail(NEBO_ERR_INVALID, "Nebo error in %s: null mask", what);
+  if (reduce && !d_out4) return fail(NEBO_ERR_INVALID, "Nebo error in %s: null result pointer", what);
+  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in %s: math tables upload", what);
   int n[3];
   interior_extent(*a, n);
-  cudaStream_t s = (cudaStream_t)stream;
   const View<const double> va = make_view<const double>(*a), vb = make_view<const double>(*b),
                            vc = make_view<const double>(*c);
   const View<double> vo = make_view<double>(*out), vf = make_view<double>(*filt);
@@ -132,21 +214,76 @@ extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const n
     LaunchScope ls("deep_chain", s);
     deep_out_kernel<<<grid, block, 0, s>>>(va.base, vb.base, vc.base, mask_words, mask_base, vo.base, vo.sy, vo.sz,
                                            n[0], n[1], n[2], q);
-    NEBO_LAUNCH_CHECK("nebo_deep_chain (chain)");
+    NEBO_LAUNCH_CHECK(what);
+  }
+  // filter: one full wave of blocks (z chunks from the resident-block count)
+  static int per_sm[2] = {0, 0};
+  if (!per_sm[reduce]) {
+    int v = 0;
+    cudaError_t e = reduce ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<true>, FX * FY, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<false>, FX * FY, 0);
+    per_sm[reduce] = (e == cudaSuccess && v > 0) ? v : 1;
+  }
+  const int gxb = (n[0] + FX - 1) / FX, gyb = (n[1] + FY - 1) / FY;
+  int chunks = std::max(1, std::min(num_sms() * per_sm[reduce] / (gxb * gyb), (n[2] + 7) / 8));
+  const int zchunk = (n[2] + chunks - 1) / chunks;
+  chunks = (n[2] + zchunk - 1) / zchunk;
+  const int fblocks = gxb * gyb * chunks;
+  if (!reduce) {
+    LaunchScope ls("box_filter", s);
+    box_filter_kernel<false><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0],
+                                                                            n[1], n[2], zchunk, nullptr);
+    NEBO_LAUNCH_CHECK(what);
+    return NEBO_OK;
+  }
+  // reduction region (valid ghosts included unless interior) and the filter's written box
+  int lo[3], hi[3], ilo[3], ihi[3];
+  reduction_region(*filt, interior, lo, hi);
+  for (int i = 0; i < 3; ++i) {
+    ilo[i] = filt->offset[i] + filt->ghost_minus[i];
+    ihi[i] = ilo[i] + n[i];
+  }
+  const bool shell = lo[0] != ilo[0] || hi[0] != ihi[0] || lo[1] != ilo[1] || hi[1] != ihi[1] || lo[2] != ilo[2] ||
+                     hi[2] != ihi[2];
+  const int sblocks = shell ? num_sms() * 2 : 0;
+  Acc4* partials = nullptr;
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&partials, sizeof(Acc4) * (fblocks + sblocks), s));
+  {
+    LaunchScope ls("box_filter_reduce", s);
+    box_filter_kernel<true><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0],
+                                                                           n[1], n[2], zchunk, partials);
+  }
+  if (shell) {
+    LaunchScope ls("shell_reduce", s);
+    shell_reduce_kernel<<<sblocks, 256, 0, s>>>((const double*)filt->data, filt->glob[0],
+                                                (long)filt->glob[0] * filt->glob[1], lo[0], hi[0], lo[1], hi[1], lo[2],
+                                                hi[2], ilo[0], ihi[0], ilo[1], ihi[1], ilo[2], ihi[2],
+                                                partials + fblocks);
   }
   {
-    const int gxb = (n[0] + FX - 1) / FX, gyb = (n[1] + FY - 1) / FY;
-    int chunks = (num_sms() * 4 + gxb * gyb - 1) / (gxb * gyb);
-    chunks = chunks < 1 ? 1 : (chunks > (n[2] + 7) / 8 ? (n[2] + 7) / 8 : chunks);
-    if (chunks < 1) chunks = 1;
-    const int zchunk = (n[2] + chunks - 1) / chunks;
-    chunks = (n[2] + zchunk - 1) / zchunk;
-    LaunchScope ls("box_filter", s);
-    box_filter_kernel<<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2],
-                                                                      zchunk);
-    NEBO_LAUNCH_CHECK("nebo_deep_chain (filter)");
+    LaunchScope ls("reduce4_final", s);
+    reduce4_final_kernel<<<1, 256, 0, s>>>(partials, fblocks + sblocks, d_out4);
   }
+  cudaError_t le = cudaGetLastError();
+  cudaFreeAsync(partials, s);
+  if (le != cudaSuccess) return cuda_fail(le, what);
   return NEBO_OK;
+}
+
+}  // namespace
+}  // namespace nebo
+
+extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* c,
+                               const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt, double dx,
+                               nebo_stream_t stream) {
+  return deep_impl(a, b, c, mask_words, out, filt, dx, false, 0, nullptr, (cudaStream_t)stream, "nebo_deep_chain");
+}
+
+extern "C" int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, const nebo_field* c,
+                                      const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
+                                      double dx, int interior, double* d_out4, nebo_stream_t stream) {
+  return deep_impl(a, b, c, mask_words, out, filt, dx, true, interior, d_out4, (cudaStream_t)stream,
+                   "nebo_deep_chain_reduce");
 }
 
 // Element-wise FP64 exp / sin of the integer-pipe functions (fn 0: exp, 1: sin).

@@ -1,36 +1,41 @@
-// FP64 exp and sin evaluated mostly on the integer pipe.
+// FP64 exp and sin evaluated mostly outside the FP64 pipe.
 //
-// On this GPU an FP64 instruction issues at about 1/64 of the FP32 rate, while 32-bit integer
-// multiply-adds, shifts and logic issue at 64 lanes per clock per SM, so a kernel whose time goes
-// to FP64 transcendentals runs faster when the polynomial work moves to 64-bit fixed point.  Only
-// the argument reduction stays in FP64 (three instructions, for the exact Cody-Waite product).
+// On this GPU an FP64 instruction issues at about 2 per clock per SM, a signed 64-bit high
+// product at about 4, an unsigned one at about 7, and 32-bit integer multiply-adds, FP32 arithmetic
+// and f32<->f64 conversions at 60-128.  A kernel whose time goes to FP64 transcendentals therefore
+// runs faster when (1) the FP64 pipe keeps only the one exact Cody-Waite product that needs all 53
+// bits of x, (2) the polynomials run in fixed point with as few 64-bit products as the error
+// budget allows (unsigned), and (3) the low-order terms use FP32 or 32x32-bit products.
 //
-// exp(x), |x| < 708   Tang's table method (P. T. P. Tang, ACM TOMS 15(2), 1989):
-//     x = (64 m + j) ln2/64 + r,  |r| <= ln2/128 (+ rounding),
-//     exp(x) = 2^m * 2^(j/64) * (1 + p(r)),   p(r) = r + r^2/2 + ... + r^6/720 (Taylor; the first
-//     dropped term r^7/5040 < 2^-64).  k = 64 m + j from the FP64 product x * 64/ln2; the exact
-//     r1 = x - k*L1 in FP64 (L1 = ln2/64 to 29 bits, so k*L1 is exact for |k| < 2^24); then
-//     r = r1 - k*L2 in fixed point (L2 = ln2/64 - L1 to 2^-102).  p, 2^(j/64)*(1 + p) and the
-//     rounding to a double run in signed 64-bit fixed point with 62 fraction bits.
-// sin(x), |x| < 2^20  x = k pi/64 + r,  |r| <= pi/128:
-//     sin(x) = S_k cos r + C_k sin r  with S_k, C_k = sin, cos(k pi/64) (128-entry table),
-//     sin r = r (1 - u/6 + u^2/120 - u^3/5040), cos r = 1 - u/2 + u^2/24 - u^3/720 + u^4/40320,
-//     u = r^2 (Taylor; dropped terms below 2^-66 and 2^-71).  r1 = x - k*A1 exactly in FP64
-//     (A1 = pi/64 to 27 bits), r = r1 - k*A23 in fixed point (A23 = pi/64 - A1 to 2^-96).  When
-//     k is a multiple of 64 the result is +-sin r, which can be tiny: then r is formed in FP64
-//     (three more FMAs with pi/64 in four parts, 2^-173) and sin r = r * (1 - u/6 + ...) is a
-//     floating product of r's significand.
+// exp(x), |x| < 708   Tang's table method (P. T. P. Tang, ACM TOMS 15(2), 1989) with 256 entries:
+//     x = (256 m + j) ln2/256 + r,  |r| <= ln2/512 (+0.02 % from the FP32 rounding of k),
+//     exp(x) = 2^m * 2^(j/256) * (1 + p),  p = r + r^2 (1/2 + r (1/6 + r (1/24 + r/120)))
+//     (Taylor; the dropped r^6/720 < 2^-66).  k = round(x * 256/ln2) in FP32 (any k within one of
+//     the nearest works); r1 = x - k*L1 exactly in FP64 (L1 = ln2/256 to 35 bits, so k*L1 is exact
+//     for |k| < 2^18); r = r1 - k*L2 in fixed point (L2 = ln2/256 - L1 to 2^-104).  The inner
+//     factors 1/24 + r/120 (FP32) and 1/6 + r*(...), 1/2 + r*(...) (32x32-bit products) need few
+//     bits; r^2, r^2*(...) and 2^(j/256)*(1 + p) are 64-bit products; the result is rounded to a
+//     double from the 62-fraction-bit fixed point.
+// sin(x), |x| < 2^20  x = k pi/256 + r,  |r| <= pi/512 (+1 % from the FP32 rounding of k):
+//     sin(x) = S_k (1 + (cos r - 1)) + C_k sin r,  S_k, C_k = sin, cos(k pi/256) from a 128-entry
+//     quarter table and the quadrant of k;  sin r = r (1 - u/6 + u^2/120),
+//     cos r - 1 = -u/2 + u^2/24 - u^3/720,  u = r^2 (Taylor; dropped terms below 2^-70).
+//     k in FP32 for |x| < 4096, else in FP64 (two more instructions); r1 = x - k*A1 exactly in
+//     FP64 (A1 = pi/256 to 26 bits, exact for |k| < 2^26.3); r = r1 - k*A23 in fixed point
+//     (A23 = pi/256 - A1 to 2^-94).  When k is a multiple of 256 (x near j*pi) the result is
+//     +-sin r and may be tiny: r is then formed in FP64 from pi/256 in four parts (error 2^-170)
+//     and sin r = r * (1 - u/6 + u^2/120) is a product of r's significand.
 // Everything else -- |x| beyond those ranges, NaN, infinities -- goes to CUDA's exp and sin.
 //
-// Fixed-point products keep the high bits: mulq(a, b) = floor(a*b / 2^62) up to 3 units of
-// 2^-62 (the high word shifted; used inside the polynomials, whose errors are scaled down by r),
-// mulx(a, b) = floor(a*b / 2^62) exactly (high and low words; used where the error would reach the
-// result).  The error bound of both functions stays below one ulp; the tests compare them with
-// CUDA's exp and sin (at most 2 ulp apart) on random and edge inputs.
+// Fixed point: signed or unsigned 64-bit integers with 62 fraction bits ("at 2^62").  Error: exp
+// within 0.52 ulp, sin within about 1.1 ulp (the FP64 rounding of r before the final rounding in
+// the multiple-of-pi branch; fixed-point roundings where |sin x| is near sin(pi/512), whose ulp is
+// 4 units of 2^-62); the tests compare both with long double on the host and with CUDA's
+// functions on the device.
 //
-// The tables (2^(j/64), sin and cos of k pi/64 in fixed point) are computed on the host in long
-// double and uploaded once per device; the functions are __host__ __device__ so the host can run
-// the same integer arithmetic.
+// The tables (2^(j/256); sin and cos of j pi/256, j < 128) are computed on the host in long
+// double and uploaded once per device.  Every function is __host__ __device__, so the host runs
+// the same integer arithmetic in the CPU tests.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -44,39 +49,40 @@ namespace nebo {
 namespace fixmath {
 
 struct Tables {
-  int64_t exp2j[64];   // round(2^(j/64) * 2^62)
-  int64_t sink[128];   // round(sin(k pi/64) * 2^62)
-  int64_t cosk[128];   // round(cos(k pi/64) * 2^62)
+  int64_t exp2j[256];  // round(2^(j/256) * 2^62)
+  int64_t sinj[128];   // round(sin(j pi/256) * 2^62)
+  int64_t cosj[128];   // round(cos(j pi/256) * 2^62)
 };
 
 constexpr int64_t ONE = (int64_t)1 << 62;
-// ln2/64 - L1 at 2^-102 and pi/64 - A1 at 2^-96 (computed with 300-bit arithmetic)
-constexpr int64_t L2_FIX102 = -3328307820869995624LL;
-constexpr int64_t A23_FIX96 = 2456304730009003561LL;
+constexpr int64_t HALF = (int64_t)1 << 61;
+constexpr int64_t SIXTH = 768614336404564651LL;                 // 2^62 / 6
+constexpr uint64_t SIXTH64 = 0x2AAAAAAAAAAAAAABULL;            // 2^64 / 6, rounded up
+constexpr uint32_t C24 = 178956971u;                            // 2^32 / 24
+constexpr uint32_t C120 = 35791394u;                            // 2^32 / 120
+constexpr uint32_t C720 = 5965232u;                             // 2^32 / 720
+// ln2/256 = L1 + L2: L1 to 35 significant bits, L2 at 2^-104.  pi/256 = A1 + A23: A1 to 26
+// bits, A23 at 2^-94; A23 = A2 + A3 + A4 as doubles (A2 to 26 bits).  (300-bit arithmetic.)
+constexpr double L1 = 0.0027076061741126978;
+constexpr int64_t L2_FIX104 = -1022464811656301672LL;
+constexpr double A1 = 0.01227184641174972;
+constexpr int64_t A23_FIX94 = -2152323963588131229LL;
+constexpr double A2 = -1.0866459121405825e-10, A3 = 4.783776559169348e-19, A4 = -1.1698319569212264e-35;
 
 inline void fill_tables(Tables* t) {
-  for (int j = 0; j < 64; ++j) t->exp2j[j] = (int64_t)llroundl(exp2l((long double)j / 64.0L) * 4611686018427387904.0L);
+  const long double s62 = 4611686018427387904.0L;
+  for (int j = 0; j < 256; ++j) t->exp2j[j] = (int64_t)llroundl(exp2l((long double)j / 256.0L) * s62);
   const long double pi = 3.141592653589793238462643383279502884L;
-  for (int k = 0; k < 128; ++k) {
-    t->sink[k] = (int64_t)llroundl(sinl((long double)k * pi / 64.0L) * 4611686018427387904.0L);
-    t->cosk[k] = (int64_t)llroundl(cosl((long double)k * pi / 64.0L) * 4611686018427387904.0L);
+  for (int j = 0; j < 128; ++j) {
+    t->sinj[j] = (int64_t)llroundl(sinl((long double)j * pi / 256.0L) * s62);
+    t->cosj[j] = (int64_t)llroundl(cosl((long double)j * pi / 256.0L) * s62);
   }
-  // exact values at multiples of pi/2
-  const int64_t qs[4] = {0, ONE, 0, -ONE}, qc[4] = {ONE, 0, -ONE, 0};
-  for (int i = 0; i < 4; ++i) {
-    t->sink[32 * i] = qs[i];
-    t->cosk[32 * i] = qc[i];
-  }
+  t->sinj[0] = 0;
+  t->cosj[0] = ONE;
 }
 
-__host__ __device__ __forceinline__ int64_t hi_s(int64_t a, int64_t b) {
-#ifdef __CUDA_ARCH__
-  return __mul64hi(a, b);
-#else
-  return (int64_t)(((__int128)a * (__int128)b) >> 64);
-#endif
-}
-__host__ __device__ __forceinline__ uint64_t hi_u(uint64_t a, uint64_t b) {
+// ------------------------------------------------------------------ integer helpers
+__host__ __device__ __forceinline__ uint64_t umulhi(uint64_t a, uint64_t b) {
 #ifdef __CUDA_ARCH__
   return __umul64hi(a, b);
 #else
@@ -108,47 +114,69 @@ __host__ __device__ __forceinline__ double from_bits(uint64_t b) {
   return x;
 #endif
 }
+__host__ __device__ __forceinline__ int fbits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_int(x);
+#else
+  int b;
+  std::memcpy(&b, &x, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ uint64_t uabs(int64_t a) { return a < 0 ? 0 - (uint64_t)a : (uint64_t)a; }
 
-// a*b / 2^62, high word only (error < 4 units of 2^-62)
-__host__ __device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) { return hi_s(a, b) * 4; }
-// floor(a*b / 2^62)
-__host__ __device__ __forceinline__ int64_t mulx(int64_t a, int64_t b) {
-  return (int64_t)(((uint64_t)hi_s(a, b) << 2) | (((uint64_t)a * (uint64_t)b) >> 62));
+// a * b / 2^62 for a, b >= 0: high word only (truncation below 4 units of 2^-62), and rounded to
+// nearest (the full 128-bit product plus one half, a < 2^64, a * b < 2^126).
+__host__ __device__ __forceinline__ uint64_t umulq(uint64_t a, uint64_t b) { return umulhi(a, b) << 2; }
+__host__ __device__ __forceinline__ uint64_t umulx(uint64_t a, uint64_t b) {
+  const uint64_t lo = a * b, lo2 = lo + (1ULL << 61);
+  return ((umulhi(a, b) + (lo2 < lo)) << 2) | (lo2 >> 62);
+}
+// signed a * b / 2^62 (magnitudes rounded, then the sign)
+__host__ __device__ __forceinline__ int64_t smulx(int64_t a, int64_t b) {
+  const uint64_t m = umulx(uabs(a), uabs(b));
+  return ((a ^ b) < 0) ? -(int64_t)m : (int64_t)m;
 }
 
-// A finite double with |v| < 2 as fixed point with 62 fraction bits (truncated toward zero).
+// A finite double with |v| < 2 at 2^62 (truncated toward zero; 0 for subnormals).
 __host__ __device__ __forceinline__ int64_t to_fix(double v) {
   const uint64_t b = bits(v);
   const int e = (int)((b >> 52) & 0x7ff);
   const uint64_t m = (b & 0xfffffffffffffULL) | 0x10000000000000ULL;
-  const int sh = e - 1013;  // v = m * 2^(e - 1075), fixed = v * 2^62
-  uint64_t f;
-  if (sh >= 0)
-    f = m << sh;
-  else
-    f = sh > -64 ? m >> -sh : 0;
+  const int sh = e - 1013;  // v = m * 2^(e - 1075)
+  uint64_t f = sh >= 0 ? m << sh : (sh > -64 ? m >> -sh : 0);
   if (e == 0) f = 0;
   return (b >> 63) ? -(int64_t)f : (int64_t)f;
 }
 
-// k * C / 2^s for a signed 32-bit k and a positive 62-bit constant C, 32 <= s < 64 (floor).
+// k * C / 2^S for a signed 32-bit k and a 62-bit signed constant C, 32 <= S < 64, rounded
+// (|k * (C mod 2^32)| < 2^62).
 template <int S>
 __host__ __device__ __forceinline__ int64_t mul_k(int k, int64_t c) {
-  const int64_t hi = (int64_t)k * (c >> 32);                     // |.| < 2^(31+30)
-  const int64_t lo = (int64_t)k * (int64_t)(uint32_t)c;          // |.| < 2^63
-  return (hi + (lo >> 32)) >> (S - 32);
+  const int64_t hi = (int64_t)k * (c >> 32);
+  const int64_t lo = (int64_t)k * (int64_t)(uint32_t)c;
+  const int64_t v = hi + ((lo + (1LL << 31)) >> 32);
+  if (S == 32) return v;
+  return (v + (1LL << (S - 33 > 0 ? S - 33 : 0))) >> (S - 32);
 }
 
-// Positive fixed-point y (62 fraction bits, y < 2^63) times 2^e as a double, rounded to nearest.
-// The result must be a normal number.
+// Bits of the double y * 2^(e - 62) for 0 < y < 2^64, rounded to nearest (normal results only).
 __host__ __device__ __forceinline__ uint64_t fix_to_bits(uint64_t y, int e) {
   const int lz = clz64(y);
-  const uint64_t yn = y << lz;                     // top bit at 63
-  const uint64_t m = (yn >> 11) + ((yn >> 10) & 1);  // rounded 53-bit significand (2^53 on carry)
-  // value = (yn / 2^63) * 2^(1 - lz + e); the implicit bit of m adds one to the exponent field
+  const uint64_t yn = y << lz;                       // top bit at 63
+  const uint64_t m = (yn >> 11) + ((yn >> 10) & 1);  // 53-bit significand, 2^53 on carry-out
+  // value = (yn / 2^63) * 2^(1 - lz + e); m's implicit bit adds one to the exponent field
   return ((uint64_t)(e + 1 - lz + 1022) << 52) + m;
 }
 
+// k = round(x * c) (within one) through FP32, |x * c| < 2^22; kd = k as a double.
+__host__ __device__ __forceinline__ int k_f32(double x, float c, double* kd) {
+  const float t = fmaf((float)x, c, 12582912.0f);  // 1.5 * 2^23
+  *kd = (double)(t - 12582912.0f);
+  return fbits(t) - 0x4B400000;
+}
+
+// ------------------------------------------------------------------ exp
 template <class T>
 __host__ __device__ __forceinline__ double exp_fix(double x, const T& tb) {
   const uint64_t xb = bits(x);
@@ -159,82 +187,115 @@ __host__ __device__ __forceinline__ double exp_fix(double x, const T& tb) {
     return std::exp(x);
 #endif
   }
-  const double shifter = 6755399441055744.0;  // 1.5 * 2^52
-  const double t = fma(x, 92.33248261689366, shifter);  // x * 64/ln2 rounded to an integer
-  const int k = (int)(uint32_t)bits(t);
-  const double kd = t - shifter;
-  const double r1 = fma(-kd, 0.010830424696905538, x);  // exact: L1 has 29 significant bits
-  const int64_t r = to_fix(r1) - mul_k<40>(k, L2_FIX102);
-  // p = r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r/720))))
-  int64_t h = 6405119470038039LL;                  // 1/720
-  h = 38430716820228233LL + mulq(r, h);           // 1/120
-  h = 192153584101141163LL + mulq(r, h);          // 1/24
-  h = 768614336404564651LL + mulq(r, h);          // 1/6
-  h = 2305843009213693952LL + mulq(r, h);         // 1/2
-  const int64_t p = r + mulq(mulq(r, r), h);
-  const int64_t tj = tb.exp2j[k & 63];
-  const uint64_t y = (uint64_t)(tj + mulx(tj, p));
-  return from_bits(fix_to_bits(y, k >> 6));
+  double kd;
+  const int k = k_f32(x, 369.32992553710938f, &kd);  // 256/ln2
+  const double r1 = fma(-kd, L1, x);                  // exact
+  const int64_t r = to_fix(r1) - mul_k<42>(k, L2_FIX104);
+  // g2 = 1/24 + r/120 in FP32, in [2^-5, 2^-4): its significand at 2^35 is exact
+  const float g2 = fmaf((float)r1, 1.0f / 120.0f, 1.0f / 24.0f);
+  const int32_t g2f = (int32_t)(((uint32_t)fbits(g2) & 0x7fffffu) | 0x800000u) << 7;
+  const int32_t r40 = (int32_t)(r >> 22);  // r at 2^40
+  const int64_t g = SIXTH + (((int64_t)r40 * g2f) >> 13);               // 1/6 + r g2
+  const int64_t h = HALF + (((int64_t)r40 * (int32_t)(g >> 30)) >> 10);  // 1/2 + r g
+  const uint64_t u = umulq(uabs(r), uabs(r));                           // r^2
+  const int64_t p = r + (int64_t)umulq(u, (uint64_t)h);
+  const uint64_t tj = (uint64_t)tb.e(k & 255);
+  const uint64_t tp = umulx(tj, uabs(p));
+  const uint64_t y = p < 0 ? tj - tp : tj + tp;
+  return from_bits(fix_to_bits(y, k >> 8));
+}
+
+// ------------------------------------------------------------------ sin
+// -u/6 + u^2/120 and cos r - 1 = -u/2 + u^2/24 - u^3/720 at 2^62, from u = r^2 at 2^62 (u < 2^-14)
+__host__ __device__ __forceinline__ void sin_cos_poly(uint64_t u, int64_t* sfac_m1, int64_t* cm1) {
+  const uint32_t u46 = (uint32_t)(u >> 16);                          // u at 2^46
+  const uint32_t uu60 = (uint32_t)(((uint64_t)u46 * u46) >> 32);      // u^2 at 2^60
+  const int64_t u2_120 = (int64_t)(((uint64_t)uu60 * C120) >> 30);    // u^2/120 at 2^62
+  const int64_t u2_24 = (int64_t)(((uint64_t)uu60 * C24) >> 30);      // u^2/24
+  const uint64_t u3 = ((uint64_t)uu60 * u46) >> 44;                   // u^3 at 2^62
+  const int64_t u3_720 = (int64_t)((u3 * C720) >> 32);               // u^3/720
+  *sfac_m1 = -(int64_t)umulhi(u, SIXTH64) + u2_120;
+  *cm1 = -(int64_t)(u >> 1) + u2_24 - u3_720;
 }
 
 template <class T>
 __host__ __device__ __forceinline__ double sin_fix(double x, const T& tb) {
   const uint64_t xb = bits(x);
-  if ((uint32_t)(xb >> 32 & 0x7fffffffu) >= 0x41300000u) {  // |x| >= 2^20, inf, NaN
+  const uint32_t hx = (uint32_t)(xb >> 32 & 0x7fffffffu);
+  if (hx >= 0x41300000u) {  // |x| >= 2^20, inf, NaN
 #ifdef __CUDA_ARCH__
     return sin(x);
 #else
     return std::sin(x);
 #endif
   }
-  const double shifter = 6755399441055744.0;
-  const double t = fma(x, 20.371832715762604, shifter);  // x * 64/pi rounded to an integer
-  const int k = (int)(uint32_t)bits(t);
-  const double kd = t - shifter;
-  const double r1 = fma(-kd, 0.049087385181337595, x);  // exact: A1 has 27 significant bits
-  const int q = k & 127;
-  if ((k & 63) == 0) {
-    // +-sin r with r possibly tiny: r in FP64, then r * S(u) as a product of significands
-    double rd = fma(-kd, 3.100292418622974e-11, r1);
-    rd = fma(-kd, 1.7878714769093224e-19, rd);
-    rd = fma(-kd, 1.3549703328318407e-36, rd);  // pi/64 in four parts: x near j*pi keeps its digits
-    const uint64_t rb = bits(rd) ^ ((uint64_t)(q >> 6) << 63);  // sin(r + pi) = -sin r
+  int k;
+  double kd;
+  if (hx < 0x40B00000u) {  // |x| < 4096
+    k = k_f32(x, 81.4873275756836f, &kd);  // 256/pi
+  } else {
+    const double t = fma(x, 81.48733086305042, 6755399441055744.0);
+    k = (int)(uint32_t)bits(t);
+    kd = t - 6755399441055744.0;
+  }
+  const double r1 = fma(-kd, A1, x);  // exact
+  const int q = (k >> 7) & 3;
+  if ((k & 255) == 0) {
+    // +-sin r, r possibly tiny: r in FP64 with pi/256 in four parts, then r * (1 - u/6 + u^2/120)
+    double rd = r1;  // k = 0: r = x exactly (keeps the sign of -0)
+    if (k != 0) {
+      rd = fma(-kd, A2, rd);
+      rd = fma(-kd, A3, rd);
+      rd = fma(-kd, A4, rd);
+    }
+    const uint64_t rb = bits(rd) ^ ((uint64_t)(q >> 1) << 63);  // sin(r + pi) = -sin r
     const int er = (int)((rb >> 52) & 0x7ff);
     if (er < 1023 - 26) return from_bits(rb);                   // |r| < 2^-26: sin r = r
-    const int64_t rf = to_fix(rd);
-    const int64_t u = mulq(rf, rf);
-    int64_t s = -915017067148291LL;                 // -1/5040
-    s = 38430716820228233LL + mulq(u, s);           // 1/120
-    s = -768614336404564651LL + mulq(u, s);         // -1/6
-    s = ONE + mulq(u, s);
+    const uint64_t ra = uabs(to_fix(rd));
+    int64_t sm1, cm1;
+    sin_cos_poly(umulq(ra, ra), &sm1, &cm1);
+    const uint64_t s = (uint64_t)(ONE + sm1);                   // 1 - u/6 + u^2/120 <= 2^62
     const uint64_t mr = ((rb & 0xfffffffffffffULL) | 0x10000000000000ULL) << 11;  // top bit 63
-    const uint64_t pr = hi_u(mr, (uint64_t)s << 1);  // |r| significand * S, top bit 62 or 63
+    const uint64_t pr = umulhi(mr, s << 1);                    // top bit at 61..63
     const int lz = clz64(pr);
     const uint64_t pn = pr << lz;
     const uint64_t m = (pn >> 11) + ((pn >> 10) & 1);
     // sin r = (pn / 2^63) * 2^(er - 1022 - lz); m's implicit bit adds one to the exponent field
     return from_bits((rb & 0x8000000000000000ULL) | (((uint64_t)(er - lz) << 52) + m));
   }
-  const int64_t r = to_fix(r1) - mul_k<34>(k, A23_FIX96);
-  const int64_t u = mulq(r, r);
-  int64_t s = -915017067148291LL;                   // -1/5040
-  s = 38430716820228233LL + mulq(u, s);             // 1/120
-  s = -768614336404564651LL + mulq(u, s);           // -1/6
-  const int64_t sr = r + mulx(r, mulq(u, s));       // sin r
-  int64_t c = 114377133393536LL;                    // 1/40320
-  c = -6405119470038039LL + mulq(u, c);             // -1/720
-  c = 192153584101141163LL + mulq(u, c);            // 1/24
-  c = -2305843009213693952LL + mulq(u, c);          // -1/2
-  const int64_t cm = mulx(u, c);                    // cos r - 1
-  const int64_t sk = tb.sink[q], ck = tb.cosk[q];
-  const int64_t v = sk + mulx(sk, cm) + mulx(ck, sr);
+  const int64_t r = to_fix(r1) - mul_k<32>(k, A23_FIX94);
+  const uint64_t ra = uabs(r);
+  int64_t sm1, cm1;
+  sin_cos_poly(umulq(ra, ra), &sm1, &cm1);
+  const int64_t sr = r + smulx(r, sm1);  // sin r
+  const int j = k & 127;
+  const int64_t sj = tb.s(j), cj = tb.c(j);
+  int64_t sk = (q & 1) ? cj : sj, ck = (q & 1) ? sj : cj;
+  if (q & 2) sk = -sk;
+  if ((q ^ (q >> 1)) & 1) ck = -ck;
+  const int64_t v = sk + smulx(sk, cm1) + smulx(ck, sr);
   const uint64_t sign = (uint64_t)v & 0x8000000000000000ULL;
-  return from_bits(sign | fix_to_bits((uint64_t)(v < 0 ? -v : v), 0));
+  return from_bits(sign | fix_to_bits(uabs(v), 0));
 }
 
+// Host view of the tables.
+struct HostTables {
+  const Tables* t;
+  int64_t e(int j) const { return t->exp2j[j]; }
+  int64_t s(int j) const { return t->sinj[j]; }
+  int64_t c(int j) const { return t->cosj[j]; }
+};
+
 #ifdef __CUDACC__
-// Device copy of the tables (one per device, uploaded by tables_init).
+// Device copy of the tables (one per device, uploaded by tables_init), read through the
+// read-only data cache.
 static __device__ Tables g_fix_tables;
+
+struct DeviceTables {
+  __device__ __forceinline__ int64_t e(int j) const { return __ldg(&g_fix_tables.exp2j[j]); }
+  __device__ __forceinline__ int64_t s(int j) const { return __ldg(&g_fix_tables.sinj[j]); }
+  __device__ __forceinline__ int64_t c(int j) const { return __ldg(&g_fix_tables.cosj[j]); }
+};
 
 inline int tables_init() {
   static std::mutex mu;
@@ -250,8 +311,8 @@ inline int tables_init() {
   return 0;
 }
 
-__device__ __forceinline__ double exp_i(double x) { return exp_fix(x, g_fix_tables); }
-__device__ __forceinline__ double sin_i(double x) { return sin_fix(x, g_fix_tables); }
+__device__ __forceinline__ double exp_i(double x) { return exp_fix(x, DeviceTables()); }
+__device__ __forceinline__ double sin_i(double x) { return sin_fix(x, DeviceTables()); }
 #endif
 
 }  // namespace fixmath

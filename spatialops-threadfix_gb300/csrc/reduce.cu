@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "reduce4.cuh"
 
 namespace nebo {
 namespace {
@@ -336,57 +337,6 @@ extern "C" int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, do
 namespace nebo {
 namespace {
 
-struct Acc4 {
-  double s, sc, q, qc;  // sum and compensation, sum of squares and compensation
-  long long mx, mn;     // order-preserving keys of max and min
-};
-
-__device__ __forceinline__ double from_key(long long k) {
-  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
-}
-__device__ __forceinline__ void comp_add(double& s, double& c, double v) {
-  const double t = s + v;
-  c += (fabs(s) >= fabs(v)) ? ((s - t) + v) : ((v - t) + s);
-  s = t;
-}
-__device__ __forceinline__ void merge4(Acc4& a, const Acc4& b) {
-  comp_add(a.s, a.sc, b.s);
-  a.sc += b.sc;
-  comp_add(a.q, a.qc, b.q);
-  a.qc += b.qc;
-  a.mx = a.mx > b.mx ? a.mx : b.mx;
-  a.mn = a.mn < b.mn ? a.mn : b.mn;
-}
-__device__ __forceinline__ Acc4 shfl_down4(const Acc4& a, int o) {
-  Acc4 b;
-  b.s = __shfl_down_sync(0xffffffffu, a.s, o);
-  b.sc = __shfl_down_sync(0xffffffffu, a.sc, o);
-  b.q = __shfl_down_sync(0xffffffffu, a.q, o);
-  b.qc = __shfl_down_sync(0xffffffffu, a.qc, o);
-  b.mx = __shfl_down_sync(0xffffffffu, a.mx, o);
-  b.mn = __shfl_down_sync(0xffffffffu, a.mn, o);
-  return b;
-}
-__device__ Acc4 block_reduce4(Acc4 a) {
-  __shared__ Acc4 sh[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) merge4(a, shfl_down4(a, o));
-  if (lane == 0) sh[wid] = a;
-  __syncthreads();
-  const int nw = (blockDim.x + 31) >> 5;
-  if (wid == 0) {
-    if (lane < nw) {
-      a = sh[lane];
-    } else {
-      a.s = a.sc = a.q = a.qc = 0.0;
-      a.mx = LLONG_MIN;
-      a.mn = LLONG_MAX;
-    }
-    for (int o = 16; o > 0; o >>= 1) merge4(a, shfl_down4(a, o));
-  }
-  return a;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) reduce4_rows_kernel(const T* __restrict__ base, int sy, long sz, int x0,
                                                                    int x1, int y0, int ny, int z0, long nrows,
@@ -418,18 +368,6 @@ __global__ void __launch_bounds__(RED_THREADS) reduce4_rows_kernel(const T* __re
   if (threadIdx.x == 0) partials[blockIdx.x] = a;
 }
 
-__global__ void __launch_bounds__(RED_THREADS) reduce4_final_kernel(const Acc4* __restrict__ partials, int n,
-                                                                    double* __restrict__ out) {
-  Acc4 a{0.0, 0.0, 0.0, 0.0, LLONG_MIN, LLONG_MAX};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) merge4(a, partials[i]);
-  a = block_reduce4(a);
-  if (threadIdx.x == 0) {
-    out[0] = a.s + a.sc;
-    out[1] = a.mx == LLONG_MIN ? -INFINITY : from_key(a.mx);
-    out[2] = a.mn == LLONG_MAX ? INFINITY : from_key(a.mn);
-    out[3] = sqrt(a.q + a.qc);
-  }
-}
 
 }  // namespace
 }  // namespace nebo
