@@ -15,8 +15,9 @@
 // chain's x ghost is -1, so `out` is written on x in [1, n) and y, z in [-1, n+1); the filter's
 // region is the interior.  Other cells keep their contents.
 //
-// Kernel 1 is bound by FP64 issue (exp + sin); kernel 2 sums the 27 points separably
-// (x, then y from shared memory, then z from a register queue while marching in z).
+// Kernel 1 evaluates exp and sin mostly on the integer pipe (fp64_int.cuh); kernel 2 sums the 27
+// points separably (x, then y from shared memory, then z from registers while marching in z),
+// optionally folding the four reductions of filt into the same pass.
 #include <algorithm>
 
 #include "common.cuh"
@@ -58,27 +59,31 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-constexpr int FNS = 6;  // filter ring stages
+constexpr int FNS = 6;   // filter ring stages
+constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns two y-adjacent cells)
 
 // filt[x,y,z] = (sum over the 27 neighbours of out) / 27 on the interior, and with RED the
 // four reductions of the values written (one Acc4 partial per block).
-// Planes of `out` (the tile plus a one-cell halo) stream through a ring of FNS shared-memory
-// stages with cp.async.  Ring schedule: plane p (-1..nz) lives in stage (p+1) % FNS; the
-// prologue issues planes z0-1 .. z0+FNS-3; iteration p waits until plane p has landed (at most
-// FNS-2 groups pending), syncs, issues plane p+FNS-1 into the stage of plane p-1 (consumed in
-// iteration p-1, before the sync), then sums plane p: x-sums of 3 into `rows`, a sync, y-sums of
-// 3 from `rows`; the 2-D sums of planes p-2, p-1, p give the output of plane p-1.
+// Planes of `out` (the 32 x 16 tile plus a one-cell halo) stream through a ring of FNS
+// shared-memory stages with cp.async.  Ring schedule: plane p (-1..nz) lives in stage
+// (p+1) % FNS; the prologue issues planes z0-1 .. z0+FNS-3; iteration p waits until plane p has
+// landed (at most FNS-2 groups pending), syncs, issues plane p+FNS-1 into the stage of plane p-1
+// (consumed in iteration p-1, before the sync), then sums plane p: x-sums of 3 into `rows`
+// (two neighbouring sums share their middle pair: 3 adds for 2 sums), a sync, y-sums of 3 for
+// the thread's two cells (again sharing the middle pair); the 2-D sums of planes p-2, p-1, p
+// give the outputs of plane p-1.  FP64 adds are the bound, hence the shared pairs.
 template <bool RED>
 __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
                                                             int sy, long sz, int nx, int ny, int nz, int zchunk,
                                                             Acc4* __restrict__ partials) {
-  constexpr int PW = FX + 2, PH = FY + 2, PLANE = PW * PH;
+  constexpr int PW = FX + 2, PH = FTY + 2, PLANE = PW * PH;
   constexpr int NCOPY = (PLANE + FX * FY - 1) / (FX * FY);
+  constexpr int XTASKS = PH * (FX / 2);  // x-sum pairs per plane
   __shared__ __align__(16) double ring[FNS * PLANE];
   __shared__ double rows[PH * FX];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
-  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
-  const int x = x0 + tx, y = y0 + ty;
+  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FTY;
+  const int x = x0 + tx, ya = y0 + 2 * ty;
   const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, nz);
   int goff[NCOPY];  // within a plane (fewer than 2^31 cells)
   uint32_t soff[NCOPY];
@@ -105,10 +110,10 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
     issue(z0 - 1 + i);
     cp_async_commit();
   }
-  const bool active = x < nx && y < ny;
-  double s_prev = 0.0, s_cur = 0.0;  // 2-D 9-point sums of planes p-2 and p-1
+  const bool act0 = x < nx && ya < ny, act1 = x < nx && ya + 1 < ny;
+  double p0 = 0.0, c0 = 0.0, p1 = 0.0, c1 = 0.0;  // 2-D sums of planes p-2 and p-1, both cells
   Acc4 acc = acc4_identity();
-  double* out = dst + (long)x + (long)sy * y + sz * (z0 - 1);
+  double* out = dst + (long)x + (long)sy * ya + sz * (z0 - 1);
 #pragma unroll 1
   for (int p = z0 - 1; p <= z1; ++p, out += sz) {
     cp_async_wait<FNS - 2>();
@@ -116,19 +121,33 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
     issue(p + FNS - 1);
     cp_async_commit();
     const double* pl = ring + ((p + 1) % FNS) * PLANE;
-    for (int k = tid; k < PH * FX; k += FX * FY) {
-      const int r = k / FX, c = k % FX;
-      rows[k] = (pl[r * PW + c] + pl[r * PW + c + 1]) + pl[r * PW + c + 2];
+    for (int t = tid; t < XTASKS; t += FX * FY) {
+      const int r = t / (FX / 2), c = 2 * (t % (FX / 2));
+      const double* q = pl + r * PW + c;
+      const double mid = q[1] + q[2];
+      rows[r * FX + c] = q[0] + mid;
+      rows[r * FX + c + 1] = mid + q[3];
     }
     __syncthreads();
-    const double s2 = (rows[ty * FX + tx] + rows[(ty + 1) * FX + tx]) + rows[(ty + 2) * FX + tx];
-    if (p >= z0 + 1 && active) {
-      const double v = ((s_prev + s_cur) + s2) * (1.0 / 27.0);
-      out[-sz] = v;  // plane p-1
-      if (RED) acc4_add(acc, v);
+    const double* col = rows + 2 * ty * FX + tx;
+    const double mid = col[FX] + col[2 * FX];
+    const double s0 = col[0] + mid, s1 = mid + col[3 * FX];
+    if (p >= z0 + 1) {
+      if (act0) {
+        const double v = ((p0 + c0) + s0) * (1.0 / 27.0);
+        out[-sz] = v;  // plane p-1
+        if (RED) acc4_add(acc, v);
+      }
+      if (act1) {
+        const double v = ((p1 + c1) + s1) * (1.0 / 27.0);
+        out[sy - sz] = v;
+        if (RED) acc4_add(acc, v);
+      }
     }
-    s_prev = s_cur;
-    s_cur = s2;
+    p0 = c0;
+    c0 = s0;
+    p1 = c1;
+    c1 = s1;
   }
   cp_async_wait<0>();
   if (RED) {
@@ -139,23 +158,41 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
 
 // The four reductions over the cells of box [lo, hi) that are not in the box [ilo, ihi) (glob
 // coordinates): the valid ghost cells of `filt`, which the filter does not write but
-// nebo_sum/max/min/norm include.  A warp per (y, z) row.
+// nebo_sum/max/min/norm include.  Two parts: the rows entirely outside the inner box (planes
+// z outside it, and rows y outside it within the inner z range), a warp per row; and the x ends
+// of the rows that cross the inner box, a thread per cell.
 __global__ void __launch_bounds__(256) shell_reduce_kernel(const double* __restrict__ base, int gx, long gxy, int lx,
                                                            int hx, int ly, int hy, int lz, int hz, int ix0, int ix1,
                                                            int iy0, int iy1, int iz0, int iz1,
                                                            Acc4* __restrict__ partials) {
   Acc4 acc = acc4_identity();
   const int lane = threadIdx.x & 31;
-  const int nyr = hy - ly, nrows = nyr * (hz - lz);
-  for (int r = blockIdx.x * 8 + (threadIdx.x >> 5); r < nrows; r += gridDim.x * 8) {
-    const int z = lz + r / nyr, y = ly + r % nyr;
-    const double* row = base + (long)gx * y + gxy * z;
-    if (z >= iz0 && z < iz1 && y >= iy0 && y < iy1) {
-      for (int xx = lx + lane; xx < ix0; xx += 32) acc4_add(acc, __ldg(row + xx));
-      for (int xx = ix1 + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+  const int nyr = hy - ly;
+  const int zout = (iz0 - lz) + (hz - iz1);                   // planes outside the inner z range
+  const int yout = (iy0 - ly) + (hy - iy1);                   // rows per inner plane outside in y
+  const int nfull = zout * nyr + (iz1 - iz0) * yout;
+  for (int r = blockIdx.x * 8 + (threadIdx.x >> 5); r < nfull; r += gridDim.x * 8) {
+    int y, z;
+    if (r < zout * nyr) {
+      const int pz = r / nyr;
+      z = pz < iz0 - lz ? lz + pz : iz1 + (pz - (iz0 - lz));
+      y = ly + r % nyr;
     } else {
-      for (int xx = lx + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+      const int t = r - zout * nyr, py = t % yout;
+      z = iz0 + t / yout;
+      y = py < iy0 - ly ? ly + py : iy1 + (py - (iy0 - ly));
     }
+    const double* row = base + (long)gx * y + gxy * z;
+    for (int xx = lx + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+  }
+  const int xout = (ix0 - lx) + (hx - ix1);
+  const long nedge = (long)(iz1 - iz0) * (iy1 - iy0) * xout;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < nedge; e += gridDim.x * 256L) {
+    const int px = (int)(e % xout);
+    const long rr = e / xout;
+    const int y = iy0 + (int)(rr % (iy1 - iy0)), z = iz0 + (int)(rr / (iy1 - iy0));
+    const int xx = px < ix0 - lx ? lx + px : ix1 + (px - (ix0 - lx));
+    acc4_add(acc, __ldg(base + xx + (long)gx * y + gxy * z));
   }
   acc = block_reduce4(acc);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
@@ -224,7 +261,7 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<false>, FX * FY, 0);
     per_sm[reduce] = (e == cudaSuccess && v > 0) ? v : 1;
   }
-  const int gxb = (n[0] + FX - 1) / FX, gyb = (n[1] + FY - 1) / FY;
+  const int gxb = (n[0] + FX - 1) / FX, gyb = (n[1] + FTY - 1) / FTY;
   int chunks = std::max(1, std::min(num_sms() * per_sm[reduce] / (gxb * gyb), (n[2] + 7) / 8));
   const int zchunk = (n[2] + chunks - 1) / chunks;
   chunks = (n[2] + zchunk - 1) / zchunk;

@@ -1,11 +1,13 @@
 // FP64 exp and sin evaluated mostly outside the FP64 pipe.
 //
-// On this GPU an FP64 instruction issues at about 2 per clock per SM, a signed 64-bit high
-// product at about 4, an unsigned one at about 7, and 32-bit integer multiply-adds, FP32 arithmetic
-// and f32<->f64 conversions at 60-128.  A kernel whose time goes to FP64 transcendentals therefore
-// runs faster when (1) the FP64 pipe keeps only the one exact Cody-Waite product that needs all 53
-// bits of x, (2) the polynomials run in fixed point with as few 64-bit products as the error
-// budget allows (unsigned), and (3) the low-order terms use FP32 or 32x32-bit products.
+// Measured on this GPU (per clock per SM): FP64 add/FMA and every conversion between FP64 and
+// FP32 or integers about 2 (all on the FP64 pipe); unsigned 64-bit high product about 6; 64-bit
+// integer add, logic, shift and compare 13-45 and 32-bit multiply-adds and FP32 arithmetic more
+// (ALU and FMA pipes).  A kernel whose time goes to FP64 transcendentals therefore runs faster
+// when (1) the FP64 pipe keeps only the one exact Cody-Waite product that needs all 53 bits of x,
+// (2) the polynomials run in fixed point with as few 64-bit products as the error budget allows,
+// (3) the low-order terms use FP32 or 32x32-bit products, and (4) the few FP64<->FP32/integer
+// conversions are built from the bits with integer operations.
 //
 // exp(x), |x| < 708   Tang's table method (P. T. P. Tang, ACM TOMS 15(2), 1989) with 256 entries:
 //     x = (256 m + j) ln2/256 + r,  |r| <= ln2/512 (+0.02 % from the FP32 rounding of k),
@@ -169,11 +171,49 @@ __host__ __device__ __forceinline__ uint64_t fix_to_bits(uint64_t y, int e) {
   return ((uint64_t)(e + 1 - lz + 1022) << 52) + m;
 }
 
+__host__ __device__ __forceinline__ float from_fbits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  std::memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ int clz32(uint32_t a) {
+#ifdef __CUDA_ARCH__
+  return __clz((int)a);
+#else
+  return a ? __builtin_clz(a) : 32;
+#endif
+}
+
+// Conversions between FP64 and FP32 or integers issue on the FP64 pipe on this GPU (at the FP64
+// rate), so the few this code needs are built from the bits with integer operations instead.
+// v as a float, significand truncated (|v| < 2^128; |v| < 2^-126 gives +-0).
+__host__ __device__ __forceinline__ float f32_trunc(double v) {
+  const uint64_t b = bits(v);
+  const uint32_t hi = (uint32_t)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ff);
+  const uint32_t sign = hi & 0x80000000u;
+  const uint32_t f = sign | ((uint32_t)(e - 896) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu);
+  return from_fbits(e > 896 ? f : sign);
+}
+// k (|k| < 2^31) as a double.
+__host__ __device__ __forceinline__ double i32_to_f64(int k) {
+  const uint32_t a = k < 0 ? 0u - (uint32_t)k : (uint32_t)k;
+  const int e = 31 - clz32(a);  // a's top bit
+  const uint64_t m = ((uint64_t)a << (52 - e)) & 0xfffffffffffffULL;
+  const uint64_t b = ((uint64_t)(k < 0) << 63) | ((uint64_t)(1023 + e) << 52) | m;
+  return from_bits(a ? b : 0);
+}
+
 // k = round(x * c) (within one) through FP32, |x * c| < 2^22; kd = k as a double.
 __host__ __device__ __forceinline__ int k_f32(double x, float c, double* kd) {
-  const float t = fmaf((float)x, c, 12582912.0f);  // 1.5 * 2^23
-  *kd = (double)(t - 12582912.0f);
-  return fbits(t) - 0x4B400000;
+  const float t = fmaf(f32_trunc(x), c, 12582912.0f);  // 1.5 * 2^23
+  const int k = fbits(t) - 0x4B400000;
+  *kd = i32_to_f64(k);
+  return k;
 }
 
 // ------------------------------------------------------------------ exp
@@ -192,7 +232,7 @@ __host__ __device__ __forceinline__ double exp_fix(double x, const T& tb) {
   const double r1 = fma(-kd, L1, x);                  // exact
   const int64_t r = to_fix(r1) - mul_k<42>(k, L2_FIX104);
   // g2 = 1/24 + r/120 in FP32, in [2^-5, 2^-4): its significand at 2^35 is exact
-  const float g2 = fmaf((float)r1, 1.0f / 120.0f, 1.0f / 24.0f);
+  const float g2 = fmaf(f32_trunc(r1), 1.0f / 120.0f, 1.0f / 24.0f);
   const int32_t g2f = (int32_t)(((uint32_t)fbits(g2) & 0x7fffffu) | 0x800000u) << 7;
   const int32_t r40 = (int32_t)(r >> 22);  // r at 2^40
   const int64_t g = SIXTH + (((int64_t)r40 * g2f) >> 13);               // 1/6 + r g2

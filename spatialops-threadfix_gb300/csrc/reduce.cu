@@ -343,14 +343,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce4_rows_kernel(const T* __re
                                                                    Acc4* __restrict__ partials) {
   double s = 0.0, q = 0.0;
   long long mx = LLONG_MIN, mn = LLONG_MAX;
-  auto keys = [&](double v) {
-    const long long b = __double_as_longlong(v);
-    if ((b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) {  // not NaN: NaNs never win a comparison
-      const long long k = b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-      mx = k > mx ? k : mx;
-      mn = k < mn ? k : mn;
-    }
-  };
+  auto keys = [&](double v) { keys_add(mx, mn, order_key(v)); };  // NaNs never win a comparison
   walk_rows(base, sy, sz, x0, x1, y0, ny, z0, (int)nrows,
             [&](const double* v) {
               s += sum8(v);

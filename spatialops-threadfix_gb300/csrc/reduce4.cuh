@@ -45,12 +45,22 @@ __device__ __forceinline__ Acc4 shfl_down4(const Acc4& a, int o) {
   b.mn = __shfl_down_sync(0xffffffffu, a.mn, o);
   return b;
 }
-// Block-wide merge; the result is valid in thread 0.
+// Merge without compensation (inside a warp: 32 partials pairwise, a few ulp at most).
+__device__ __forceinline__ void merge4_plain(Acc4& a, const Acc4& b) {
+  a.s += b.s;
+  a.sc += b.sc;
+  a.q += b.q;
+  a.qc += b.qc;
+  a.mx = a.mx > b.mx ? a.mx : b.mx;
+  a.mn = a.mn < b.mn ? a.mn : b.mn;
+}
+
+// Block-wide merge (plain inside each warp, compensated across warps); valid in thread 0.
 __device__ __forceinline__ Acc4 block_reduce4(Acc4 a) {
   __shared__ Acc4 sh[32];
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int lane = tid & 31, wid = tid >> 5;
-  for (int o = 16; o > 0; o >>= 1) merge4(a, shfl_down4(a, o));
+  for (int o = 16; o > 0; o >>= 1) merge4_plain(a, shfl_down4(a, o));
   if (lane == 0) sh[wid] = a;
   __syncthreads();
   const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
@@ -70,16 +80,27 @@ __device__ __forceinline__ Acc4 block_reduce4(Acc4 a) {
 
 __device__ __forceinline__ Acc4 acc4_identity() { return Acc4{0.0, 0.0, 0.0, 0.0, LLONG_MIN, LLONG_MAX}; }
 
+// Order-preserving key of a double; NaN keys fall outside [key(-inf), key(+inf)] (positive
+// NaNs above, negative NaNs below).
+__device__ __forceinline__ long long order_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+constexpr long long KEY_PINF = 0x7ff0000000000000LL, KEY_NINF = (long long)0x800fffffffffffffULL;
+
+// Fold a key into max/min, NaNs skipped (integer compares only).
+__device__ __forceinline__ void keys_add(long long& mx, long long& mn, long long k) {
+  const long long kx = k > KEY_PINF ? LLONG_MIN : k;  // a positive NaN never wins max
+  const long long kn = k < KEY_NINF ? LLONG_MAX : k;  // a negative NaN never wins min
+  mx = kx > mx ? kx : mx;
+  mn = kn < mn ? kn : mn;
+}
+
 // Fold one value into a thread's accumulator (two FP64 operations; the keys on the integer pipe).
 __device__ __forceinline__ void acc4_add(Acc4& a, double v) {
   a.s += v;
   a.q = fma(v, v, a.q);
-  const long long b = __double_as_longlong(v);
-  if ((b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) {
-    const long long k = b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-    a.mx = k > a.mx ? k : a.mx;
-    a.mn = k < a.mn ? k : a.mn;
-  }
+  keys_add(a.mx, a.mn, order_key(v));
 }
 
 // out = {sum, max, min, norm} of the partial accumulators (one block).
