@@ -49,10 +49,13 @@ BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
     # one RK stage: phi (stencil) + u,v,w,lambda read, state accumulation read/written
     "transport": 8 * 5 + 8 + 8,            # FP64: phi, u, v, w, lam, acc read; out written
     "transport32": 4 * 5 + 8 + 8 + 4,      # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
+    # one reverse step: T_k, A_{k+1}, lambda read, glam read and written, A_k written
+    "adjoint": 8 * 6,
 }
 DOMINANT = {"deep": "deep_chain", "heat": "heat_step_f64", "heat32": "heat_step_f32",
             "patches": "patches_step_f64", "patches32": "patches_step_f32",
-            "transport": "transport_stage_f64", "transport32": "transport_stage_f32"}
+            "transport": "transport_stage_f64", "transport32": "transport_stage_f32",
+            "adjoint": "heat_adjoint_step"}
 
 
 def measured_peak_hbm():
@@ -155,6 +158,7 @@ class Deep:
         self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
         self.cells = n ** 3
         self.launches_per_step = 4  # chain, filter + reductions, ghost-shell reductions, final
+        self.label = f"deep chain {n}^3 + 1 ghost (a SVol; b, c, out, filt XVol; 5% + boundary mask), filter + 4 reductions"
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
         self.d2h_bytes = 4 * 8
         self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
@@ -212,6 +216,7 @@ class Heat:
         from spatialops_gb300 import workloads as W
 
         self.name = "heat" if dtype == "f64" else "heat32"
+        self.label = f"heat {n}^3 + 1 ghost, {'FP64 bit-exact' if dtype == 'f64' else 'FP32'} fused RHS + Euler update"
         self.N, self.n = N, n
         lam, T0, dt = W.heat_inputs((n, n, n))
         self.dt = dt
@@ -267,6 +272,8 @@ class Patches:
         self.ps.arena(0).copy_(self.host)
         self.ps.fill_ghosts(0)
         self.cells = int(np.prod(shapes.astype(np.int64), axis=1).sum())
+        self.label = (f"{count} heat patches, edges ~ U{{16..96}}, 1 ghost, {self.cells / 1e6:.1f} M cells, "
+                      f"{'FP64' if dtype == 'f64' else 'FP32'}; one persistent launch per step")
         self.launches_per_step = 1
         self.h2d_bytes = self.host.numel() * self.host.element_size()
         self.d2h_bytes = 8
@@ -299,6 +306,8 @@ class TransportWL:
         from spatialops_gb300 import workloads as W
 
         self.name = "transport" if dtype == "f64" else "transport32"
+        self.label = (f"transport {n}^3 + 2 ghosts, Heun RK2 step, "
+                      f"{'FP64' if dtype == 'f64' else 'FP32 storage, FP64 state accumulation'}")
         self.N, self.n = N, n
         phi, u, v, w, lam, dt, nu = W.transport_inputs_device(n)
         self.t = N.Transport(np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)),
@@ -325,6 +334,65 @@ class TransportWL:
         self.host_red.copy_(self.red, non_blocking=True)
 
 
+class AdjointWL:
+    """Gradient of J = 1/2 sum (T_N - T_target)^2 w.r.t. T0 and lambda: 500 FP64 heat steps at
+    192^3 with sqrt(N) checkpointing.  A step is one full gradient (forward sweep with
+    checkpoints, segment recomputation, reverse sweep); the metric counts forward cell-steps
+    (n^3 * 500) per second of gradient time, and the line adds the gradient / forward time ratio."""
+
+    name = "adjoint"
+
+    def __init__(self, N, n, steps=500):
+        import torch
+
+        from spatialops_gb300 import workloads as W
+
+        self.N, self.n, self.nsteps = N, n, steps
+        lam, T0, dt, lam_t = W.adjoint_inputs((n, n, n))
+        self.dt = dt
+        self.host = [torch.from_numpy(x).pin_memory() for x in (T0, lam)]
+        self.T0 = N.Field.from_numpy("SVol", T0, 1)
+        self.L = N.Field.from_numpy("SVol", lam, 1)
+        # target: the same run with the perturbed lambda (on the device)
+        self.Tt = N.Field.from_numpy("SVol", T0, 1)
+        tmp = N.Field("SVol", n, 1)
+        N.heat_run(self.Tt, tmp, N.Field.from_numpy("SVol", lam_t, 1), steps, dt)
+        self.cells = n ** 3 * steps
+        self.launches_per_step = None
+        self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host)
+        self.d2h_bytes = 8
+        self.J = 0.0
+        self.label = f"adjoint {n}^3 + 1 ghost, {steps} FP64 steps, sqrt(N) checkpoints"
+        self.metric = "adjoint gradient forward-cell-steps/s"
+        self.cells_per_launch = n ** 3
+
+    def step(self):
+        self.J, self.gT, self.gl = self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt)
+
+    def step_e2e(self):
+        self.T0.tensor.copy_(self.host[0], non_blocking=True)
+        self.L.tensor.copy_(self.host[1], non_blocking=True)
+        self.step()  # J comes back to the host at the end of the call
+
+    def forward_ms(self, reps=2):
+        """Device time of the plain forward run (500 steps, CUDA graph) for the cost ratio."""
+        import torch
+
+        N = self.N
+        T = N.Field("SVol", self.n, 1)
+        tmp = N.Field("SVol", self.n, 1)
+        T.tensor.copy_(self.T0.tensor)
+        N.heat_run(T, tmp, self.L, self.nsteps, self.dt)  # warm (graph capture)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            N.heat_run(T, tmp, self.L, self.nsteps, self.dt)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+
 def make_workload(N, name, n):
     if name in ("transport", "transport32"):
         return TransportWL(N, n, "f64" if name == "transport" else "f32")
@@ -336,6 +404,8 @@ def make_workload(N, name, n):
         return Heat(N, n, "f64")
     if name == "heat32":
         return Heat(N, n, "f32")
+    if name == "adjoint":
+        return AdjointWL(N, 192 if n == N_DEFAULT else n)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -415,7 +485,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="deep", choices=["deep", "heat", "heat32", "patches", "patches32", "transport",
-                                                             "transport32"])
+                                                             "transport32", "adjoint"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -483,7 +553,7 @@ def main():
     value = world * W.cells * args.steps / (ms * 1e-3) / 1e9
 
     # e2e: host buffers, copies inside the timed region
-    e_steps = max(3, min(args.steps, 50))
+    e_steps = max(3, min(args.steps, 50 if W.name != "adjoint" else 3))
     if hasattr(W, "e2e_begin"):
         warm = torch.cuda.Event()
         warm.record(stream)
@@ -515,7 +585,7 @@ def main():
         prof[dom] = {"launches": args.steps, "ms": ms}  # one kernel per step, timed as a whole
     if dom in prof and prof[dom]["launches"]:
         kms = prof[dom]["ms"] / prof[dom]["launches"]
-        alg = BYTES_PER_CELL[W.name] * W.cells
+        alg = BYTES_PER_CELL[W.name] * getattr(W, "cells_per_launch", W.cells)
         achieved = alg / (kms * 1e-3) / 1e9
         traffic = ncu_traffic(dom, f"{W.name}{args.n}")
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -530,14 +600,20 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and W.name in ("deep", "heat", "heat32"):
         cpu = cpu_baseline(W.name, args.n)
+    extra = {}
+    if W.name == "adjoint":
+        fwd = W.forward_ms()
+        extra = {"adjoint_over_forward": (ms / args.steps) / fwd, "forward_ms": fwd,
+                 "forward_value": W.cells / (fwd * 1e-3) / 1e9, "J": W.J}
     line = {
-        "metric": f"{W.name} cell-updates/s", "value": value, "unit": "Gcell-upd/s", "n_gpus": world,
+        "metric": getattr(W, "metric", f"{W.name} cell-updates/s"), "value": value, "unit": "Gcell-upd/s",
+        "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if W.name.endswith("32") else "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": f"{W.name} {args.n}^3 + 1 ghost", "cells_per_step": W.cells,
+        "config": {"workload": getattr(W, "label", f"{W.name} {args.n}^3 + 1 ghost"), "cells_per_step": W.cells,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (129 MB); no flush between steps"},
         "e2e": {"value": e2e_value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": W.h2d_bytes,
@@ -549,6 +625,7 @@ def main():
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

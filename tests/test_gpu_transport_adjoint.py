@@ -121,3 +121,58 @@ def test_adjoint_vs_central_finite_differences(which):
             g = float((gT[I] * d[I]).sum())
         fd = (Jp - Jm) / (2 * eps)
         assert abs(fd - g) <= 1e-6 * abs(g), (fd, g)
+
+
+def _periodic_direction(rng, like):
+    d = np.zeros_like(like)
+    I = (slice(1, -1),) * 3
+    d[I] = rng.normal(size=d[I].shape)
+    return O.fill_periodic(d, 1)
+
+
+def test_adjoint_16_random_directions_autograd():
+    """dJ/d(T0, lambda) through torch.autograd (HeatLoss) against FP64 central finite differences
+    along 16 random joint directions (seed 9, eps = 1e-6)."""
+    import torch
+
+    from autograd_heat import HeatLoss
+
+    n, steps = (24, 20, 16), 40
+    lam, T0, dt, Tt = _setup(n, steps)
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    T0t = cu(T0).requires_grad_(True)
+    lamt = cu(lam).requires_grad_(True)
+    Ttt = cu(Tt)
+    J = HeatLoss.apply(T0t, lamt, Ttt, steps, dt)
+    J.backward()
+    gT, gl = T0t.grad.cpu().numpy(), lamt.grad.cpu().numpy()
+    rng = np.random.default_rng(9)
+    eps = 1e-6
+    for _ in range(16):
+        dT, dl = _periodic_direction(rng, T0), _periodic_direction(rng, lam)
+        Jp = float(HeatLoss.apply(cu(T0 + eps * dT), cu(lam + eps * dl), Ttt, steps, dt))
+        Jm = float(HeatLoss.apply(cu(T0 - eps * dT), cu(lam - eps * dl), Ttt, steps, dt))
+        fd = (Jp - Jm) / (2 * eps)
+        g = float((gT * dT).sum() + (gl * dl).sum())
+        assert abs(fd - g) <= 1e-6 * abs(g), (fd, g)
+
+
+def test_adjoint_composes_with_autograd():
+    """lambda = base * (1 + s * pert): dJ/ds by the chain rule through HeatLoss vs a central difference."""
+    import torch
+
+    from autograd_heat import HeatLoss
+
+    n, steps = (16, 12, 10), 30
+    lam, T0, dt, Tt = _setup(n, steps)
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pert = cu(O.fill_periodic(np.random.default_rng(5).uniform(-1, 1, size=lam.shape), 1))
+    base, T0t, Ttt = cu(lam), cu(T0), cu(Tt)
+    s = torch.tensor(0.05, dtype=torch.float64, device="cuda", requires_grad=True)
+    J = HeatLoss.apply(T0t, base * (1 + s * pert), Ttt, steps, dt)
+    (dJds,) = torch.autograd.grad(J, s)
+    eps = 1e-6
+    Jp = float(HeatLoss.apply(T0t, base * (1 + (0.05 + eps) * pert), Ttt, steps, dt))
+    Jm = float(HeatLoss.apply(T0t, base * (1 + (0.05 - eps) * pert), Ttt, steps, dt))
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(fd - float(dJds)) <= 1e-6 * abs(fd), (fd, float(dJds))
