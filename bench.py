@@ -362,12 +362,27 @@ class AdjointWL:
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host)
         self.d2h_bytes = 8
         self.J = 0.0
-        self.label = f"adjoint {n}^3 + 1 ghost, {steps} FP64 steps, sqrt(N) checkpoints"
+        self.products = "f32"
+        self.label = (f"adjoint {n}^3 + 1 ghost, {steps} FP64 steps, sqrt(N) checkpoints; FP64 adjoint state, "
+                      f"FP32 face products in dJ/dlambda")
         self.metric = "adjoint gradient forward-cell-steps/s"
         self.cells_per_launch = n ** 3
 
     def step(self):
-        self.J, self.gT, self.gl = self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt)
+        self.J, self.gT, self.gl = self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt,
+                                                        products=self.products)
+
+    def gradient_ms(self, products):
+        """Device time of one gradient with the given face-product precision."""
+        import torch
+
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt, products=products)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
 
     def step_e2e(self):
         self.T0.tensor.copy_(self.host[0], non_blocking=True)
@@ -605,8 +620,10 @@ def main():
     extra = {}
     if W.name == "adjoint":
         fwd = W.forward_ms()
+        g64 = W.gradient_ms("f64")
         extra = {"adjoint_over_forward": (ms / args.steps) / fwd, "forward_ms": fwd,
-                 "forward_value": W.cells / (fwd * 1e-3) / 1e9, "J": W.J}
+                 "forward_value": W.cells / (fwd * 1e-3) / 1e9, "J": W.J,
+                 "adjoint_over_forward_all_fp64": g64 / fwd}
     line = {
         "metric": getattr(W, "metric", f"{W.name} cell-updates/s"), "value": value, "unit": "Gcell-upd/s",
         "n_gpus": world,

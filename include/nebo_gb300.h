@@ -230,6 +230,18 @@ int nebo_transport_run(double* phi, const void* u, const void* v, const void* w,
  *   ceil(sqrt(steps)) when <= 0), then the reverse sweep recomputing each segment from its
  *   checkpoint: device memory ~ (steps/L + L) fields.  Writes gT0 = dJ/dT_0 (window with
  *   images), glam = dJ/dlambda (interior; ghosts zero) and *J. */
+/* nebo_heat_gradient with a choice of face-product precision in the lambda gradient:
+ *   NEBO_PRODUCTS_F64  as nebo_heat_gradient (every operation FP64);
+ *   NEBO_PRODUCTS_F32  the per-face products (T_b - T_a)(A_b - A_a) of the lambda gradient are
+ *                      FP32 products of the exactly computed FP64 differences, summed per cell in
+ *                      FP32 and accumulated into glam in FP64 (relative error ~1e-7 in glam);
+ *                      the adjoint state, dJ/dT_0 and J stay FP64.  Six FP64 operations per cell
+ *                      and reverse step fewer. */
+enum { NEBO_PRODUCTS_F64 = 0, NEBO_PRODUCTS_F32 = 1 };
+int nebo_heat_gradient_ex(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget,
+                          int steps, double dt, int checkpoint_every, int products,
+                          const nebo_field* gT0, const nebo_field* glam, double* J,
+                          nebo_stream_t stream);
 int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ain, const nebo_field* Aout,
                            const nebo_field* lam, const nebo_field* glam, double dt,
                            nebo_stream_t stream);

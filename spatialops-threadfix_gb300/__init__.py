@@ -88,6 +88,7 @@ SIGNATURES = [
     ("nebo_transport_run", _I, [_P, _P, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
     ("nebo_heat_adjoint_step", _I, [_FP, _FP, _FP, _FP, _FP, _D, _P]),
     ("nebo_heat_gradient", _I, [_FP, _FP, _FP, _I, _D, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
+    ("nebo_heat_gradient_ex", _I, [_FP, _FP, _FP, _I, _D, _I, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_fastmath_eval", _I, [_I, _P, _P, ctypes.c_size_t, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
@@ -395,15 +396,22 @@ class Transport:
                                         ctypes.c_void_p(self.work.data_ptr()), _stream(stream)))
 
 
-def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None):
-    """(J, dJ/dT0, dJ/dlambda) for J = 1/2 sum (T_N - T_target)^2 (fields: SVol, 1 ghost, FP64)."""
+def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None, products="f64"):
+    """(J, dJ/dT0, dJ/dlambda) for J = 1/2 sum (T_N - T_target)^2 (fields: SVol, 1 ghost, FP64).
+
+    products="f32": the lambda gradient's face products in FP32 (nebo_heat_gradient_ex)."""
     gT = Field(T0.loc, T0.n, T0.ghost)
     gl = Field(T0.loc, T0.n, T0.ghost)
     J = ctypes.c_double()
     a, b, c, d, e = T0.desc(), lam.desc(), Ttarget.desc(), gT.desc(), gl.desc()
-    _check(lib().nebo_heat_gradient(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt),
-                                    int(checkpoint_every), ctypes.byref(d), ctypes.byref(e), ctypes.byref(J),
-                                    _stream(stream)))
+    if products == "f64":
+        _check(lib().nebo_heat_gradient(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt),
+                                        int(checkpoint_every), ctypes.byref(d), ctypes.byref(e), ctypes.byref(J),
+                                        _stream(stream)))
+    else:
+        _check(lib().nebo_heat_gradient_ex(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps),
+                                           float(dt), int(checkpoint_every), {"f32": 1}[products], ctypes.byref(d),
+                                           ctypes.byref(e), ctypes.byref(J), _stream(stream)))
     return J.value, gT, gl
 
 

@@ -13,13 +13,17 @@
 // One kernel per reverse step computes both, with every face quantity computed once and shared
 // through shared memory (x, y) or carried in a register (z), and writes abar's ghost images.
 //
-// Memory: sqrt(N) checkpointing.  The forward sweep keeps T at every L-th step (L = ceil(sqrt N));
-// the reverse sweep recomputes each segment's L states from its checkpoint into a segment buffer
-// and walks it backwards, so device memory grows like 2*sqrt(N) fields, not N.
+// Memory: sqrt(N) checkpointing.  The forward sweep keeps T at every L-th step (L = ceil(sqrt N))
+// and the states of the last segment; the reverse sweep recomputes each earlier segment's states
+// from its checkpoint into a segment buffer and walks it backwards, so device memory grows like
+// 2*sqrt(N) fields, not N, and the forward work is about 2N - sqrt(N) steps.
 #include <cmath>
 #include <vector>
 
+#include <type_traits>
+
 #include "common.cuh"
+#include "fp64_int.cuh"
 
 namespace nebo {
 namespace {
@@ -41,25 +45,30 @@ __device__ __forceinline__ void store_images1(double* base, int sy, long sz, int
   }
 }
 
-struct Face {
-  double fa;  // (lam_a + lam_b) * (abar_b - abar_a)
-  double p;   // (T_b - T_a) * (abar_b - abar_a)
-};
-
-__device__ __forceinline__ Face face(const double* T, const double* A, const double* L, long a, long b) {
-  const double da = A[b] - A[a];
-  Face f;
-  f.fa = (__ldg(L + a) + __ldg(L + b)) * da;
-  f.p = (__ldg(T + b) - __ldg(T + a)) * da;
-  return f;
-}
-
-__global__ void __launch_bounds__(BX* BY) heat_adjoint_kernel(const double* __restrict__ T, const double* __restrict__ Ain,
+// One reverse step.  Per face (a, b = a + s) the thread that owns the face computes
+//   dA = A[b] - A[a],  dT = T[b] - T[a]                                   (FP64)
+// and shares them (x, y through shared memory, z in a register).  Per cell c:
+//   Aout[c] = A[c] + (dt/2) * sum_faces +-lf_face * dA_face              (FP64 FMA chain)
+//   glam[c] -= (dt/2) * sum_faces dT_face * dA_face
+// with lf_face = lambda[a] + lambda[b] either read from precomputed face arrays (LF) or summed
+// from lambda.  EXACT: the face products dT*dA in FP64 (an FMA chain).  Otherwise each face
+// product is an FP32 product of the FP32-rounded FP64 differences (relative error ~1e-7; the
+// differences themselves are exact FP64, so no cancellation is amplified), their sum is FP32 and
+// only the fold into glam is FP64: 6 FP64 operations per cell fewer, and the adjoint state A,
+// hence dJ/dT0, is unaffected.
+template <bool EXACT, bool LF>
+__global__ void __launch_bounds__(BX* BY, 4) heat_adjoint_kernel(const double* __restrict__ T, const double* __restrict__ Ain,
                                                               double* __restrict__ Aout, const double* __restrict__ L,
-                                                              double* __restrict__ glam, int sy, long sz, int nx, int ny,
-                                                              int nz, int zchunk, double hdt) {
-  __shared__ Face sfx[2][BY][BX + 1];
-  __shared__ Face sfy[2][BY + 1][BX];
+                                                              const double* __restrict__ lfx,
+                                                              const double* __restrict__ lfy,
+                                                              const double* __restrict__ lfz, double* __restrict__ glam,
+                                                              int sy, long sz, int nx, int ny, int nz, int zchunk,
+                                                              double hdt) {
+  typedef typename std::conditional<EXACT, double, float>::type P;  // face-product operand type
+  __shared__ double sax[2][BY][BX + 1];
+  __shared__ double say[2][BY + 1][BX];
+  __shared__ P stx[2][BY][BX + 1];
+  __shared__ P sty[2][BY + 1][BX];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
   const int x = x0 + tx, y = y0 + ty;
@@ -67,31 +76,84 @@ __global__ void __launch_bounds__(BX* BY) heat_adjoint_kernel(const double* __re
   const bool active = x < nx && y < ny;
   const int xc = min(x, nx), yc = min(y, ny);
   auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
-  Face fzlo = face(T, Ain, L, at(xc, yc, z0 - 1), at(xc, yc, z0));
+  // (dA, dT) of face (a, b); dT as the product operand type
+  auto face = [&](long a, long b, double& da, P& dt) {
+    da = __ldg(Ain + b) - __ldg(Ain + a);
+    const double d = __ldg(T + b) - __ldg(T + a);
+    if constexpr (EXACT) dt = d; else dt = fixmath::f32_trunc(d);
+  };
+  auto coef = [&](const double* lf, long a, long b) { return LF ? __ldg(lf + b) : __ldg(L + a) + __ldg(L + b); };
+  double dazl;
+  P dtzl;
+  face(at(xc, yc, z0 - 1), at(xc, yc, z0), dazl, dtzl);
   for (int z = z0; z < z1; ++z) {
     const int buf = z & 1;
     const long c = at(xc, yc, z);
-    const Face fzhi = face(T, Ain, L, c, c + sz);
-    const Face fx = face(T, Ain, L, c - 1, c);
-    const Face fy = face(T, Ain, L, c - sy, c);
-    sfx[buf][ty][tx] = fx;
-    sfy[buf][ty][tx] = fy;
+    double dazh, dax, day;
+    P dtzh, dtx, dty;
+    face(c, c + sz, dazh, dtzh);
+    face(c - 1, c, dax, dtx);
+    face(c - sy, c, day, dty);
+    sax[buf][ty][tx] = dax;
+    stx[buf][ty][tx] = dtx;
+    say[buf][ty][tx] = day;
+    sty[buf][ty][tx] = dty;
     if (ty == 0) {
       const int yh = y0 + BY;
-      if (yh <= ny && x <= nx) sfy[buf][BY][tx] = face(T, Ain, L, at(xc, yh - 1, z), at(xc, yh, z));
+      if (yh <= ny && x <= nx) face(at(xc, yh - 1, z), at(xc, yh, z), say[buf][BY][tx], sty[buf][BY][tx]);
     } else if (ty == 1 && tx < BY) {
       const int xh = x0 + BX, yr = y0 + tx;
-      if (xh <= nx && yr < ny) sfx[buf][tx][BX] = face(T, Ain, L, at(xh - 1, yr, z), at(xh, yr, z));
+      if (xh <= nx && yr < ny) face(at(xh - 1, yr, z), at(xh, yr, z), sax[buf][tx][BX], stx[buf][tx][BX]);
     }
     __syncthreads();
     if (active) {
-      const Face fxhi = sfx[buf][ty][tx + 1], fyhi = sfy[buf][ty + 1][tx];
-      const double s = ((fxhi.fa - fx.fa) + (fyhi.fa - fy.fa)) + (fzhi.fa - fzlo.fa);
-      const double ps = ((fx.p + fxhi.p) + (fy.p + fyhi.p)) + (fzlo.p + fzhi.p);
-      store_images1(Aout, sy, sz, x, y, z, nx, ny, nz, Ain[c] + hdt * s);
-      glam[c] -= hdt * ps;
+      const double daxh = sax[buf][ty][tx + 1], dayh = say[buf][ty + 1][tx];
+      const P dtxh = stx[buf][ty][tx + 1], dtyh = sty[buf][ty + 1][tx];
+      double s = dazh * coef(lfz, c, c + sz);
+      s = fma(-dazl, coef(lfz, c - sz, c), s);
+      s = fma(dayh, coef(lfy, c, c + sy), s);
+      s = fma(-day, coef(lfy, c - sy, c), s);
+      s = fma(daxh, coef(lfx, c, c + 1), s);
+      s = fma(-dax, coef(lfx, c - 1, c), s);
+      store_images1(Aout, sy, sz, x, y, z, nx, ny, nz, fma(hdt, s, Ain[c]));
+      double ps;
+      if constexpr (EXACT) {
+        ps = dtzh * dazh;
+        ps = fma(dtzl, dazl, ps);
+        ps = fma(dtyh, dayh, ps);
+        ps = fma(dty, day, ps);
+        ps = fma(dtxh, daxh, ps);
+        ps = fma(dtx, dax, ps);
+      } else {
+        using fixmath::f32_trunc;
+        float q = dtzh * f32_trunc(dazh);
+        q = fmaf(dtzl, f32_trunc(dazl), q);
+        q = fmaf(dtyh, f32_trunc(dayh), q);
+        q = fmaf(dty, f32_trunc(day), q);
+        q = fmaf(dtxh, f32_trunc(daxh), q);
+        q = fmaf(dtx, f32_trunc(dax), q);
+        ps = fixmath::f32_to_f64(q);
+      }
+      glam[c] = fma(-hdt, ps, glam[c]);
     }
-    fzlo = fzhi;
+    dazl = dazh;
+    dtzl = dtzh;
+  }
+}
+
+// Face coefficients lf_d[c] = lambda[c - s_d] + lambda[c] for the faces the reverse step reads:
+// along axis d indices 0..n_d (the last one is the high face of the last cell), the other two
+// axes 0..n-1.
+__global__ void face_coef_kernel(const double* __restrict__ L, double* __restrict__ lfx, double* __restrict__ lfy,
+                                 double* __restrict__ lfz, int sy, long sz, int nx, int ny, int nz) {
+  const long total = (long)(nx + 1) * (ny + 1) * (nz + 1);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % (nx + 1)), y = (int)((i / (nx + 1)) % (ny + 1)), z = (int)(i / ((long)(nx + 1) * (ny + 1)));
+    const long c = (long)x + (long)sy * y + sz * z;
+    const double lc = L[c];
+    if (y < ny && z < nz) lfx[c] = L[c - 1] + lc;
+    if (x < nx && z < nz) lfy[c] = L[c - sy] + lc;
+    if (x < nx && y < ny) lfz[c] = L[c - sz] + lc;
   }
 }
 
@@ -150,16 +212,47 @@ extern "C" int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ai
   chunks = (n[2] + zchunk - 1) / zchunk;
   cudaStream_t s = (cudaStream_t)stream;
   LaunchScope ls("heat_adjoint_step", s);
-  heat_adjoint_kernel<<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(vt.base, va.base, vo.base, vl.base, vg.base,
-                                                                        vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
+  heat_adjoint_kernel<true, false><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
+      vt.base, va.base, vo.base, vl.base, nullptr, nullptr, nullptr, vg.base, vt.sy, vt.sz, n[0], n[1], n[2], zchunk,
+      0.5 * dt);
   NEBO_LAUNCH_CHECK("nebo_heat_adjoint_step");
   return NEBO_OK;
 }
 
 namespace {
+// One reverse step of the gradient driver: precomputed face coefficients (View bases of the
+// three face arrays, same layout as T), exact or FP32 face products.
+int adjoint_step_lf(const nebo_field* Tk, const nebo_field* Ain, const nebo_field* Aout, const double* lfx,
+                    const double* lfy, const double* lfz, const nebo_field* glam, double dt, bool exact,
+                    cudaStream_t s) {
+  int n[3];
+  interior_extent(*Tk, n);
+  const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
+                     vg = make_view<double>(*glam);
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
+  chunks = chunks < 1 ? 1 : (chunks > (n[2] + 7) / 8 ? (n[2] + 7) / 8 : chunks);
+  const int zchunk = (n[2] + chunks - 1) / chunks;
+  chunks = (n[2] + zchunk - 1) / zchunk;
+  LaunchScope ls("heat_adjoint_step", s);
+  if (exact)
+    heat_adjoint_kernel<true, true><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
+        vt.base, va.base, vo.base, nullptr, lfx, lfy, lfz, vg.base, vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
+  else
+    heat_adjoint_kernel<false, true><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
+        vt.base, va.base, vo.base, nullptr, lfx, lfy, lfz, vg.base, vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
+  NEBO_LAUNCH_CHECK("nebo_heat_gradient (reverse step)");
+  return NEBO_OK;
+}
+}  // namespace
+
+namespace {
+// Buffers of the pool (each one field): [0, nck) checkpoints T_0, T_L, ...; [nck, nck+L) segment
+// states; two adjoint states; one forward temporary; three face-coefficient arrays; then 256
+// doubles of loss partials.
 int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const nebo_field* T0, const nebo_field* lam,
-                  const nebo_field* Ttarget, int steps, double dt, const nebo_field* gT0, const nebo_field* glam,
-                  double* J, nebo_stream_t stream) {
+                  const nebo_field* Ttarget, int steps, double dt, bool exact, const nebo_field* gT0,
+                  const nebo_field* glam, double* J, nebo_stream_t stream) {
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = cells * sizeof(double);
   auto buf = [&](size_t i) { return pool + i * cells; };
@@ -172,69 +265,114 @@ int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const ne
   const double unit[3] = {1.0, 1.0, 1.0};
   int rc = NEBO_OK;
   nebo_field lamf = *lam;
-  // lambda's ghosts must be periodic images (they are read at boundary faces)
+  int n[3];
+  interior_extent(*T0, n);
+  // lambda's ghosts must be periodic images (they are read at boundary faces); face coefficients
   if ((rc = fill_periodic_any(&lamf, s))) return rc;
-  // forward sweep with checkpoints
+  double* A0 = buf(nck + L);
+  double* A1 = buf(nck + L + 1);
+  double* tmp = buf(nck + L + 2);
+  const View<double> vl = make_view<double>(lamf);
+  const long origin = vl.base - (const double*)lamf.data;  // interior origin within a window
+  double* lf[3] = {buf(nck + L + 3) + origin, buf(nck + L + 4) + origin, buf(nck + L + 5) + origin};
+  {
+    LaunchScope ls("face_coef", s);
+    face_coef_kernel<<<num_sms() * 4, 256, 0, s>>>(vl.base, lf[0], lf[1], lf[2], vl.sy, vl.sz, n[0], n[1], n[2]);
+    NEBO_LAUNCH_CHECK("nebo_heat_gradient (face coefficients)");
+  }
+  // forward sweep: checkpoints every L steps; the last segment's states go straight to the
+  // segment buffers (they need no recomputation)
+  const int klast = (nck - 1) * L;
   NEBO_CUDA_TRY(cudaMemcpyAsync(buf(0), T0->data, bytes, cudaMemcpyDeviceToDevice, s));
   {
     nebo_field c0 = field_at(buf(0));
     if ((rc = fill_periodic_any(&c0, s))) return rc;
   }
+  double* cur = buf(0);
+  for (int k = 0; k < steps && !rc; ++k) {
+    const int j = k + 1;  // state being written
+    double* nxt;
+    if (j == steps)
+      nxt = cur == tmp ? A1 : tmp;
+    else if (j % L == 0)
+      nxt = buf(j / L);
+    else if (j > klast)
+      nxt = buf(nck + (j - klast - 1));
+    else
+      nxt = cur == tmp ? A1 : tmp;
+    nebo_field a = field_at(cur), b = field_at(nxt);
+    rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
+    cur = nxt;
+  }
+  if (rc) return rc;
+  // seed: abar_N = T_N - T_target, J (the final state is in tmp or A1; the seed goes to A0)
+  const View<double> vt = make_view<double>(field_at(cur));
+  const View<double> vtt = make_view<double>(*Ttarget);
+  const View<double> va = make_view<double>(field_at(A0));
   {
-    double* tmp = buf(nbuf - 1);
-    double* cur = buf(0);
-    for (int k = 0; k < steps && !rc; ++k) {
-      double* nxt = ((k + 1) % L == 0 && (k + 1) / L < nck) ? buf((k + 1) / L) : (cur == tmp ? buf(nbuf - 2) : tmp);
-      nebo_field a = field_at(cur), b = field_at(nxt);
+    LaunchScope ls("loss_seed", s);
+    loss_seed_kernel<<<256, 256, 0, s>>>(vt.base, vtt.base, va.base, vt.sy, vt.sz, n[0], n[1], n[2], partial);
+  }
+  NEBO_CUDA_TRY(cudaGetLastError());
+  double hp[256];
+  NEBO_CUDA_TRY(cudaMemcpyAsync(hp, partial, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  NEBO_CUDA_TRY(cudaMemsetAsync(glam->data, 0, bytes, s));
+  // reverse sweep, segment by segment
+  double* Ain = A0;
+  double* Aout = A1;
+  for (int seg = nck - 1; seg >= 0 && !rc; --seg) {
+    const int k0 = seg * L, k1 = (k0 + L < steps) ? k0 + L : steps;  // states k0 .. k1-1
+    // recompute states k0+1 .. k1-1 into the segment buffers (state k0 is the checkpoint)
+    for (int k = k0; seg != nck - 1 && k + 1 < k1 && !rc; ++k) {
+      nebo_field a = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
+      nebo_field b = field_at(buf(nck + (k - k0)));
       rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
-      cur = nxt;
     }
-    if (rc) return rc;
-    // seed: abar_N = T_N - T_target, J
-    double* A0 = buf(nck + L);
-    double* A1 = buf(nck + L + 1);
-    const View<double> vt = make_view<double>(field_at(cur));
-    const View<double> vtt = make_view<double>(*Ttarget);
-    const View<double> va = make_view<double>(field_at(A0));
-    int n[3];
-    interior_extent(*T0, n);
-    {
-      LaunchScope ls("loss_seed", s);
-      loss_seed_kernel<<<256, 256, 0, s>>>(vt.base, vtt.base, va.base, vt.sy, vt.sz, n[0], n[1], n[2], partial);
-    }
-    NEBO_CUDA_TRY(cudaGetLastError());
-    double hp[256];
-    NEBO_CUDA_TRY(cudaMemcpyAsync(hp, partial, sizeof(hp), cudaMemcpyDeviceToHost, s));
-    NEBO_CUDA_TRY(cudaMemsetAsync(glam->data, 0, bytes, s));
-    // reverse sweep, segment by segment
-    double* Ain = A0;
-    double* Aout = A1;
-    for (int seg = nck - 1; seg >= 0 && !rc; --seg) {
-      const int k0 = seg * L, k1 = (k0 + L < steps) ? k0 + L : steps;  // states k0 .. k1-1
-      // recompute states k0+1 .. k1-1 into the segment buffers (state k0 is the checkpoint)
-      for (int k = k0; k + 1 < k1 && !rc; ++k) {
-        nebo_field a = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
-        nebo_field b = field_at(buf(nck + (k - k0)));
-        rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
-      }
-      for (int k = k1 - 1; k >= k0 && !rc; --k) {
-        nebo_field tk = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
-        nebo_field ai = field_at(Ain), ao = field_at(Aout);
-        rc = nebo_heat_adjoint_step(&tk, &ai, &ao, &lamf, glam, dt, stream);
-        double* t = Ain;
-        Ain = Aout;
-        Aout = t;
-      }
-    }
-    if (rc) return rc;
-    NEBO_CUDA_TRY(cudaMemcpyAsync(gT0->data, Ain, bytes, cudaMemcpyDeviceToDevice, s));
-    NEBO_CUDA_TRY(cudaStreamSynchronize(s));
-    if (J) {
-      double t = 0.0;
-      for (int i = 0; i < 256; ++i) t += hp[i];
-      *J = 0.5 * t;
+    for (int k = k1 - 1; k >= k0 && !rc; --k) {
+      nebo_field tk = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
+      nebo_field ai = field_at(Ain), ao = field_at(Aout);
+      rc = adjoint_step_lf(&tk, &ai, &ao, lf[0], lf[1], lf[2], glam, dt, exact, s);
+      double* t = Ain;
+      Ain = Aout;
+      Aout = t;
     }
   }
+  if (rc) return rc;
+  NEBO_CUDA_TRY(cudaMemcpyAsync(gT0->data, Ain, bytes, cudaMemcpyDeviceToDevice, s));
+  NEBO_CUDA_TRY(cudaStreamSynchronize(s));
+  if (J) {
+    double t = 0.0;
+    for (int i = 0; i < 256; ++i) t += hp[i];
+    *J = 0.5 * t;
+  }
+  return rc;
+}
+
+int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps, double dt,
+                   int checkpoint_every, bool exact, const nebo_field* gT0, const nebo_field* glam, double* J,
+                   nebo_stream_t stream, const char* what) {
+  const nebo_field* fs[5] = {T0, lam, Ttarget, gT0, glam};
+  for (int i = 0; i < 5; ++i) {
+    int rc = check_field(fs[i], what);
+    if (rc) return rc;
+    if (fs[i]->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: FP64 only", what);
+    if ((rc = check_periodic_patch(fs[i], 1, what))) return rc;
+    if (i && (rc = check_same_layout(T0, fs[i], what))) return rc;
+  }
+  if (steps < 1) return fail(NEBO_ERR_INVALID, "Nebo error in %s: steps < 1", what);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
+  const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
+  const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
+  const size_t bytes = cells * sizeof(double);
+  // device memory: nck checkpoints + L segment states + 2 adjoint states + 1 forward temp +
+  // 3 face-coefficient arrays, ~ (2 sqrt(N) + 6) fields
+  const size_t nbuf = (size_t)nck + (size_t)L + 6;
+  double* pool = nullptr;
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&pool, nbuf * bytes + 256 * sizeof(double), s));
+  const int rc = gradient_impl(pool, cells, nck, L, (int)nbuf, T0, lam, Ttarget, steps, dt, exact, gT0, glam, J,
+                               stream);
+  cudaFreeAsync(pool, s);
   return rc;
 }
 }  // namespace
@@ -245,25 +383,15 @@ int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const ne
 extern "C" int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
                                   double dt, int checkpoint_every, const nebo_field* gT0, const nebo_field* glam,
                                   double* J, nebo_stream_t stream) {
-  const nebo_field* fs[5] = {T0, lam, Ttarget, gT0, glam};
-  for (int i = 0; i < 5; ++i) {
-    int rc = check_field(fs[i], "nebo_heat_gradient");
-    if (rc) return rc;
-    if (fs[i]->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_heat_gradient: FP64 only");
-    if ((rc = check_periodic_patch(fs[i], 1, "nebo_heat_gradient"))) return rc;
-    if (i && (rc = check_same_layout(T0, fs[i], "nebo_heat_gradient"))) return rc;
-  }
-  if (steps < 1) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_heat_gradient: steps < 1");
-  cudaStream_t s = (cudaStream_t)stream;
-  const int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
-  const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
-  const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
-  const size_t bytes = cells * sizeof(double);
-  // device memory: nck checkpoints + L segment states + 2 adjoint buffers + 1 forward temp
-  const size_t nbuf = (size_t)nck + (size_t)L + 3;
-  double* pool = nullptr;
-  NEBO_CUDA_TRY(cudaMallocAsync((void**)&pool, nbuf * bytes + 1024 * sizeof(double), s));
-  const int rc = gradient_impl(pool, cells, nck, L, (int)nbuf, T0, lam, Ttarget, steps, dt, gT0, glam, J, stream);
-  cudaFreeAsync(pool, s);
-  return rc;
+  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, true, gT0, glam, J, stream,
+                        "nebo_heat_gradient");
+}
+
+extern "C" int nebo_heat_gradient_ex(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
+                                     double dt, int checkpoint_every, int products, const nebo_field* gT0,
+                                     const nebo_field* glam, double* J, nebo_stream_t stream) {
+  if (products != NEBO_PRODUCTS_F64 && products != NEBO_PRODUCTS_F32)
+    return fail(NEBO_ERR_INVALID, "Nebo error in nebo_heat_gradient_ex: products %d", products);
+  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, products == NEBO_PRODUCTS_F64, gT0, glam, J,
+                        stream, "nebo_heat_gradient_ex");
 }

@@ -199,6 +199,13 @@ __host__ __device__ __forceinline__ float f32_trunc(double v) {
   const uint32_t f = sign | ((uint32_t)(e - 896) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu);
   return from_fbits(e > 896 ? f : sign);
 }
+// A float as a double (subnormal floats give +-0).
+__host__ __device__ __forceinline__ double f32_to_f64(float f) {
+  const uint32_t b = (uint32_t)fbits(f);
+  const uint32_t e = (b >> 23) & 0xff;
+  const uint64_t d = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
+  return from_bits(e ? d : (uint64_t)(b & 0x80000000u) << 32);
+}
 // k (|k| < 2^31) as a double.
 __host__ __device__ __forceinline__ double i32_to_f64(int k) {
   const uint32_t a = k < 0 ? 0u - (uint32_t)k : (uint32_t)k;

@@ -176,3 +176,27 @@ def test_adjoint_composes_with_autograd():
     Jm = float(HeatLoss.apply(T0t, base * (1 + (0.05 - eps) * pert), Ttt, steps, dt))
     fd = (Jp - Jm) / (2 * eps)
     assert abs(fd - float(dJds)) <= 1e-6 * abs(fd), (fd, float(dJds))
+
+
+def test_adjoint_f32_face_products():
+    """nebo_heat_gradient_ex(NEBO_PRODUCTS_F32): dJ/dT0 and J as the all-FP64 gradient (1e-12),
+    dJ/dlambda within 1e-6 of the oracle adjoint, and against central differences."""
+    n, steps = (24, 20, 16), 40
+    lam, T0, dt, Tt = _setup(n, steps)
+    F = lambda a: N.Field.from_numpy("SVol", a, 1)
+    J, gT, gl = N.heat_gradient(F(T0), F(lam), F(Tt), steps, dt, products="f32")
+    J64, gT64, gl64 = _gpu_grad(lam, T0, Tt, steps, dt)
+    I = (slice(1, -1),) * 3
+    gT, gl = gT.numpy(), gl.numpy()
+    assert abs(J - J64) <= 1e-14 * J64
+    assert _rel(gT[I], gT64[I]) <= 1e-12
+    assert _rel(gl[I], gl64[I]) <= 1e-6
+    rng = np.random.default_rng(9)
+    eps = 1e-6
+    for _ in range(4):
+        dl = _periodic_direction(rng, lam)
+        Jp = N.heat_gradient(F(T0), F(lam + eps * dl), F(Tt), steps, dt)[0]
+        Jm = N.heat_gradient(F(T0), F(lam - eps * dl), F(Tt), steps, dt)[0]
+        fd = (Jp - Jm) / (2 * eps)
+        g = float((gl[I] * dl[I]).sum())
+        assert abs(fd - g) <= 1e-6 * abs(g), (fd, g)
