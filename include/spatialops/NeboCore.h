@@ -214,13 +214,38 @@ struct DCond {
 // (NeboStencils.h:407-448).  Ghost rule: arg ghosts + min over points of
 // additive_reductive_point_to_ghost (NeboStencils.h:222-239).
 template <typename PointType, typename CollectionType>
+struct NeboStencilPointCollection;
+namespace nebo_detail {
+// Last (the innermost, first-listed point) and AllButLast of a point collection
+// (NeboStencils.h:197-278).
+template <class P, class C>
+struct PtsTail {
+  typedef typename C::Last Last;
+  typedef NeboStencilPointCollection<P, typename C::AllButLast> AllButLast;
+};
+template <class P>
+struct PtsTail<P, NeboNil> {
+  typedef P Last;
+  typedef NeboNil AllButLast;
+};
+}  // namespace nebo_detail
+
+template <typename PointType, typename CollectionType>
 struct NeboStencilPointCollection {
   typedef PointType Point;
   typedef CollectionType Collection;
   typedef NeboStencilPointCollection<Point, Collection> MyType;
   typedef Point First;
   typedef Collection AllButFirst;
+  typedef typename nebo_detail::PtsTail<Point, Collection>::Last Last;
+  typedef typename nebo_detail::PtsTail<Point, Collection>::AllButLast AllButLast;
   enum { length = 1 + Collection::length };
+  // the edgeless stencil's ghost rule: this point additive only, the rest as in possible_ghosts
+  static GhostData possible_additive_ghosts() {
+    return Collection::length == 0 ? additive_point_to_ghost(Point::int_vec())
+                                   : min(additive_point_to_ghost(Point::int_vec()), rest_ghosts());
+  }
+  static GhostData possible_additive_ghosts(const GhostData& g) { return g + possible_additive_ghosts(); }
   template <typename NewPoint>
   struct AddPoint {
     typedef NeboStencilPointCollection<NewPoint, MyType> Result;
@@ -268,6 +293,12 @@ struct NeboStencilCoefCollection {
     return c[index];
   }
   double last() const { return c[0]; }
+  // every coefficient but the first listed one
+  NeboStencilCoefCollection<Length - 1> all_but_last() const {
+    NeboStencilCoefCollection<Length - 1> o;
+    for (int i = 0; i < Length - 1; ++i) o.c[i] = c[i + 1];
+    return o;
+  }
 };
 
 template <>
@@ -397,6 +428,29 @@ struct MaskNode {
   }
 };
 
+// A mask read at a shifted point (NeboMaskShift, NeboStencils.h:1048-1213): true at (x,y,z) when
+// the mask holds (x,y,z) + P.  Ghosts: the mask's plus additive_reductive_point_to_ghost(P).
+template <class P>
+struct DMaskShift {
+  DMask m;
+  __device__ __forceinline__ bool check(int x, int y, int z) const { return m.check(x + P::X, y + P::Y, z + P::Z); }
+};
+template <class P, class F>
+struct MaskShiftNode {
+  typedef bool value_type;
+  MaskNode<F> m;
+  explicit MaskShiftNode(const SpatialMask<F>& mk) : m(mk) {}
+  GhostData ghosts_with_bc() const { return m.ghosts_with_bc() + additive_reductive_point_to_ghost(P::int_vec()); }
+  GhostData ghosts_without_bc() const {
+    return m.ghosts_without_bc() + additive_reductive_point_to_ghost(P::int_vec());
+  }
+  bool has_extents() const { return m.has_extents(); }
+  IntVec extents() const { return m.extents(); }
+  IntVec has_bc() const { return m.has_bc(); }
+  void prepare() const { m.prepare(); }
+  DMaskShift<P> device() const { return DMaskShift<P>{m.device()}; }
+};
+
 // Nodes with children: ghosts are the min over children; extents and BC flags come from the
 // first child that has extents (NeboOperators.h:56-100).
 template <class A, class B>
@@ -512,6 +566,15 @@ struct StencilNode {
     for (int i = 0; i < Pts::length; ++i) d.c[i] = coefs.c[i];
     return d;
   }
+};
+
+// A stencil without the edge (reductive) part of the ghost rule (NeboEdgelessStencil,
+// NeboStencils.h:526-824): the same weighted sum, ghosts from possible_additive_ghosts.
+template <typename T, class Pts, class A>
+struct EdgelessStencilNode : StencilNode<T, Pts, A> {
+  EdgelessStencilNode(const A& a_, const NeboStencilCoefCollection<Pts::length>& c) : StencilNode<T, Pts, A>(a_, c) {}
+  GhostData ghosts_with_bc() const { return Pts::possible_additive_ghosts(this->a.ghosts_with_bc()); }
+  GhostData ghosts_without_bc() const { return Pts::possible_additive_ghosts(this->a.ghosts_without_bc()); }
 };
 
 template <typename T, class Pts, class A>

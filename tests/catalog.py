@@ -214,4 +214,69 @@ def run_catalog(domain):
         C.val("red_x_sum", O.reduce("sum", xa))
         C.val("red_x_max_interior", O.reduce("max", xb, interior=True))
     C.case("red_xvol", red_x)
+
+    # boundary conditions (NeboBoundaryConditionBuilder over whole boundary planes)
+    n = C.n
+
+    def plane(axis, i):
+        a1, a2 = (axis + 1) % 3, (axis + 2) % 3
+        pts = []
+        for v in range(n[a2]):
+            for u in range(n[a1]):
+                q = [0, 0, 0]
+                q[axis], q[a1], q[a2] = i, u, v
+                pts.append(tuple(q))
+        return pts
+
+    def evaluated(loc, expr):
+        f = C.fresh(loc)
+        O.assign(f, expr)
+        return O.field_values(f)
+
+    def stencil(builder):
+        st = builder(a)
+        return st.pts, st.coefs
+
+    def copy_of(loc, src):
+        f = C.fresh(loc)
+        O.assign(f, src)
+        return f
+
+    def bc_gradx():
+        pts, cf = stencil(db.grad("SVol", "SSurfX"))
+        phi = copy_of("SVol", a)
+        O.bc_apply(phi, O.field_values(C.inp("SSurfX", 0)), plane(0, 0),
+                   O.bc_geometry(pts, cf, "SVol", "SSurfX", True))
+        O.bc_apply(phi, lambda x, y, z: 0.75, plane(0, n[0]), O.bc_geometry(pts, cf, "SVol", "SSurfX", False))
+        C.rec("bc_gradx_field_and_scalar", phi)
+    C.case("bc_gradx_field_and_scalar", bc_gradx)
+
+    def bc_interpy():
+        pts, cf = stencil(db.interp("SVol", "SSurfY"))
+        phi = copy_of("SVol", b)
+        gy = C.inp("SSurfY", 1)
+        O.bc_apply(phi, evaluated("SSurfY", O.sin(gy) * 2.0 + 1.0), plane(1, 0),
+                   O.bc_geometry(pts, cf, "SVol", "SSurfY", True))
+        O.bc_apply(phi, evaluated("SSurfY", gy - 0.5), plane(1, n[1]),
+                   O.bc_geometry(pts, cf, "SVol", "SSurfY", False))
+        C.rec("bc_interpy_expr", phi)
+    C.case("bc_interpy_expr", bc_interpy)
+
+    def bc_divz():
+        st = db.div("SSurfZ", "SVol")(C.inp("SSurfZ", 2))
+        pts, cf = st.pts, st.coefs
+        phi = copy_of("SSurfZ", C.inp("SSurfZ", 2))
+        O.bc_apply(phi, O.field_values(c), plane(2, n[2] - 1), O.bc_geometry(pts, cf, "SSurfZ", "SVol", False))
+        O.bc_apply(phi, lambda x, y, z: 1.25, plane(2, 0), O.bc_geometry(pts, cf, "SSurfZ", "SVol", True))
+        C.rec("bc_divz_faces", phi)
+    C.case("bc_divz_faces", bc_divz)
+
+    def bc_fd():
+        pts, cf = stencil(db.fd("grad", 0))
+        phi = copy_of("SVol", c)
+        O.bc_apply(phi, O.field_values(a), plane(0, 0), O.bc_geometry(pts, cf, "SVol", "SVol", True, (1, 0, 0)))
+        O.bc_apply(phi, evaluated("SVol", b * 2.0), plane(0, n[0] - 1),
+                   O.bc_geometry(pts, cf, "SVol", "SVol", False, (1, 0, 0)))
+        C.rec("bc_fd_gradx", phi)
+    C.case("bc_fd_gradx", bc_fd)
     return C.records

@@ -134,6 +134,23 @@ struct CatalogCtx {
     return f;
   }
 
+  std::vector<IntVec> plane_points(int axis, int i) const {
+    std::vector<IntVec> pts;
+    const int a1 = (axis + 1) % 3, a2 = (axis + 2) % 3;
+    for (int v = 0; v < d.n[a2]; ++v)
+      for (int u = 0; u < d.n[a1]; ++u) {
+        int q[3];
+        q[axis] = i;
+        q[a1] = u;
+        q[a2] = v;
+        pts.push_back(IntVec(q[0], q[1], q[2]));
+      }
+    return pts;
+  }
+  template <typename F> SpatialMask<F> plane_mask(int axis, int i) {
+    F proto = make<F>();
+    return SpatialMask<F>(proto, plane_points(axis, i));
+  }
   template <typename F> SpatialMask<F> mask(int k) {
     std::vector<int> p = catalog::mask_points(k, domain_id, d.n, d.ghost);
     std::vector<IntVec> pts;

@@ -317,6 +317,56 @@ def masked_assign(points, lhs: Field, expr):
     return lhs
 
 
+def bc_geometry(pts, coefs, phi_loc, gamma_loc, minus, fd_dir=None):
+    """NeboBoundaryConditionBuilder's geometry (spatialops/NeboStencilBuilder.h:503-526,584-640)
+    for a stencil with points `pts` / coefficients `coefs` in listed order (first listed = Low,
+    last listed = High):
+      minus: gamma point -Low, phi points pts[1:] - Low with coefs[1:], divisor coefs[0];
+      plus:  gamma point -High, phi points pts[:-1] - High with coefs[:-1], divisor coefs[-1];
+      mask shift: for two location types, minus = (gamma offset < phi offset) per axis and
+      plus = -(gamma offset > phi offset); for one type (FD) +-the stencil direction.
+    Returns (shift, gamma_point, phi_points, phi_coefs, divisor)."""
+    sub = lambda p, q: tuple(p[i] - q[i] for i in range(3))
+    if minus:
+        piv, gpt, rest, rc, div = pts[0], None, pts[1:], coefs[1:], coefs[0]
+    else:
+        piv, gpt, rest, rc, div = pts[-1], None, pts[:-1], coefs[:-1], coefs[-1]
+    gpt = tuple(-v for v in piv)
+    if phi_loc == gamma_loc:
+        shift = tuple(fd_dir) if minus else tuple(-v for v in fd_dir)
+    else:
+        go, po = OFFSET[gamma_loc], OFFSET[phi_loc]
+        shift = tuple(1 if go[i] < po[i] else 0 for i in range(3)) if minus else \
+            tuple(-(1 if go[i] > po[i] else 0) for i in range(3))
+    return shift, gpt, [sub(q, piv) for q in rest], list(rc), div
+
+
+def bc_apply(phi: Field, gamma_value, points, geometry):
+    """The reference's serial BC point loop (NeboBoundaryConditionBuilder::cpu_apply,
+    spatialops/NeboStencilBuilder.h:641-678): for every mask point m, p = m - shift and
+      phi[p] = (1.0 * gamma[p + gamma_point] - fold_q c_q phi[p + q]) / divisor
+    with the stencil fold of NeboStencils.h:415-440 (first point first), in IEEE double, in
+    point order.  gamma_value(x, y, z) returns the gamma expression at a gamma-field index."""
+    shift, gpt, qs, cs, div = geometry
+    g = phi.ghost
+    at = lambda x, y, z: (z + g, y + g, x + g)
+    for m in points:
+        p = tuple(int(m[i]) - shift[i] for i in range(3))
+        s = None
+        for q, c in zip(qs, cs):
+            term = float(c) * float(phi.data[at(p[0] + q[0], p[1] + q[1], p[2] + q[2])])
+            s = term if s is None else s + term
+        gv = 1.0 * float(gamma_value(p[0] + gpt[0], p[1] + gpt[1], p[2] + gpt[2]))
+        phi.data[at(*p)] = (gv - s) / float(div)
+    return phi
+
+
+def field_values(f: Field):
+    """Callable (x, y, z) -> f at that interior-relative index (ghosts included)."""
+    g = f.ghost
+    return lambda x, y, z: f.data[z + g, y + g, x + g]
+
+
 RED = {"sum": 0, "max": 1, "min": 2, "norm": 3}
 
 
