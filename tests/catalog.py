@@ -255,7 +255,7 @@ def run_catalog(domain):
         pts, cf = stencil(db.interp("SVol", "SSurfY"))
         phi = copy_of("SVol", b)
         gy = C.inp("SSurfY", 1)
-        O.bc_apply(phi, evaluated("SSurfY", O.sin(gy) * 2.0 + 1.0), plane(1, 0),
+        O.bc_apply(phi, evaluated("SSurfY", gy * gy * 2.0 + 1.0), plane(1, 0),
                    O.bc_geometry(pts, cf, "SVol", "SSurfY", True))
         O.bc_apply(phi, evaluated("SSurfY", gy - 0.5), plane(1, n[1]),
                    O.bc_geometry(pts, cf, "SVol", "SSurfY", False))
