@@ -4,6 +4,7 @@
 #ifndef SpatialOps_Nebo_h
 #define SpatialOps_Nebo_h
 
+#include <spatialops/NeboApplyPointwise.h>
 #include <spatialops/NeboAssignment.h>
 #include <spatialops/NeboBasic.h>
 #include <spatialops/NeboCore.h>

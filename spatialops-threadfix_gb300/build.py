@@ -58,7 +58,8 @@ TESTS_CPP = os.path.join(REPO, "tests", "cpp")
 TESTS_BUILD = os.path.join(TESTS_CPP, "_build")
 # C++ programs written against the drop-in headers (include/spatialops): name -> (source, flags)
 PROGRAMS = {
-    "catalog_gpu_exact": ("catalog_gpu.cu", ["-DNEBO_EXACT_ARITHMETIC"]),
+    # exact: no contraction anywhere, user functors (apply_pointwise) included
+    "catalog_gpu_exact": ("catalog_gpu.cu", ["-DNEBO_EXACT_ARITHMETIC", "--fmad=false"]),
     "catalog_gpu_fast": ("catalog_gpu.cu", []),
 }
 

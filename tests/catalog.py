@@ -215,6 +215,34 @@ def run_catalog(domain):
         C.val("red_x_max_interior", O.reduce("max", xb, interior=True))
     C.case("red_xvol", red_x)
 
+    # apply_pointwise: the operands evaluated by the oracle, the functor in IEEE double (numpy,
+    # element-wise, no contraction) over the write region the operands' ghosts allow
+    def apply_case(name, fn, ops):
+        def body():
+            out = C.fresh("SVol")
+            lim, ok = O.write_limits(out, sum(o for o in ops if not isinstance(o, float)))
+            if not ok:
+                raise O.NeboError("write limits")
+            vals = []
+            for o in ops:
+                if isinstance(o, float):
+                    vals.append(o)
+                    continue
+                f = C.fresh("SVol")
+                O.assign(f, o)
+                vals.append(f.data)
+            g = out.ghost
+            sl = tuple(slice(lim[2 * i] + g, lim[2 * i + 1] + g) for i in (2, 1, 0))
+            args = [v if isinstance(v, float) else v[sl] for v in vals]
+            out.data[sl] = fn(*args)
+            C.rec(name, out)
+        C.case(name, body)
+
+    apply_case("s_apply_sum4", lambda i1, i2, i3, i4: i1 + i2 + i3 + i4, [a + b, c, 5.0, 6.0])
+    apply_case("s_apply_quad", lambda v: v * v - 3.0, [a * b])
+    apply_case("s_apply_mix7_stencil", lambda a_, b_, c_, d_, e_, f_, g_: (a_ * b_ - c_) / (d_ + 2.5) + e_ * f_ - g_,
+               [a, b, c, db.fd("grad", 0)(a), 1.5, b * c, a - 1.0])
+
     # boundary conditions (NeboBoundaryConditionBuilder over whole boundary planes)
     n = C.n
 
