@@ -199,13 +199,34 @@ __host__ __device__ __forceinline__ float f32_trunc(double v) {
   const uint32_t f = sign | ((uint32_t)(e - 896) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu);
   return from_fbits(e > 896 ? f : sign);
 }
-// A float as a double (subnormal floats give +-0).
+// A float as a double, exactly (subnormals, zeros, infinities and NaNs included).
 __host__ __device__ __forceinline__ double f32_to_f64(float f) {
   const uint32_t b = (uint32_t)fbits(f);
-  const uint32_t e = (b >> 23) & 0xff;
-  const uint64_t d = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
-  return from_bits(e ? d : (uint64_t)(b & 0x80000000u) << 32);
+  const uint32_t e = (b >> 23) & 0xff, m = b & 0x7fffffu;
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  const uint64_t normal = ((uint64_t)(e + 896) << 52) | ((uint64_t)m << 29);
+  const uint64_t special = (0x7ffULL << 52) | ((uint64_t)m << 29);  // inf / NaN
+  const int p = 31 - clz32(m);                                     // subnormal: m * 2^-149
+  const uint64_t sub = m ? (((uint64_t)(874 + p) << 52) | (((uint64_t)m << (52 - p)) & 0xfffffffffffffULL)) : 0;
+  return from_bits(sign | (e == 0 ? sub : (e == 0xff ? special : normal)));
 }
+// A double rounded to the nearest float, ties to even (the hardware's cvt.rn.f32.f64 for every
+// result in the normal float range; results below 2^-126 in magnitude give +-0).
+__host__ __device__ __forceinline__ float f64_to_f32_rn(double v) {
+  const uint64_t b = bits(v);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xfffffffffffffULL;
+  const uint32_t f = (uint32_t)(m >> 29);
+  const uint32_t rem = (uint32_t)(m & 0x1fffffffu);
+  const uint32_t up = (rem > 0x10000000u) || (rem == 0x10000000u && (f & 1u));
+  uint32_t out = ((uint32_t)(e - 896) << 23) + f + up;  // a carry moves into the exponent
+  if (e <= 896) out = 0;
+  if (e >= 1151) out = 0x7f800000u;                      // overflow to infinity
+  if (e == 2047 && m) out = 0x7fc00000u;                 // NaN
+  return from_fbits(sign | out);
+}
+
 // k (|k| < 2^31) as a double.
 __host__ __device__ __forceinline__ double i32_to_f64(int k) {
   const uint32_t a = k < 0 ? 0u - (uint32_t)k : (uint32_t)k;

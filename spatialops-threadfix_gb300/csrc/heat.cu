@@ -161,109 +161,150 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
 
 
 // FP32 heat step with an asynchronous plane pipeline.  FP32 arithmetic is nearly free on this
-// GPU, so the kernel is bound by how many bytes it keeps in flight: each block streams planes
-// of T and lambda (its 32x8 tile plus a one-cell halo) into a ring of NS shared-memory stages
-// with cp.async, up to NS-3 planes ahead of the plane it computes, using no registers for the
-// loads in flight.  Each thread then evaluates its cell's six face fluxes straight from shared
-// memory (recomputing a shared face costs three FP32 operations, cheaper than exchanging it).
+// GPU, so the kernel is bound by instruction issue and by the bytes it keeps in flight: each block
+// streams planes of T and lambda (its 32x16 tile plus a one-cell halo) into a ring of NS shared-
+// memory stages with cp.async, using no registers for the loads in flight, and each thread owns
+// two y-adjacent cells, so the face between them is computed once and the per-plane overhead
+// (ring bookkeeping, barrier, copies) is shared by two cells.  When the window's row pitch is
+// even (VEC), the halo rows are copied as 8-byte chunks (17 per row) instead of 34 floats.
 //
 // Ring schedule: the prologue issues planes z0-1 .. z0+NS-3 (one commit group each); iteration z
 // waits until at most NS-4 groups are pending (so planes up to z+1 have landed), syncs the block,
 // issues plane z+NS-2 into the stage of plane z-2 (last read in iteration z-1, before the sync),
 // then computes from the stages of planes z-1, z, z+1.
-constexpr int NS = 8;              // pipeline stages (planes resident or in flight)
-constexpr int HX = BX + 2, HY = BY + 2;
+constexpr int NS = 6;              // pipeline stages (planes resident or in flight)
+constexpr int FTY = 16;            // tile y: two cells per thread of the 32 x 8 block
+constexpr int HX = BX + 2, HY = FTY + 2;
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
-               : "memory");
-}
 __device__ __forceinline__ void cp_async4_s(uint32_t smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8_s(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-__global__ void __launch_bounds__(BX* BY, 8) heat_step_f32_async_kernel(const float* __restrict__ tin,
+template <bool VEC>
+__global__ void __launch_bounds__(BX* BY, 4) heat_step_f32_async_kernel(const float* __restrict__ tin,
                                                                       float* __restrict__ tout,
                                                                       const float* __restrict__ lam, int sy, long sz,
                                                                       int nx, int ny, int nz, int zchunk, float w0,
                                                                       float w1, float w2) {
-  constexpr int PLANE = HX * HY;                            // floats per stage and field
-  constexpr int NCOPY = (PLANE + BX * BY - 1) / (BX * BY);  // copy slots per thread
+  constexpr int PLANE = HX * HY;                                // floats per stage and field
+  constexpr int UNITS = VEC ? (HX / 2) * HY : PLANE;            // copies per plane and field
+  constexpr int NCOPY = (UNITS + BX * BY - 1) / (BX * BY);      // copy slots per thread
   __shared__ __align__(16) float sT[NS * PLANE];
   __shared__ __align__(16) float sL[NS * PLANE];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
-  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * FTY;
   const int z0 = blockIdx.z * zchunk;
   const int z1 = min(z0 + zchunk, nz);
-  // this thread's copy slots: tile cell k = tid + j*BX*BY of the (HY x HX) halo tile; cells past
-  // the +ghost column/row clamp to it (they exist and are never used)
+  // copy slots: unit k of the (HY x HX) halo tile (VEC: 8-byte pairs of columns); units past the
+  // +ghost column/row clamp to it (they exist and are never used; VEC keeps pairs aligned since
+  // nx is even when the pitch is)
   int goff[NCOPY];  // within a plane (a plane holds fewer than 2^31 cells)
   uint32_t soff[NCOPY];
 #pragma unroll
   for (int j = 0; j < NCOPY; ++j) {
-    const int k = min(tid + j * BX * BY, PLANE - 1);
-    const int r = k / HX, c = k - r * HX;
-    goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
-    soff[j] = (uint32_t)(k * sizeof(float));
-  }
-  const uint32_t sT0 = (uint32_t)__cvta_generic_to_shared(sT), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
-  auto issue = [&](int p) {  // plane p (interior z index, -1..nz) into stage p % NS
-    if (p > z1) return;
-    const uint32_t st = (uint32_t)((p + NS) % NS) * (PLANE * sizeof(float));
-    const float* tp = tin + sz * p;
-    const float* lp = lam + sz * p;
-#pragma unroll
-    for (int j = 0; j < NCOPY; ++j) {
-      if (j == NCOPY - 1 && tid + j * BX * BY >= PLANE) break;
-      cp_async4_s(sT0 + st + soff[j], tp + goff[j]);
-      cp_async4_s(sL0 + st + soff[j], lp + goff[j]);
+    const int k = min(tid + j * BX * BY, UNITS - 1);
+    if (VEC) {
+      const int r = k / (HX / 2), c = 2 * (k - r * (HX / 2));
+      goff[j] = min(x0 - 1 + c, nx - 1) + sy * min(y0 - 1 + r, ny);
+      soff[j] = (uint32_t)((r * HX + c) * sizeof(float));
+    } else {
+      const int r = k / HX, c = k - r * HX;
+      goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
+      soff[j] = (uint32_t)(k * sizeof(float));
     }
+  }
+  const bool last_slot = tid + (NCOPY - 1) * BX * BY < UNITS;
+  const uint32_t sT0 = (uint32_t)__cvta_generic_to_shared(sT), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
+  int ist = (z0 - 1 + NS) % NS;  // stage of the next plane to issue
+  int ip = z0 - 1;               // next plane to issue
+  auto issue = [&]() {           // plane ip into stage ist
+    if (ip <= z1) {
+      const uint32_t st = (uint32_t)ist * (PLANE * sizeof(float));
+      const float* tp = tin + sz * ip;
+      const float* lp = lam + sz * ip;
+#pragma unroll
+      for (int j = 0; j < NCOPY; ++j) {
+        if (j == NCOPY - 1 && !last_slot) break;
+        if (VEC) {
+          cp_async8_s(sT0 + st + soff[j], tp + goff[j]);
+          cp_async8_s(sL0 + st + soff[j], lp + goff[j]);
+        } else {
+          cp_async4_s(sT0 + st + soff[j], tp + goff[j]);
+          cp_async4_s(sL0 + st + soff[j], lp + goff[j]);
+        }
+      }
+    }
+    ++ip;
+    ist = ist + 1 == NS ? 0 : ist + 1;
   };
 #pragma unroll 1
   for (int i = 0; i < NS - 1; ++i) {
-    issue(z0 - 1 + i);
+    issue();
     cp_async_commit();
   }
-  const int x = x0 + tx, y = y0 + ty;
-  const bool active = x < nx && y < ny;
-  const bool edge_xy = x == 0 || x == nx - 1 || y == 0 || y == ny - 1;
-  const int ci = (ty + 1) * HX + tx + 1;  // this cell in a stage
-  float tc = 0.f, lc = 0.f, fzl = 0.f;
-  float* out = tout + (long)x + (long)sy * y + sz * z0;
+  const int x = x0 + tx, ya = y0 + 2 * ty, yb = ya + 1;
+  const bool acta = x < nx && ya < ny, actb = x < nx && yb < ny;
+  const bool edgea = x == 0 || x == nx - 1 || ya == 0 || ya == ny - 1;
+  const bool edgeb = x == 0 || x == nx - 1 || yb == 0 || yb == ny - 1;
+  const int ca = (2 * ty + 1) * HX + tx + 1;  // cell a in a stage; cell b is ca + HX
+  float ta = 0.f, la = 0.f, tb = 0.f, lb = 0.f, fza = 0.f, fzb = 0.f;
+  float* outa = tout + (long)x + (long)sy * ya + sz * z0;
+  int cur = (z0 + NS) % NS;  // stage of plane z
 #pragma unroll 1
-  for (int z = z0; z < z1; ++z, out += sz) {
+  for (int z = z0; z < z1; ++z, outa += sz) {
     cp_async_wait<NS - 4>();  // planes up to z+1 have landed (this thread's copies)
     __syncthreads();          // ... and everyone's; plane z-2's stage is no longer read
-    issue(z + NS - 2);
+    issue();                  // plane z+NS-2
     cp_async_commit();
-    const float* T0 = sT + ((z + NS) % NS) * PLANE;
-    const float* L0 = sL + ((z + NS) % NS) * PLANE;
-    const float* Tp = sT + ((z + 1) % NS) * PLANE;
-    const float* Lp = sL + ((z + 1) % NS) * PLANE;
-    if (z == z0) {  // first plane of the chunk: centre and low z face from the stages
-      const float* Tm = sT + ((z - 1 + NS) % NS) * PLANE;
-      const float* Lm = sL + ((z - 1 + NS) % NS) * PLANE;
-      tc = T0[ci];
-      lc = L0[ci];
-      fzl = (Lm[ci] + lc) * (tc - Tm[ci]);
+    const int nxt = cur + 1 == NS ? 0 : cur + 1;
+    const float* T0 = sT + cur * PLANE;
+    const float* L0 = sL + cur * PLANE;
+    if (z == z0) {  // first plane of the chunk: centres and low z faces from the stages
+      const int prv = cur == 0 ? NS - 1 : cur - 1;
+      const float* Tm = sT + prv * PLANE;
+      const float* Lm = sL + prv * PLANE;
+      ta = T0[ca];
+      la = L0[ca];
+      tb = T0[ca + HX];
+      lb = L0[ca + HX];
+      fza = (Lm[ca] + la) * (ta - Tm[ca]);
+      fzb = (Lm[ca + HX] + lb) * (tb - Tm[ca + HX]);
     }
-    const float tn = Tp[ci], ln = Lp[ci];
-    const float fzh = (lc + ln) * (tn - tc);
-    if (active) {
-      const float fxl = (L0[ci - 1] + lc) * (tc - T0[ci - 1]);
-      const float fxh = (lc + L0[ci + 1]) * (T0[ci + 1] - tc);
-      const float fyl = (L0[ci - HX] + lc) * (tc - T0[ci - HX]);
-      const float fyh = (lc + L0[ci + HX]) * (T0[ci + HX] - tc);
-      const float v = tc + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fzl);
-      *out = v;
-      if (edge_xy || z == 0 || z == nz - 1) store_images_only(tout, sy, sz, x, y, z, nx, ny, nz, v);
+    const float* Tn = sT + nxt * PLANE;
+    const float* Ln = sL + nxt * PLANE;
+    const float tna = Tn[ca], lna = Ln[ca], tnb = Tn[ca + HX], lnb = Ln[ca + HX];
+    const float fzha = (la + lna) * (tna - ta), fzhb = (lb + lnb) * (tnb - tb);
+    const float fy0 = (L0[ca - HX] + la) * (ta - T0[ca - HX]);
+    const float fy1 = (la + lb) * (tb - ta);  // the face between the two cells
+    const float fy2 = (lb + L0[ca + 2 * HX]) * (T0[ca + 2 * HX] - tb);
+    const float fxla = (L0[ca - 1] + la) * (ta - T0[ca - 1]);
+    const float fxha = (la + L0[ca + 1]) * (T0[ca + 1] - ta);
+    const float fxlb = (L0[ca + HX - 1] + lb) * (tb - T0[ca + HX - 1]);
+    const float fxhb = (lb + L0[ca + HX + 1]) * (T0[ca + HX + 1] - tb);
+    const float va = ta + w0 * (fxha - fxla) + w1 * (fy1 - fy0) + w2 * (fzha - fza);
+    const float vb = tb + w0 * (fxhb - fxlb) + w1 * (fy2 - fy1) + w2 * (fzhb - fzb);
+    const bool zedge = z == 0 || z == nz - 1;
+    if (acta) {
+      *outa = va;
+      if (edgea || zedge) store_images_only(tout, sy, sz, x, ya, z, nx, ny, nz, va);
     }
-    tc = tn;
-    lc = ln;
-    fzl = fzh;
+    if (actb) {
+      outa[sy] = vb;
+      if (edgeb || zedge) store_images_only(tout, sy, sz, x, yb, z, nx, ny, nz, vb);
+    }
+    ta = tna;
+    la = lna;
+    tb = tnb;
+    lb = lnb;
+    fza = fzha;
+    fzb = fzhb;
+    cur = nxt;
   }
   cp_async_wait<0>();
 }
@@ -309,21 +350,32 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
       heat_step_kernel<double, ExactD, MODE_REFERENCE><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                               vin.sz, n[0], n[1], n[2], zchunk, p);
   } else {
+    // 8-byte copies when every row of T and lambda starts 8-byte aligned (even pitch, aligned
+    // windows); then nx is even too, which keeps the clamped column pairs aligned
+    const bool vec = (vin.sy % 2 == 0) && ((uintptr_t)(vin.base - 1) % 8 == 0) && ((uintptr_t)(vl.base - 1) % 8 == 0);
     // one full wave: as many z chunks as the resident blocks allow (each chunk re-reads two
     // halo planes and fills the ring once, so more chunks than slots only cost)
-    static int per_sm = 0;
-    if (!per_sm) {
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat_step_f32_async_kernel, BX * BY, 0) !=
-              cudaSuccess ||
-          per_sm < 1)
-        per_sm = 1;
+    static int per_sm[2] = {0, 0};
+    if (!per_sm[vec]) {
+      int v = 0;
+      const cudaError_t e =
+          vec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<true>, BX * BY, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<false>, BX * BY, 0);
+      per_sm[vec] = (e == cudaSuccess && v > 0) ? v : 1;
     }
-    int ch = max(1, min(num_sms() * per_sm / (gxb * gyb), (n[2] + 7) / 8));
+    const int fyb = (n[1] + FTY - 1) / FTY;
+    int ch = max(1, min(num_sms() * per_sm[vec] / (gxb * fyb), (n[2] + 7) / 8));
     const int zc = (n[2] + ch - 1) / ch;
     ch = (n[2] + zc - 1) / zc;
     LaunchScope ls("heat_step_f32", s);
-    heat_step_f32_async_kernel<<<dim3(gxb, gyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz, n[0],
-                                                                    n[1], n[2], zc, p.w[0], p.w[1], p.w[2]);
+    if (vec)
+      heat_step_f32_async_kernel<true><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
+                                                                            vin.sz, n[0], n[1], n[2], zc, p.w[0],
+                                                                            p.w[1], p.w[2]);
+    else
+      heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
+                                                                             vin.sz, n[0], n[1], n[2], zc, p.w[0],
+                                                                             p.w[1], p.w[2]);
   }
   NEBO_LAUNCH_CHECK("nebo_heat_step");
   return NEBO_OK;

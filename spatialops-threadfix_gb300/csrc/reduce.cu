@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "fp64_int.cuh"
 #include "reduce4.cuh"
 
 namespace nebo {
@@ -75,6 +76,11 @@ __device__ Acc block_reduce(Acc a, int op) {
   return a;
 }
 
+// FP32 elements widen exactly through integer operations (a hardware f32 -> f64 conversion issues
+// on the FP64 pipe, which the accumulation itself needs).
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return fixmath::f32_to_f64(v); }
+
 // Every element of the region's rows, a warp per row (rows strided over all warps of the grid),
 // each lane issuing 8 independent loads before it uses them; f8(v[8]) gets each full batch of 8
 // (lanes 32 apart), f1(v) each element of the row tails.
@@ -90,10 +96,10 @@ __device__ __forceinline__ void walk_rows(const T* __restrict__ base, int sy, lo
     for (; x + 7 * 32 < x1; x += 8 * 32) {
       double v[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = (double)__ldg(row + x + 32 * i);
+      for (int i = 0; i < 8; ++i) v[i] = widen(__ldg(row + x + 32 * i));
       f8(v);
     }
-    for (; x < x1; x += 32) f1((double)__ldg(row + x));
+    for (; x < x1; x += 32) f1(widen(__ldg(row + x)));
   }
 }
 

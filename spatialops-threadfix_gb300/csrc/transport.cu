@@ -16,6 +16,7 @@
 // faces through shared memory or carried in z), RK combination fused, periodic ghost images of
 // the stencil copy written in the same pass.
 #include "common.cuh"
+#include "fp64_int.cuh"
 
 namespace nebo {
 namespace {
@@ -121,16 +122,22 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, in
     __syncthreads();
     if (active) {
       const T rhs = ((sfx[buf][ty][tx + 1] - fx) + (sfy[buf][ty + 1][tx] - fy)) + (fzhi - fzlo);
+      // FP32 mode: the float <-> double conversions from the bits (a hardware conversion issues
+      // on the FP64 pipe, at the FP64 rate)
+      double rd;
+      if constexpr (sizeof(T) == 4) rd = fixmath::f32_to_f64(rhs); else rd = rhs;
       double r;
       if (!SECOND)
-        r = a.acc[c] + a.dt * (double)rhs;
+        r = a.acc[c] + a.dt * rd;
       else
-        r = 0.5 * a.base[c] + 0.5 * (a.acc[c] + a.dt * (double)rhs);
+        r = 0.5 * a.base[c] + 0.5 * (a.acc[c] + a.dt * rd);
+      T rs;
+      if constexpr (sizeof(T) == 4) rs = fixmath::f64_to_f32_rn(r); else rs = r;
       if (a.outS) {
         a.out64[c] = r;
-        store_images2(a.outS, sy, sz, x, y, z, n, (T)r);
+        store_images2(a.outS, sy, sz, x, y, z, n, rs);
       } else {
-        store_images2(reinterpret_cast<T*>(a.out64), sy, sz, x, y, z, n, (T)r);
+        store_images2(reinterpret_cast<T*>(a.out64), sy, sz, x, y, z, n, rs);
       }
     }
     fzlo = fzhi;
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, in
 
 __global__ void cast_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+    b[i] = fixmath::f64_to_f32_rn(a[i]);
 }
 
 int cast_f64_to_f32(const double* a, float* b, size_t n, cudaStream_t s) {

@@ -3,6 +3,7 @@
 // Prints one line per range: "<name> <max ulp> <worst x>".
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <random>
 
 #include "../../spatialops-threadfix_gb300/csrc/fp64_int.cuh"
@@ -48,5 +49,31 @@ int main(int argc, char** argv) {
     }
   }
   std::printf("sin_near_jpi %.4f %.17g\n", mx, worst);
+  // conversions built from the bits: against the C casts on random bit patterns and edge values
+  long bad_d2f = 0, bad_f2d = 0;
+  std::uniform_int_distribution<uint64_t> bits64;
+  for (long i = 0; i < 4 * n; ++i) {
+    const uint64_t b = bits64(g);
+    double v;
+    std::memcpy(&v, &b, 8);
+    const double av = std::fabs(v);
+    if (std::isnan(v) || (av >= 1.1754943508222875e-38 && av < 3.4028234663852886e38) || av == 0.0) {
+      const float want = (float)v, got = f64_to_f32_rn(v);
+      if (std::memcmp(&want, &got, 4) != 0 && !(std::isnan(want) && std::isnan(got))) ++bad_d2f;
+    }
+    const uint32_t fb = (uint32_t)b;
+    float f;
+    std::memcpy(&f, &fb, 4);
+    const double wd = (double)f, gd = f32_to_f64(f);
+    if (std::memcmp(&wd, &gd, 8) != 0 && !(std::isnan(wd) && std::isnan(gd))) ++bad_f2d;
+  }
+  for (uint32_t fb : {0u, 0x80000000u, 1u, 0x80000001u, 0x007fffffu, 0x00400000u, 0x00800000u, 0x7f7fffffu,
+                      0x7f800000u, 0xff800000u, 0x7fc00000u}) {
+    float f;
+    std::memcpy(&f, &fb, 4);
+    const double wd = (double)f, gd = f32_to_f64(f);
+    if (std::memcmp(&wd, &gd, 8) != 0 && !(std::isnan(wd) && std::isnan(gd))) ++bad_f2d;
+  }
+  std::printf("conv_d2f_mismatch %ld 0\nconv_f2d_mismatch %ld 0\n", bad_d2f, bad_f2d);
   return 0;
 }

@@ -30,6 +30,11 @@ def results(tmp_path_factory):
     return {ln.split()[0]: float(ln.split()[1]) for ln in out.splitlines() if ln.strip()}
 
 
+@pytest.mark.parametrize("name", ["conv_d2f_mismatch", "conv_f2d_mismatch"])
+def test_bit_built_conversions_match_casts(results, name):
+    assert results[name] == 0, (name, results[name])
+
+
 @pytest.mark.parametrize("name", ["exp_unit", "exp_full", "exp_tiny", "sin_unit", "sin_100", "sin_1e5", "sin_tiny",
                                   "sin_2p20", "sin_near_jpi"])
 def test_error_bound(results, name):

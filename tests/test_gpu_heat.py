@@ -50,8 +50,8 @@ def test_heat_graph_equals_stream_launches():
     assert (_bits(a) == _bits(b)).all()
 
 
-def test_heat_fp32_error_vs_fp64_oracle():
-    n = (64, 48, 40)
+@pytest.mark.parametrize("n", [(64, 48, 40), (37, 21, 19)])  # even pitch (8-byte copies), odd pitch
+def test_heat_fp32_error_vs_fp64_oracle(n):
     lam, T0, dt = W.heat_inputs(n, cfl=0.15)  # a stable step, so the error measure is meaningful
     ref = O.heat_run(lam, T0, n, 50, dt)
     T = _run(lam, T0, 50, dt, dtype="f32").numpy().astype(np.float64)
