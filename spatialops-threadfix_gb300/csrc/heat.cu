@@ -162,18 +162,22 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
 
 // FP32 heat step with an asynchronous plane pipeline.  FP32 arithmetic is nearly free on this
 // GPU, so the kernel is bound by instruction issue and by the bytes it keeps in flight: each block
-// streams planes of T and lambda (its 32x16 tile plus a one-cell halo) into a ring of NS shared-
-// memory stages with cp.async, using no registers for the loads in flight, and each thread owns
-// two y-adjacent cells, so the face between them is computed once and the per-plane overhead
-// (ring bookkeeping, barrier, copies) is shared by two cells.  When the window's row pitch is
-// even (VEC), the halo rows are copied as 8-byte chunks (17 per row) instead of 34 floats.
+// streams planes of T and lambda (its 32x32 tile plus a one-cell halo) into a ring of NS shared-
+// memory stages with cp.async, using no registers for the loads in flight, and each thread owns a
+// column of four y-adjacent cells, so three of its five y faces are interior to it and the per-plane
+// overhead (barrier, copies) is shared by four cells.  z chunks are multiples of NS and the z loop is
+// unrolled by NS, so every stage index and shared-memory offset is a compile-time constant.  When
+// the window's row pitch is even (VEC), halo rows are copied as 8-byte chunks (17 per row).
 //
-// Ring schedule: the prologue issues planes z0-1 .. z0+NS-3 (one commit group each); iteration z
+// Ring schedule: plane p (z0-1 <= p <= z1) lives in stage (p - z0 + NS) % NS.  Before the loop,
+// planes z0-1 .. z0+NS-3 are issued (one commit group each) and the first two awaited; iteration z
 // waits until at most NS-4 groups are pending (so planes up to z+1 have landed), syncs the block,
 // issues plane z+NS-2 into the stage of plane z-2 (last read in iteration z-1, before the sync),
-// then computes from the stages of planes z-1, z, z+1.
-constexpr int NS = 6;              // pipeline stages (planes resident or in flight)
-constexpr int FTY = 16;            // tile y: two cells per thread of the 32 x 8 block
+// then computes from the stages of planes z and z+1 (plane z-1 enters only through the z faces
+// carried in registers).
+constexpr int NS = 5;              // pipeline stages (planes resident or in flight)
+constexpr int FTY = 32;            // tile y: a column of CPT cells per thread of the 32 x 8 block
+constexpr int CPT = FTY / BY;
 constexpr int HX = BX + 2, HY = FTY + 2;
 
 __device__ __forceinline__ void cp_async4_s(uint32_t smem, const void* gmem) {
@@ -187,7 +191,7 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 template <bool VEC>
-__global__ void __launch_bounds__(BX* BY, 4) heat_step_f32_async_kernel(const float* __restrict__ tin,
+__global__ void __launch_bounds__(BX* BY, 3) heat_step_f32_async_kernel(const float* __restrict__ tin,
                                                                       float* __restrict__ tout,
                                                                       const float* __restrict__ lam, int sy, long sz,
                                                                       int nx, int ny, int nz, int zchunk, float w0,
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(BX* BY, 4) heat_step_f32_async_kernel(const fl
   __shared__ __align__(16) float sL[NS * PLANE];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
   const int x0 = blockIdx.x * BX, y0 = blockIdx.y * FTY;
-  const int z0 = blockIdx.z * zchunk;
+  const int z0 = blockIdx.z * zchunk;  // a multiple of NS
   const int z1 = min(z0 + zchunk, nz);
   // copy slots: unit k of the (HY x HX) halo tile (VEC: 8-byte pairs of columns); units past the
   // +ghost column/row clamp to it (they exist and are never used; VEC keeps pairs aligned since
@@ -221,90 +225,97 @@ __global__ void __launch_bounds__(BX* BY, 4) heat_step_f32_async_kernel(const fl
   }
   const bool last_slot = tid + (NCOPY - 1) * BX * BY < UNITS;
   const uint32_t sT0 = (uint32_t)__cvta_generic_to_shared(sT), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
-  int ist = (z0 - 1 + NS) % NS;  // stage of the next plane to issue
-  int ip = z0 - 1;               // next plane to issue
-  auto issue = [&]() {           // plane ip into stage ist
-    if (ip <= z1) {
-      const uint32_t st = (uint32_t)ist * (PLANE * sizeof(float));
-      const float* tp = tin + sz * ip;
-      const float* lp = lam + sz * ip;
+  // plane p into stage st (a constant wherever the z loop below is unrolled)
+  auto issue = [&](int p, int st) {
+    if (p <= z1) {
+      const uint32_t so = (uint32_t)st * (PLANE * sizeof(float));
+      const float* tp = tin + sz * p;
+      const float* lp = lam + sz * p;
 #pragma unroll
       for (int j = 0; j < NCOPY; ++j) {
         if (j == NCOPY - 1 && !last_slot) break;
         if (VEC) {
-          cp_async8_s(sT0 + st + soff[j], tp + goff[j]);
-          cp_async8_s(sL0 + st + soff[j], lp + goff[j]);
+          cp_async8_s(sT0 + so + soff[j], tp + goff[j]);
+          cp_async8_s(sL0 + so + soff[j], lp + goff[j]);
         } else {
-          cp_async4_s(sT0 + st + soff[j], tp + goff[j]);
-          cp_async4_s(sL0 + st + soff[j], lp + goff[j]);
+          cp_async4_s(sT0 + so + soff[j], tp + goff[j]);
+          cp_async4_s(sL0 + so + soff[j], lp + goff[j]);
         }
       }
     }
-    ++ip;
-    ist = ist + 1 == NS ? 0 : ist + 1;
   };
-#pragma unroll 1
-  for (int i = 0; i < NS - 1; ++i) {
-    issue();
+  issue(z0 - 1, NS - 1);
+  cp_async_commit();
+#pragma unroll
+  for (int i = 0; i < NS - 2; ++i) {
+    issue(z0 + i, i);
     cp_async_commit();
   }
-  const int x = x0 + tx, ya = y0 + 2 * ty, yb = ya + 1;
-  const bool acta = x < nx && ya < ny, actb = x < nx && yb < ny;
-  const bool edgea = x == 0 || x == nx - 1 || ya == 0 || ya == ny - 1;
-  const bool edgeb = x == 0 || x == nx - 1 || yb == 0 || yb == ny - 1;
-  const int ca = (2 * ty + 1) * HX + tx + 1;  // cell a in a stage; cell b is ca + HX
-  float ta = 0.f, la = 0.f, tb = 0.f, lb = 0.f, fza = 0.f, fzb = 0.f;
-  float* outa = tout + (long)x + (long)sy * ya + sz * z0;
-  int cur = (z0 + NS) % NS;  // stage of plane z
+  const int x = x0 + tx, yt = y0 + CPT * ty;
+  const int ci = (CPT * ty + 1) * HX + tx + 1;  // the thread's first cell in a stage
+  bool act[CPT], edge[CPT];
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    act[k] = x < nx && yt + k < ny;
+    edge[k] = x == 0 || x == nx - 1 || yt + k == 0 || yt + k == ny - 1;
+  }
+  // centres and low z faces of plane z0 (planes z0-1 and z0 landed)
+  cp_async_wait<NS - 3>();
+  __syncthreads();
+  float t[CPT], l[CPT], fz[CPT];
+  {
+    const float* Tm = sT + (NS - 1) * PLANE;
+    const float* Lm = sL + (NS - 1) * PLANE;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      t[k] = sT[ci + k * HX];
+      l[k] = sL[ci + k * HX];
+      fz[k] = (Lm[ci + k * HX] + l[k]) * (t[k] - Tm[ci + k * HX]);
+    }
+  }
+  float* out = tout + (long)x + (long)sy * yt + sz * z0;
 #pragma unroll 1
-  for (int z = z0; z < z1; ++z, outa += sz) {
-    cp_async_wait<NS - 4>();  // planes up to z+1 have landed (this thread's copies)
-    __syncthreads();          // ... and everyone's; plane z-2's stage is no longer read
-    issue();                  // plane z+NS-2
-    cp_async_commit();
-    const int nxt = cur + 1 == NS ? 0 : cur + 1;
-    const float* T0 = sT + cur * PLANE;
-    const float* L0 = sL + cur * PLANE;
-    if (z == z0) {  // first plane of the chunk: centres and low z faces from the stages
-      const int prv = cur == 0 ? NS - 1 : cur - 1;
-      const float* Tm = sT + prv * PLANE;
-      const float* Lm = sL + prv * PLANE;
-      ta = T0[ca];
-      la = L0[ca];
-      tb = T0[ca + HX];
-      lb = L0[ca + HX];
-      fza = (Lm[ca] + la) * (ta - Tm[ca]);
-      fzb = (Lm[ca + HX] + lb) * (tb - Tm[ca + HX]);
+  for (int zb = z0; zb < z1; zb += NS) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      const int z = zb + i;
+      if (z >= z1) break;
+      cp_async_wait<NS - 4>();  // planes up to z+1 have landed (this thread's copies)
+      __syncthreads();          // ... and everyone's; plane z-2's stage is no longer read
+      issue(z + NS - 2, (i + NS - 2) % NS);
+      cp_async_commit();
+      const float* T0 = sT + i * PLANE;
+      const float* L0 = sL + i * PLANE;
+      const float* Tn = sT + ((i + 1) % NS) * PLANE;
+      const float* Ln = sL + ((i + 1) % NS) * PLANE;
+      float tn[CPT], ln[CPT], fy[CPT + 1];
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        tn[k] = Tn[ci + k * HX];
+        ln[k] = Ln[ci + k * HX];
+      }
+      fy[0] = (L0[ci - HX] + l[0]) * (t[0] - T0[ci - HX]);
+#pragma unroll
+      for (int k = 1; k < CPT; ++k) fy[k] = (l[k - 1] + l[k]) * (t[k] - t[k - 1]);
+      fy[CPT] = (l[CPT - 1] + L0[ci + CPT * HX]) * (T0[ci + CPT * HX] - t[CPT - 1]);
+      const bool zedge = z == 0 || z == nz - 1;
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int c = ci + k * HX;
+        const float fxl = (L0[c - 1] + l[k]) * (t[k] - T0[c - 1]);
+        const float fxh = (l[k] + L0[c + 1]) * (T0[c + 1] - t[k]);
+        const float fzh = (l[k] + ln[k]) * (tn[k] - t[k]);
+        const float v = t[k] + w0 * (fxh - fxl) + w1 * (fy[k + 1] - fy[k]) + w2 * (fzh - fz[k]);
+        if (act[k]) {
+          out[(long)sy * k] = v;
+          if (edge[k] || zedge) store_images_only(tout, sy, sz, x, yt + k, z, nx, ny, nz, v);
+        }
+        fz[k] = fzh;
+        t[k] = tn[k];
+        l[k] = ln[k];
+      }
+      out += sz;
     }
-    const float* Tn = sT + nxt * PLANE;
-    const float* Ln = sL + nxt * PLANE;
-    const float tna = Tn[ca], lna = Ln[ca], tnb = Tn[ca + HX], lnb = Ln[ca + HX];
-    const float fzha = (la + lna) * (tna - ta), fzhb = (lb + lnb) * (tnb - tb);
-    const float fy0 = (L0[ca - HX] + la) * (ta - T0[ca - HX]);
-    const float fy1 = (la + lb) * (tb - ta);  // the face between the two cells
-    const float fy2 = (lb + L0[ca + 2 * HX]) * (T0[ca + 2 * HX] - tb);
-    const float fxla = (L0[ca - 1] + la) * (ta - T0[ca - 1]);
-    const float fxha = (la + L0[ca + 1]) * (T0[ca + 1] - ta);
-    const float fxlb = (L0[ca + HX - 1] + lb) * (tb - T0[ca + HX - 1]);
-    const float fxhb = (lb + L0[ca + HX + 1]) * (T0[ca + HX + 1] - tb);
-    const float va = ta + w0 * (fxha - fxla) + w1 * (fy1 - fy0) + w2 * (fzha - fza);
-    const float vb = tb + w0 * (fxhb - fxlb) + w1 * (fy2 - fy1) + w2 * (fzhb - fzb);
-    const bool zedge = z == 0 || z == nz - 1;
-    if (acta) {
-      *outa = va;
-      if (edgea || zedge) store_images_only(tout, sy, sz, x, ya, z, nx, ny, nz, va);
-    }
-    if (actb) {
-      outa[sy] = vb;
-      if (edgeb || zedge) store_images_only(tout, sy, sz, x, yb, z, nx, ny, nz, vb);
-    }
-    ta = tna;
-    la = lna;
-    tb = tnb;
-    lb = lnb;
-    fza = fzha;
-    fzb = fzhb;
-    cur = nxt;
   }
   cp_async_wait<0>();
 }
@@ -365,7 +376,8 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     }
     const int fyb = (n[1] + FTY - 1) / FTY;
     int ch = max(1, min(num_sms() * per_sm[vec] / (gxb * fyb), (n[2] + 7) / 8));
-    const int zc = (n[2] + ch - 1) / ch;
+    int zc = (n[2] + ch - 1) / ch;
+    zc = (zc + NS - 1) / NS * NS;  // chunks start on a multiple of NS: constant ring stages
     ch = (n[2] + zc - 1) / zc;
     LaunchScope ls("heat_step_f32", s);
     if (vec)
