@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(BX* BY) heat_step_kernel(const T* __restrict__
 // issues plane z+NS-2 into the stage of plane z-2 (last read in iteration z-1, before the sync),
 // then computes from the stages of planes z and z+1 (plane z-1 enters only through the z faces
 // carried in registers).
-constexpr int NS = 7;              // pipeline stages (planes resident or in flight)
+constexpr int NS = 5;              // pipeline stages (planes resident or in flight)
 constexpr int FTY = 32;            // tile y: a column of CPT cells per thread of the 32 x 8 block
 constexpr int CPT = FTY / BY;
 constexpr int HX = BX + 2, HY = FTY + 2;
@@ -199,9 +199,8 @@ __global__ void __launch_bounds__(BX* BY, 3) heat_step_f32_async_kernel(const fl
   constexpr int PLANE = HX * HY;                                // floats per stage and field
   constexpr int UNITS = VEC ? (HX / 2) * HY : PLANE;            // copies per plane and field
   constexpr int NCOPY = (UNITS + BX * BY - 1) / (BX * BY);      // copy slots per thread
-  extern __shared__ __align__(16) float heat_ring[];  // NS stages of T, then NS of lambda
-  float* const sT = heat_ring;
-  float* const sL = heat_ring + NS * PLANE;
+  __shared__ __align__(16) float sT[NS * PLANE];
+  __shared__ __align__(16) float sL[NS * PLANE];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
   const int x0 = blockIdx.x * BX, y0 = blockIdx.y * FTY;
   const int z0 = blockIdx.z * zchunk;  // a multiple of NS
@@ -321,39 +320,6 @@ __global__ void __launch_bounds__(BX* BY, 3) heat_step_f32_async_kernel(const fl
   cp_async_wait<0>();
 }
 
-// The FP32 ring (2 x NS planes of the halo tile) is dynamic shared memory above the 48 KB default:
-// the opt-in and the occupancy query run once per device (before any stream capture: see
-// nebo_heat_run).
-constexpr size_t HEAT32_RING_BYTES = 2 * (size_t)NS * HX * HY * sizeof(float);
-int heat32_prepare(int* dev_out, int per_sm_out[2]) {
-  static std::mutex mu;
-  static int per_sm[64][2];
-  static bool ready[64] = {false};
-  int dev = 0;
-  NEBO_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_heat_step: device index %d", dev);
-  std::lock_guard<std::mutex> g(mu);
-  if (!ready[dev]) {
-    NEBO_CUDA_TRY(cudaFuncSetAttribute(heat_step_f32_async_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)HEAT32_RING_BYTES));
-    NEBO_CUDA_TRY(cudaFuncSetAttribute(heat_step_f32_async_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)HEAT32_RING_BYTES));
-    for (int v = 0; v < 2; ++v) {
-      int b = 0;
-      const cudaError_t e = v ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, heat_step_f32_async_kernel<true>,
-                                                                              BX * BY, HEAT32_RING_BYTES)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, heat_step_f32_async_kernel<false>,
-                                                                              BX * BY, HEAT32_RING_BYTES);
-      per_sm[dev][v] = (e == cudaSuccess && b > 0) ? b : 1;
-    }
-    ready[dev] = true;
-  }
-  *dev_out = dev;
-  per_sm_out[0] = per_sm[dev][0];
-  per_sm_out[1] = per_sm[dev][1];
-  return NEBO_OK;
-}
-
 int check_heat(const nebo_field* T, const nebo_field* To, const nebo_field* L, const char* what) {
   int rc;
   if ((rc = check_field(T, what)) || (rc = check_field(To, what)) || (rc = check_field(L, what))) return rc;
@@ -400,10 +366,14 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     const bool vec = (vin.sy % 2 == 0) && ((uintptr_t)(vin.base - 1) % 8 == 0) && ((uintptr_t)(vl.base - 1) % 8 == 0);
     // one full wave: as many z chunks as the resident blocks allow (each chunk re-reads two
     // halo planes and fills the ring once, so more chunks than slots only cost)
-    int dev = 0, per_sm[2];
-    int rc = heat32_prepare(&dev, per_sm);
-    if (rc) return rc;
-    const size_t ring_bytes = HEAT32_RING_BYTES;
+    static int per_sm[2] = {0, 0};
+    if (!per_sm[vec]) {
+      int v = 0;
+      const cudaError_t e =
+          vec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<true>, BX * BY, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<false>, BX * BY, 0);
+      per_sm[vec] = (e == cudaSuccess && v > 0) ? v : 1;
+    }
     const int fyb = (n[1] + FTY - 1) / FTY;
     int ch = max(1, min(num_sms() * per_sm[vec] / (gxb * fyb), (n[2] + 7) / 8));
     int zc = (n[2] + ch - 1) / ch;
@@ -411,11 +381,11 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     ch = (n[2] + zc - 1) / zc;
     LaunchScope ls("heat_step_f32", s);
     if (vec)
-      heat_step_f32_async_kernel<true><<<dim3(gxb, fyb, ch), block, ring_bytes, s>>>(vin.base, vout.base, vl.base, vin.sy,
+      heat_step_f32_async_kernel<true><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                             vin.sz, n[0], n[1], n[2], zc, p.w[0],
                                                                             p.w[1], p.w[2]);
     else
-      heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), block, ring_bytes, s>>>(vin.base, vout.base, vl.base, vin.sy,
+      heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                              vin.sz, n[0], n[1], n[2], zc, p.w[0],
                                                                              p.w[1], p.w[2]);
   }
@@ -491,10 +461,6 @@ extern "C" int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const 
     if (it != g_graphs.end()) exec = it->second;
   }
   if (!exec) {
-    if (T->dtype == NEBO_F32) {  // per-device set-up of the FP32 kernel happens outside the capture
-      int dev, per_sm[2];
-      if ((rc = heat32_prepare(&dev, per_sm))) return rc;
-    }
     cudaStream_t cap;
     NEBO_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     NEBO_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
