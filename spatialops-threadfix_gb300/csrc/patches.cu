@@ -50,7 +50,8 @@ struct WorkItem {
 
 // Storage and arithmetic of the three precision modes.
 //   PMODE_F64   value = double, fluxes double, round-to-nearest FP64 ops (bit-exact form)
-//   PMODE_F32   value = float: FP32 storage and arithmetic (half the bytes of FP64)
+//   PMODE_F32   value = float: FP32 storage and arithmetic (half the bytes of FP64); served by
+//               patches_f32_ring_kernel below
 //   PMODE_F32X2 value = float2 (hi, lo): the state as an unevaluated sum of two floats (~48-bit
 //               significand); differences (hb-ha)+(lb-la), fluxes and the update in float, the
 //               update added with an error-free two-sum.  No FP64 operation on the sweep.
@@ -64,14 +65,6 @@ template <> struct PM<PMODE_F64> {
   static __device__ __forceinline__ F add(F a, F b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ F sub(F a, F b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ F mul(F a, F b) { return __dmul_rn(a, b); }
-};
-template <> struct PM<PMODE_F32> {
-  typedef float S;
-  typedef float F;
-  static __device__ __forceinline__ F diff(S a, S b) { return b - a; }
-  static __device__ __forceinline__ F add(F a, F b) { return a + b; }
-  static __device__ __forceinline__ F sub(F a, F b) { return a - b; }
-  static __device__ __forceinline__ F mul(F a, F b) { return a * b; }
 };
 template <> struct PM<PMODE_F32X2> {
   typedef float2 S;
@@ -170,8 +163,6 @@ __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev
         const F s = PM<M>::add(PM<M>::add(PM<M>::sub(fxhi, fx), PM<M>::sub(fyhi, fy)), PM<M>::sub(fzhi, fzlo));
         if constexpr (M == PMODE_F64) {
           store_images(tout, sy, sz, x, y, z, nx, ny, nz, __dadd_rn(tc, __dmul_rn(hdt, s)));
-        } else if constexpr (M == PMODE_F32) {
-          store_images(tout, sy, sz, x, y, z, nx, ny, nz, tc + hdt * s);
         } else {
           store_images(tout, sy, sz, x, y, z, nx, ny, nz, ff_add(tc, hdt * s));
         }
@@ -180,6 +171,135 @@ __global__ void __launch_bounds__(PT_THREADS) patches_step_kernel(const PatchDev
       fzlo = fzhi;
     }
     __syncthreads();  // shared faces are reused by the next item
+  }
+}
+
+// FP32 mode: one persistent launch over (patch, x-tile, y-tile) items that each cover the patch's
+// whole z extent.  Per item the tile (TX = 16, 32 or 64 wide, 4 * 256/TX rows: a column of CPT = 4
+// cells per thread) streams through a ring of PNS shared-memory stages with cp.async, as in the
+// FP32 heat step: plane p (z0-1 <= p <= z1) lives in stage (p - z0 + PNS) % PNS, iteration z waits
+// for planes up to z+1, syncs, refills the stage of plane z-2 with plane z+PNS-2 and computes from
+// the stages of planes z and z+1; the z loop is unrolled over the ring so stages are constants.
+// lambda is a scalar per patch, so each face costs (2 lambda) * (Tb - Ta): two FP32 operations.
+constexpr int PNS = 5;
+constexpr int PCPT = 4;
+constexpr int P_STAGE = 1188;  // (TX + 2) * (PCPT * 256 / TX + 2), largest over TX = 16, 32, 64
+constexpr int P_NCOPY = (P_STAGE + PT_THREADS - 1) / PT_THREADS;
+
+// the periodic ghost images of a boundary cell, out of line (rare; keeps the ring loop small)
+__device__ __noinline__ void patch_images(float* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
+                                          float v) {
+  const int ax = x == 0 ? nx : -1, ay = y == 0 ? ny : -1, az = z == 0 ? nz : -1;
+  const int m = (x == 0 || x == nx - 1) | ((y == 0 || y == ny - 1) << 1) | ((z == 0 || z == nz - 1) << 2);
+  for (int b = 1; b < 8; ++b) {
+    if (b & ~m) continue;
+    const int xx = (b & 1) ? ax : x, yy = (b & 2) ? ay : y, zz = (b & 4) ? az : z;
+    base[(long)xx + (long)sy * yy + sz * zz] = v;
+  }
+}
+
+__device__ __forceinline__ void pcp_async4(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void pcp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void pcp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__global__ void __launch_bounds__(PT_THREADS, 3) patches_f32_ring_kernel(const PatchDev* __restrict__ patches,
+                                                                         const WorkItem* __restrict__ items,
+                                                                         int nitems, const float* __restrict__ src,
+                                                                         float* __restrict__ dst) {
+  __shared__ __align__(16) float ring[PNS * P_STAGE];
+  const int tid = threadIdx.x;
+  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(ring);
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const WorkItem it = items[w];
+    const PatchDev P = patches[it.patch];
+    const int lx = P.log2tx, TX = 1 << lx, TYT = PT_THREADS >> lx;
+    const int PW = TX + 2, PLANE = PW * (PCPT * TYT + 2);
+    const int tx = tid & (TX - 1), ty = tid >> lx;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int sy = nx + 2;
+    const long sz = (long)(nx + 2) * (ny + 2);
+    const long interior = (long)1 + sy + sz;  // flat offset of interior (0,0,0)
+    const float* tin = src + P.offset + interior;
+    float* tout = dst + P.offset + interior;
+    const float l2 = (float)P.lam2, hdt = (float)P.hdt;
+    const int z0 = it.z0, z1 = it.z1;
+    // copy slots: unit k of the halo tile; units past the +ghost column/row clamp to it
+    int goff[P_NCOPY];
+#pragma unroll
+    for (int j = 0; j < P_NCOPY; ++j) {
+      const int k = min(tid + j * PT_THREADS, PLANE - 1);
+      const int r = k / PW, c = k - r * PW;
+      goff[j] = min(it.x0 - 1 + c, nx) + sy * min(it.y0 - 1 + r, ny);
+    }
+    auto issue = [&](int p, int st) {
+      if (p <= z1) {
+        const float* tp = tin + sz * p;
+        const uint32_t so = ring0 + (uint32_t)(st * P_STAGE) * sizeof(float);
+#pragma unroll
+        for (int j = 0; j < P_NCOPY; ++j) {
+          const int k = tid + j * PT_THREADS;
+          if (k < PLANE) pcp_async4(so + (uint32_t)k * sizeof(float), tp + goff[j]);
+        }
+      }
+    };
+    issue(z0 - 1, PNS - 1);
+    pcp_commit();
+#pragma unroll
+    for (int i = 0; i < PNS - 2; ++i) {
+      issue(z0 + i, i);
+      pcp_commit();
+    }
+    const int x = it.x0 + tx, yt = it.y0 + PCPT * ty;
+    const int ci = (PCPT * ty + 1) * PW + tx + 1;
+    pcp_wait<PNS - 3>();
+    __syncthreads();
+    float t[PCPT], fz[PCPT];
+#pragma unroll
+    for (int k = 0; k < PCPT; ++k) {
+      t[k] = ring[ci + k * PW];
+      fz[k] = l2 * (t[k] - ring[(PNS - 1) * P_STAGE + ci + k * PW]);
+    }
+    for (int zb = z0; zb < z1; zb += PNS) {
+#pragma unroll
+      for (int i = 0; i < PNS; ++i) {
+        const int z = zb + i;
+        if (z >= z1) break;
+        pcp_wait<PNS - 4>();
+        __syncthreads();
+        issue(z + PNS - 2, (i + PNS - 2) % PNS);
+        pcp_commit();
+        const float* T0 = ring + i * P_STAGE;
+        const float* Tn = ring + ((i + 1) % PNS) * P_STAGE;
+        float tn[PCPT], fy[PCPT + 1];
+#pragma unroll
+        for (int k = 0; k < PCPT; ++k) tn[k] = Tn[ci + k * PW];
+        fy[0] = l2 * (t[0] - T0[ci - PW]);
+#pragma unroll
+        for (int k = 1; k < PCPT; ++k) fy[k] = l2 * (t[k] - t[k - 1]);
+        fy[PCPT] = l2 * (T0[ci + PCPT * PW] - t[PCPT - 1]);
+#pragma unroll
+        for (int k = 0; k < PCPT; ++k) {
+          const int c = ci + k * PW;
+          const float fxl = l2 * (t[k] - T0[c - 1]);
+          const float fxh = l2 * (T0[c + 1] - t[k]);
+          const float fzh = l2 * (tn[k] - t[k]);
+          const float s = ((fxh - fxl) + (fy[k + 1] - fy[k])) + (fzh - fz[k]);
+          if (x < nx && yt + k < ny) {
+            const float v = t[k] + hdt * s;
+            tout[(long)x + (long)sy * (yt + k) + sz * z] = v;
+            if (x == 0 || x == nx - 1 || yt + k == 0 || yt + k == ny - 1 || z == 0 || z == nz - 1)
+              patch_images(tout, sy, sz, x, yt + k, z, nx, ny, nz, v);
+          }
+          fz[k] = fzh;
+          t[k] = tn[k];
+        }
+      }
+    }
+    pcp_wait<0>();
+    __syncthreads();  // the ring is refilled by the next item
   }
 }
 
@@ -201,6 +321,7 @@ struct PatchSet {
   int nitems = 0;
   int zchunk = 16;
   int grid = 0;
+  int grid32 = 0;  // resident blocks of the FP32 ring kernel (one full wave)
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, parity) -> graph
   ~PatchSet() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -221,7 +342,8 @@ std::vector<WorkItem> build_items(const PatchSet& ps, const std::vector<int>& wh
   std::vector<WorkItem> items;
   for (int p : which) {
     const int nx = ps.shape[3 * p], ny = ps.shape[3 * p + 1], nz = ps.shape[3 * p + 2];
-    const int TX = 1 << ps.log2tx[p], TY = PT_THREADS / TX;
+    // tile rows: one per thread row, or a column of PCPT cells per thread in FP32 mode
+    const int TX = 1 << ps.log2tx[p], TY = (ps.dtype == NEBO_F32 ? PCPT : 1) * (PT_THREADS / TX);
     for (int z0 = 0; z0 < nz; z0 += zchunk)
       for (int y0 = 0; y0 < ny; y0 += TY)
         for (int x0 = 0; x0 < nx; x0 += TX) items.push_back(WorkItem{p, x0, y0, z0, std::min(z0 + zchunk, nz)});
@@ -264,8 +386,9 @@ int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parit
                                                                (const double*)ps.arena[parity],
                                                                (double*)ps.arena[parity ^ 1]);
   else if (ps.dtype == NEBO_F32)
-    patches_step_kernel<PMODE_F32><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, ps.arena32[parity],
-                                                               ps.arena32[parity ^ 1]);
+    patches_f32_ring_kernel<<<std::min(nitems, ps.grid32), PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
+                                                                              ps.arena32[parity],
+                                                                              ps.arena32[parity ^ 1]);
   else
     patches_step_kernel<PMODE_F32X2><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems, ps.arena2[parity],
                                                                  ps.arena2[parity ^ 1]);
@@ -353,6 +476,14 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
     return cuda_fail(e, "nebo_patchset_create");
   }
   ps->grid = num_sms() * 8;
+  if (dtype == NEBO_F32) {
+    ps->zchunk = 1 << 30;  // FP32 items cover the patch's whole z extent
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, patches_f32_ring_kernel, PT_THREADS, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    ps->grid32 = num_sms() * per_sm;
+  }
   std::vector<int> all(npatch);
   for (int p = 0; p < npatch; ++p) all[p] = p;
   int rc = upload_tables(*ps, build_items(*ps, all, ps->zchunk), 0);
