@@ -249,6 +249,36 @@ int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_f
                        int steps, double dt, int checkpoint_every, const nebo_field* gT0,
                        const nebo_field* glam, double* J, nebo_stream_t stream);
 
+/* ------------------------------------------------------------------ particle <-> cell operators
+ * Replace Particle::CellToParticle<CellField>::apply_to_field and
+ * Particle::ParticleToCell<CellField>::apply_to_field (spatialops/particles/ParticleOperators.h:
+ * 319-398 and 183-246).  A particle is a cube of edge psize[p] centred at (px, py, pz)[p]; a null
+ * coordinate array switches that axis off (the particle covers one cell along it, weight 1).
+ * `mesh` holds the operator's state after its constructor (ParticleOperators.h:153-166): spacing
+ * already with the "spacing <= 0 becomes 1, low 0" rule applied, and the cell field's ghost
+ * cells on the - faces (GhostData::get_minus of get_ghost_data()).  Cell indices run over the
+ * field's window including its ghost cells, as SpatialField::operator()(i,j,k) does.
+ * Results equal the reference's serial loops bit for bit; boxes reaching outside the window are
+ * clipped to it at both ends (the reference clips the high end; its low end is undefined).
+ *   nebo_cell_to_particle  dest[p] = sum over the particle's cells of src(c) * weight, in the
+ *                          reference's (k, j, i) order.  Asynchronous.
+ *   nebo_particle_to_cell  every window cell of `cell` = sum over the particles that overlap it,
+ *                          in particle order, of src[p] * weight (+0 where none does).  Reads a
+ *                          64-bit overlap count back to size its entry list: synchronises the
+ *                          stream once.  Deterministic: no floating-point atomics. */
+typedef struct nebo_particle_mesh {
+  double spacing[3];       /* dx_, dy_, dz_ (> 0) */
+  double low[3];           /* xlo_, ylo_, zlo_: coordinate of the first interior cell's centre */
+  int32_t ghost_minus[3];  /* the cell field's ghost cells on the - faces */
+} nebo_particle_mesh;
+
+int nebo_cell_to_particle(const nebo_particle_mesh* mesh, const double* px, const double* py, const double* pz,
+                          const double* psize, int64_t nparticles, const nebo_field* cell, double* dest,
+                          nebo_stream_t stream);
+int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const double* px, const double* py, const double* pz,
+                          const double* psize, int64_t nparticles, const double* src, const nebo_field* cell,
+                          nebo_stream_t stream);
+
 /* ------------------------------------------------------------------ launch accounting
  * Every kernel launch of this library is counted; with profiling on, each launch (outside
  * graph capture) is also bracketed by CUDA events on its stream.  nebo_profile_report

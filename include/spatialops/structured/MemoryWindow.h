@@ -29,8 +29,10 @@ class MemoryWindow {
   IntVec extents() const { return extent_; }
   size_t glob_npts() const { return (size_t)nptsGlob_[0] * nptsGlob_[1] * nptsGlob_[2]; }
   size_t local_npts() const { return (size_t)extent_[0] * extent_[1] * extent_[2]; }
+  // Window-relative (i,j,k) -> allocation index; an axis of allocation extent 1 is always index 0
+  // (MemoryWindow.h:121-131 of the reference).
   size_t flat_index(IntVec loc) const {
-    loc += offset_;
+    for (int d = 0; d < 3; ++d) loc[d] = nptsGlob_[d] > 1 ? loc[d] + offset_[d] : 0;
     return (size_t)loc[0] + (size_t)nptsGlob_[0] * ((size_t)loc[1] + (size_t)nptsGlob_[1] * (size_t)loc[2]);
   }
   bool fits_between(const MemoryWindow& inner, const MemoryWindow& outer) const {

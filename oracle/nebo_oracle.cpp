@@ -756,3 +756,101 @@ void orc_heat_adjoint(const double* T0, const double* lam, double* gT, double* g
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- particle <-> cell operators
+namespace {
+
+struct PartBox {
+  long lo[3], hi[3];
+  double plo[3], phi[3], face[3];
+  double pvol;
+};
+
+// The box of window cells particle p touches (ParticleOperators.h:200-238 / 327-365).
+void part_box(PartBox& b, const double d[3], const double low[3], const int32_t ngm[3], const int32_t glob[3],
+              const int32_t nmax[3], const double* const pos[3], const double* psize, int64_t p) {
+  const double rp = psize[p] * 0.5;
+  for (int a = 0; a < 3; ++a) {
+    b.face[a] = low[a] - d[a] * ngm[a] - d[a] / 2;
+    b.plo[a] = pos[a] ? pos[a][p] - rp : 0;
+    b.phi[a] = pos[a] ? b.plo[a] + psize[p] : 0;
+    const double ql = (b.plo[a] - b.face[a]) / d[a];
+    // size_t conversion of the reference; a negative quotient clips to cell 0
+    b.lo[a] = !(ql < (double)nmax[a]) ? nmax[a] : (ql > 0 ? (long)ql : 0);
+    if (pos[a]) {
+      const double qh = (b.phi[a] - b.face[a]) / d[a];
+      if (!(qh > -1.0))
+        b.hi[a] = 0;
+      else
+        b.hi[a] = qh >= (double)nmax[a] ? nmax[a] : std::min((long)nmax[a], (long)(int)qh + 1);
+    } else if (glob[a] == 1) {
+      b.lo[a] = 0;  // flat_index maps every index of an extent-1 axis to 0
+      b.hi[a] = 1;
+    } else {
+      b.hi[a] = std::min((long)nmax[a], b.lo[a] + 1);
+    }
+  }
+  b.pvol = (pos[0] ? 2 * rp : 1) * (pos[1] ? 2 * rp : 1) * (pos[2] ? 2 * rp : 1);
+}
+
+double part_cont(const PartBox& b, const double d[3], const double* const pos[3], int a, long i) {
+  if (!pos[a]) return 1;
+  const double cm = b.face[a] + i * d[a];
+  const double cp = cm + d[a];
+  return std::min(cp, b.phi[a]) - std::max(cm, b.plo[a]);
+}
+
+size_t part_flat(const int32_t glob[3], const int32_t off[3], long i, long j, long k) {
+  const long x = glob[0] > 1 ? i + off[0] : 0, y = glob[1] > 1 ? j + off[1] : 0, z = glob[2] > 1 ? k + off[2] : 0;
+  return (size_t)x + (size_t)glob[0] * ((size_t)y + (size_t)glob[1] * (size_t)z);
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_cell_to_particle(const double spacing[3], const double low[3], const int32_t ngm[3], const int32_t glob[3],
+                          const int32_t off[3], const int32_t nmax[3], const double* cell, const double* px,
+                          const double* py, const double* pz, const double* psize, int64_t np, double* dest) {
+  const double* const pos[3] = {px, py, pz};
+  for (int64_t p = 0; p < np; ++p) {
+    PartBox b;
+    part_box(b, spacing, low, ngm, glob, nmax, pos, psize, p);
+    dest[p] = 0.0;
+    for (long k = b.lo[2]; k < b.hi[2]; ++k) {
+      const double zc = part_cont(b, spacing, pos, 2, k);
+      for (long j = b.lo[1]; j < b.hi[1]; ++j) {
+        const double yc = part_cont(b, spacing, pos, 1, j);
+        for (long i = b.lo[0]; i < b.hi[0]; ++i) {
+          const double xc = part_cont(b, spacing, pos, 0, i);
+          dest[p] += cell[part_flat(glob, off, i, j, k)] * (xc * yc * zc / b.pvol);
+        }
+      }
+    }
+  }
+}
+
+void orc_particle_to_cell(const double spacing[3], const double low[3], const int32_t ngm[3], const int32_t glob[3],
+                          const int32_t off[3], const int32_t nmax[3], double* cell, const double* px,
+                          const double* py, const double* pz, const double* psize, int64_t np, const double* src) {
+  for (long k = 0; k < nmax[2]; ++k)
+    for (long j = 0; j < nmax[1]; ++j)
+      for (long i = 0; i < nmax[0]; ++i) cell[part_flat(glob, off, i, j, k)] = 0.0;
+  const double* const pos[3] = {px, py, pz};
+  for (int64_t p = 0; p < np; ++p) {
+    PartBox b;
+    part_box(b, spacing, low, ngm, glob, nmax, pos, psize, p);
+    for (long k = b.lo[2]; k < b.hi[2]; ++k) {
+      const double zc = part_cont(b, spacing, pos, 2, k);
+      for (long j = b.lo[1]; j < b.hi[1]; ++j) {
+        const double yc = part_cont(b, spacing, pos, 1, j);
+        for (long i = b.lo[0]; i < b.hi[0]; ++i) {
+          const double xc = part_cont(b, spacing, pos, 0, i);
+          cell[part_flat(glob, off, i, j, k)] += src[p] * (xc * yc * zc / b.pvol);
+        }
+      }
+    }
+  }
+}
+
+}  // extern "C"

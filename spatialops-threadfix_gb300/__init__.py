@@ -47,6 +47,16 @@ class NeboField(ctypes.Structure):
     ]
 
 
+class ParticleMesh(ctypes.Structure):
+    """struct nebo_particle_mesh (include/nebo_gb300.h)."""
+
+    _fields_ = [
+        ("spacing", ctypes.c_double * 3),
+        ("low", ctypes.c_double * 3),
+        ("ghost_minus", ctypes.c_int32 * 3),
+    ]
+
+
 # (name, restype, argtypes) of every entry point declared in include/nebo_gb300.h
 _P = ctypes.c_void_p
 _FP = ctypes.POINTER(NeboField)
@@ -90,6 +100,8 @@ SIGNATURES = [
     ("nebo_heat_gradient", _I, [_FP, _FP, _FP, _I, _D, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_heat_gradient_ex", _I, [_FP, _FP, _FP, _I, _D, _I, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_fastmath_eval", _I, [_I, _P, _P, ctypes.c_size_t, _P]),
+    ("nebo_cell_to_particle", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _FP, _P, _P]),
+    ("nebo_particle_to_cell", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _P, _FP, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
     ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
@@ -429,3 +441,38 @@ def fastmath_eval(fn, x, stream=None):
     _check(lib().nebo_fastmath_eval({"exp": 0, "sin": 1}[fn], ctypes.c_void_p(x.data_ptr()),
                                     ctypes.c_void_p(y.data_ptr()), x.numel(), _stream(stream)))
     return y
+
+
+# ----------------------------------------------------------------------------- particles
+def _particle_args(cell, px, py, pz, psize, spacing, low, ghost_minus):
+    d = cell.desc() if isinstance(cell, Field) else cell
+    m = ParticleMesh()
+    m.spacing[:] = [float(v) for v in spacing]
+    m.low[:] = [float(v) for v in low]
+    m.ghost_minus[:] = list(d.ghost_minus) if ghost_minus is None else [int(v) for v in ghost_minus]
+    ptr = [ctypes.c_void_p(t.data_ptr()) if t is not None else None for t in (px, py, pz, psize)]
+    n = int(psize.numel()) if psize is not None else 0
+    return d, m, ptr, n
+
+
+def cell_to_particle(cell, px, py, pz, psize, dest, spacing, low, ghost_minus=None, stream=None):
+    """Particle::CellToParticle::apply_to_field (spatialops/particles/ParticleOperators.h:319-398):
+    dest[p] = the particle-volume-weighted sum of the cell values its box covers.  cell is a Field
+    (or a NeboField descriptor); px, py, pz (None = axis off), psize and dest are float64 device
+    tensors of one value per particle; spacing / low are the operator's state after its
+    constructor; ghost_minus defaults to the field's ghost cells on the - faces."""
+    d, m, ptr, n = _particle_args(cell, px, py, pz, psize, spacing, low, ghost_minus)
+    _check(lib().nebo_cell_to_particle(ctypes.byref(m), *ptr, ctypes.c_int64(n), ctypes.byref(d),
+                                       ctypes.c_void_p(dest.data_ptr()), _stream(stream)))
+    return dest
+
+
+def particle_to_cell(src, px, py, pz, psize, cell, spacing, low, ghost_minus=None, stream=None):
+    """Particle::ParticleToCell::apply_to_field (spatialops/particles/ParticleOperators.h:183-246):
+    every window cell of `cell` = the sum, in particle order, of src[p] x the fraction of particle
+    p's volume inside it (0 where no particle reaches).  Synchronises the stream once."""
+    d, m, ptr, n = _particle_args(cell, px, py, pz, psize, spacing, low, ghost_minus)
+    _check(lib().nebo_particle_to_cell(ctypes.byref(m), *ptr, ctypes.c_int64(n),
+                                       ctypes.c_void_p(src.data_ptr()) if src is not None else None,
+                                       ctypes.byref(d), _stream(stream)))
+    return cell

@@ -61,6 +61,8 @@ PROGRAMS = {
     # exact: no contraction anywhere, user functors (apply_pointwise) included
     "catalog_gpu_exact": ("catalog_gpu.cu", ["-DNEBO_EXACT_ARITHMETIC", "--fmad=false"]),
     "catalog_gpu_fast": ("catalog_gpu.cu", []),
+    # particle <-> cell scenes (tests/cpp/particles_scene.h) on the drop-in headers
+    "particles_gpu": ("particles_gpu.cu", []),
 }
 
 

@@ -190,3 +190,57 @@ def transport_inputs_device(n, seed=10, modes=4, nu=0.05, device="cuda"):
     r2 = ((xx + 0.5 - n / 2.0) ** 2 + (yy + 0.5 - n / 2.0) ** 2 + (zz + 0.5 - n / 2.0) ** 2)
     phi = torch.exp(-r2 / (2.0 * (n / 8.0) ** 2))
     return phi.contiguous(), u.contiguous(), v.contiguous(), w.contiguous(), lam.contiguous(), 0.4, nu
+
+
+# ----------------------------------------------------------------------------- particles
+def particle_window(n, g, field="svol", bcx=False):
+    """Allocation (= window, ghosts included) of an SVol or XVol cell field with g ghost cells
+    (plus the +x boundary cell of an XVol with a boundary there), and its ghost cells on the -
+    faces after limit_by_extent (0 on an axis of extent 1).  Returns (glob xyz, ngm xyz)."""
+    n = tuple(n)
+    glob, ngm = [], []
+    for a in range(3):
+        if n[a] > 1:
+            glob.append(n[a] + 2 * g + (1 if (a == 0 and bcx and field == "xvol") else 0))
+            ngm.append(g)
+        else:
+            glob.append(1)
+            ngm.append(0)
+    return tuple(glob), tuple(ngm)
+
+
+def particle_inputs(n, g, nparticles, axes=7, spacing=(1.0, 1.0, 1.0), low=(0.5, 0.5, 0.5),
+                    size_range=(0.3, 2.5), seed=11, spill=False, field="svol", bcx=False):
+    """Seeded inputs of one particle <-> cell case.
+
+    Cell values ~ U(-1, 1) over the whole allocation; particle values ~ U(0.5, 2); particle
+    edges ~ U(size_range) x the smallest spacing of the axes in use.  Along each axis in use the
+    centres are uniform such that every box lies inside the window, or (spill=True) such that a
+    box may stick out of either end by up to 0.9 of a cell (the reference's own behaviour is
+    defined there).  Axes not in use get coordinates 0.  `spacing` / `low` are the operator's
+    state after its constructor (spacing > 0)."""
+    rng = np.random.default_rng(seed)
+    glob, ngm = particle_window(n, g, field, bcx)
+    cell = rng.uniform(-1.0, 1.0, size=(glob[2], glob[1], glob[0]))
+    on = [(axes >> a) & 1 for a in range(3)]
+    dmin = min(spacing[a] for a in range(3) if on[a]) if any(on) else 1.0
+    size = rng.uniform(size_range[0], size_range[1], nparticles) * dmin
+    pos = []
+    for a in range(3):
+        if not on[a]:
+            pos.append(np.zeros(nparticles))
+            continue
+        d = spacing[a]
+        face = low[a] - d * ngm[a] - d / 2
+        span = glob[a] * d
+        r = size / 2
+        u = rng.uniform(0.0, 1.0, nparticles)
+        if spill:
+            lo_c, hi_c = face - 0.9 * d + r, face + span + 0.9 * d - r
+        else:
+            lo_c, hi_c = face + r, face + span - r
+        pos.append(lo_c + u * np.maximum(hi_c - lo_c, 0.0))
+    pval = rng.uniform(0.5, 2.0, nparticles)
+    return dict(glob=np.array(glob), ngm=np.array(ngm), cell=cell, px=pos[0], py=pos[1], pz=pos[2],
+                psize=size, pval=pval, axes=axes, spacing=np.array(spacing, dtype=float),
+                low=np.array(low, dtype=float))

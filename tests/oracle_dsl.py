@@ -501,6 +501,31 @@ def reduce_field(f, g, op, interior=False):
     return lib().orc_reduce_field(_p(np.ascontiguousarray(f)), _i3((gx, gy, gz)), int(g), RED[op], int(interior))
 
 
+def particle_ops(case, off=(0, 0, 0), nmax=None, fill=-7777.25):
+    """CellToParticle(cell) and ParticleToCell(pval) of the oracle for one particle case (the dict
+    of workloads.particle_inputs or a golden case).  The cell field's window starts at `off` and
+    spans `nmax` (default: the whole allocation); allocation cells outside it keep `fill`."""
+    glob = tuple(int(v) for v in case["glob"])
+    nmax = glob if nmax is None else tuple(nmax)
+    axes = int(case["axes"])
+    cell = np.ascontiguousarray(case["cell"], dtype=np.float64)
+    npart = len(case["psize"])
+    pos = [np.ascontiguousarray(case[k], dtype=np.float64) for k in ("px", "py", "pz")]
+    ptrs = [_p(pos[a]) if (axes >> a) & 1 else None for a in range(3)]
+    psize = np.ascontiguousarray(case["psize"], dtype=np.float64)
+    pval = np.ascontiguousarray(case["pval"], dtype=np.float64)
+    d3 = (ctypes.c_double * 3)(*[float(v) for v in case["spacing"]])
+    l3 = (ctypes.c_double * 3)(*[float(v) for v in case["low"]])
+    c2p = np.empty(npart)
+    p2c = np.full_like(cell, fill)
+    L = lib()
+    L.orc_cell_to_particle(d3, l3, _i3(case["ngm"]), _i3(glob), _i3(off), _i3(nmax), _p(cell), *ptrs, _p(psize),
+                           ctypes.c_int64(npart), _p(c2p))
+    L.orc_particle_to_cell(d3, l3, _i3(case["ngm"]), _i3(glob), _i3(off), _i3(nmax), _p(p2c), *ptrs, _p(psize),
+                           ctypes.c_int64(npart), _p(pval))
+    return c2p, p2c
+
+
 def fill_periodic(f, g):
     gz, gy, gx = f.shape
     lib().orc_fill_periodic(_p(f), _i3((gx - 2 * g, gy - 2 * g, gz - 2 * g)), int(g))

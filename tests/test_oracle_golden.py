@@ -95,3 +95,49 @@ def test_write_limits_deep_chain_negative_ghost():
     i, g = db.interp("SVol", "XVol"), db.grad("XVol", "SVol")
     lim, any_ = O.write_limits(out, i(g(i(a))))
     assert any_ and lim == (1, 8, -1, 9, -1, 9)
+
+
+# ----------------------------------------------------------------------------- particles
+_PARTICLES = np.load(os.path.join(GOLD, "particles.npz"))
+
+
+def particle_case(name):
+    """One case of particles.npz: the inputs of workloads.particle_inputs plus the reference's
+    outputs c2p (CellToParticle) and p2c (ParticleToCell, allocation pre-filled with -7777.25)."""
+    pre = name + "__"
+    return {k[len(pre):]: _PARTICLES[k] for k in _PARTICLES.files if k.startswith(pre)}
+
+
+PARTICLE_NAMES = [str(c) for c in _PARTICLES["cases"]]
+
+
+@pytest.mark.parametrize("name", PARTICLE_NAMES)
+def test_particles_match_reference(name):
+    c = particle_case(name)
+    c2p, p2c = O.particle_ops(c)
+    assert _same_bits(c2p, c["c2p"]), name
+    assert _same_bits(p2c, c["p2c"]), name
+
+
+def test_particles_reference_known_answers():
+    # the reference's own checks (spatialops/particles/test/TestParticleOperators.cpp:86-97)
+    c = particle_case("reftest")
+    c2p, p2c = O.particle_ops(c)
+    assert c2p[0] == 32.5
+    assert list(p2c.ravel()[3:13]) == [1, 4, 4, 4, 4, 3, 0, 0, 0, 0]
+
+
+def test_particles_low_clip_keeps_inside_fraction():
+    # a box sticking out of the window's low end by more than one cell: the reference leaves
+    # this undefined; the oracle (and the GPU) clip it, so a constant field interpolates to the
+    # fraction of the particle inside the window and the scatter deposits that fraction
+    c = W.particle_inputs((6, 5, 4), 1, 3, axes=7, seed=3)
+    c["cell"][:] = 1.0
+    face = c["low"] - c["spacing"] * c["ngm"] - c["spacing"] / 2
+    c["psize"][:] = 3.0
+    c["px"][:] = face[0] + 0.25   # 1.25 cells out on the low x side
+    c["py"][:] = face[1] + 2.5
+    c["pz"][:] = face[2] + 2.0
+    c2p, p2c = O.particle_ops(c)
+    assert np.allclose(c2p, 1.75 / 3.0, rtol=0, atol=1e-15)
+    assert abs(p2c.sum() - c["pval"].sum() * 1.75 / 3.0) < 1e-13
