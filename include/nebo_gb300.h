@@ -168,7 +168,9 @@ int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, const nebo_
  * argument reduction's one exact product in FP64, the rest in FP32, 32-bit and 64-bit fixed
  * point (Tang's 2^(j/256) table for exp; sin/cos(k pi/256) for sin).  Within 0.52 ulp (exp,
  * |x| < 708) and about 1.1 ulp (sin, |x| < 2^20) of the exact result; other arguments use
- * CUDA's exp and sin. */
+ * CUDA's exp and sin.  fn 2 and 3 take n pairs (a, b) in x (2n doubles) and write a / b:
+ * fn 2 through the reciprocal-and-correction quotient the particle operators use, fn 3 by
+ * plain division; both must agree bit for bit. */
 int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ batched patches

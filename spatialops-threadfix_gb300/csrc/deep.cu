@@ -327,14 +327,22 @@ extern "C" int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, 
 namespace nebo {
 namespace {
 __global__ void fastmath_kernel(int fn, const double* __restrict__ x, double* __restrict__ y, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    y[i] = fn == 0 ? fixmath::exp_i(x[i]) : fixmath::sin_i(x[i]);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (fn == 0) {
+      y[i] = fixmath::exp_i(x[i]);
+    } else if (fn == 1) {
+      y[i] = fixmath::sin_i(x[i]);
+    } else {
+      const double a = x[2 * i], b = x[2 * i + 1];
+      y[i] = fn == 2 ? fixmath::div_by(a, b, __drcp_rn(b), fixmath::divisor_ok(b)) : __ddiv_rn(a, b);
+    }
+  }
 }
 }  // namespace
 }  // namespace nebo
 
 extern "C" int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream) {
-  if ((fn != 0 && fn != 1) || (n && (!x || !y))) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_fastmath_eval");
+  if (fn < 0 || fn > 3 || (n && (!x || !y))) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_fastmath_eval");
   if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_fastmath_eval: math tables upload");
   if (!n) return NEBO_OK;
   cudaStream_t s = (cudaStream_t)stream;

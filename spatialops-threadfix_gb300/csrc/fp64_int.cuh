@@ -381,6 +381,34 @@ inline int tables_init() {
 
 __device__ __forceinline__ double exp_i(double x) { return exp_fix(x, DeviceTables()); }
 __device__ __forceinline__ double sin_i(double x) { return sin_fix(x, DeviceTables()); }
+
+// Biased exponent of a double (integer pipe).
+__device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+// A divisor whose reciprocal div_by may use: positive, exponent within 2^+-400 (integer pipe).
+__device__ __forceinline__ bool divisor_ok(double b) {
+  const int e = dexp(b);
+  return __double_as_longlong(b) >= 0 && e >= 1023 - 400 && e <= 1023 + 400;
+}
+
+// RN(a / b) given y = RN(1/b) (one reciprocal serves many quotients by the same b):
+// q0 = RN(a y), then two FMA corrections q' = RN(q + (a - b q) y).  Markstein's theorem
+// (P. W. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): when y is within half an ulp of 1/b and q within
+// one ulp of a/b, a - b q is exact and q' = RN(a/b).  The first correction brings q0 (within
+// 1.5 ulps) to within one ulp; the second rounds correctly.  Applied where a / b and every
+// intermediate stay normal (b_ok: divisor_ok(b); a's exponent within 2^+-500; a zero quotient
+// is a * y); anywhere else the division itself.
+__device__ __forceinline__ double div_by(double a, double b, double y, bool b_ok) {
+  const int ea = dexp(a);
+  if (b_ok && ea >= 1023 - 500 && ea <= 1023 + 500) {
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, b, a), y, q0);
+    return __fma_rn(__fma_rn(-q1, b, a), y, q1);
+  }
+  if (b_ok && a == 0.0) return __dmul_rn(a, y);
+  return __ddiv_rn(a, b);
+}
 #endif
 
 }  // namespace fixmath

@@ -1,5 +1,6 @@
 """The integer-pipe FP64 exp and sin (nebo_fastmath_eval, the functions of the deep chain)
 against CUDA's own (torch's) exp and sin, in ulps."""
+import ctypes
 import zlib
 
 import numpy as np
@@ -65,3 +66,42 @@ def test_sin_near_multiples_of_pi():
     u = _ulps(got, ref)
     assert u.max() <= 2, (int(u.max()), x[int(np.argmax(u))])
     assert (np.signbit(got[-4:]) == np.signbit(x[-4:])).all()
+
+
+def _quotients(fn, a, b):
+    import torch
+
+    import spatialops_gb300 as S
+
+    x = torch.from_numpy(np.stack([a, b], axis=1).ravel().copy()).cuda()
+    y = torch.empty(len(a), dtype=torch.float64, device="cuda")
+    S._check(S.lib().nebo_fastmath_eval(fn, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                        len(a), S._stream()))
+    torch.cuda.synchronize()
+    return y.cpu().numpy()
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_reciprocal_quotient_is_correctly_rounded(seed):
+    # the particle operators' a / b from RN(1/b) and two FMA corrections against the division,
+    # bit for bit: random mantissas over wide exponent ranges, the operators' own value ranges
+    # (products of overlaps over particle volumes), exact quotients, signed zeros, and operands
+    # outside the corrected path's range (division fallback)
+    rng = np.random.default_rng(seed)
+    n = 4_000_000
+    a = rng.uniform(1, 2, n) * np.exp2(rng.integers(-60, 60, n))
+    b = rng.uniform(1, 2, n) * np.exp2(rng.integers(-60, 60, n))
+    a[: n // 8] = rng.uniform(0, 1, n // 8) ** 3                   # overlap products in [0, 1]
+    b[: n // 8] = rng.uniform(0.1, 3.0, n // 8) ** 3               # particle volumes
+    k = rng.integers(1, 1 << 20, n // 8).astype(np.float64)
+    a[n // 8: n // 4] = k * b[n // 8: n // 4]                      # exact integer quotients (where exact)
+    a[n // 4: n // 4 + 1000] = 0.0
+    a[n // 4 + 1000: n // 4 + 2000] = -0.0
+    a[n // 4 + 2000: n // 4 + 3000] = np.exp2(-900.0) * rng.uniform(1, 2, 1000)  # fallback ranges
+    b[n // 4 + 3000: n // 4 + 4000] = np.exp2(600.0)
+    neg = rng.random(n) < 0.3
+    a[neg] = -a[neg]
+    fast = _quotients(2, a, b)
+    div = _quotients(3, a, b)
+    assert np.array_equal(fast.view(np.uint64), div.view(np.uint64))
+    assert np.array_equal(div, a / b)  # and the host's correctly rounded division
