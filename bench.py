@@ -51,11 +51,13 @@ BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
     "transport32": 4 * 5 + 8 + 8 + 4,      # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
     # one reverse step: T_k, A_{k+1}, lambda read, glam read and written, A_k written
     "adjoint": 8 * 6,
+    # ParticleToCell fill, per particle: x, y, z, size and value read (its entries are not counted)
+    "particles": 8 * 5,
 }
 DOMINANT = {"deep": "deep_chain", "heat": "heat_step_f64", "heat32": "heat_step_f32",
             "patches": "patches_step_f64", "patches32": "patches_step_f32",
             "transport": "transport_stage_f64", "transport32": "transport_stage_f32",
-            "adjoint": "heat_adjoint_step"}
+            "adjoint": "heat_adjoint_step", "particles": "particle_to_cell_fill"}
 
 
 def measured_peak_hbm():
@@ -408,6 +410,59 @@ class AdjointWL:
         return e0.elapsed_time(e1) / reps
 
 
+class ParticlesWL:
+    """Particle <-> cell exchange: a 256^3 SVol cell field + 1 ghost and one particle per interior
+    cell (16.8 M), edges ~ U(0.5, 1.5) cells, centres uniform with every box inside the window,
+    in random order.  A step is CellToParticle (cell field -> one value per particle) then
+    ParticleToCell (particle values -> cell field); the metric counts particles per second."""
+
+    name = "particles"
+
+    def __init__(self, N, n):
+        import torch
+
+        self.N, self.n = N, n
+        self.npart = n ** 3
+        gen = torch.Generator(device="cuda").manual_seed(12)
+        d = 1.0 / n
+        self.spacing, self.low = (d, d, d), (0.5 * d,) * 3
+        face = 0.5 * d - d - d / 2
+        span = (n + 2) * d
+        f64 = dict(device="cuda", dtype=torch.float64)
+        self.size = torch.rand(self.npart, generator=gen, **f64) * d + 0.5 * d
+        self.pos = [face + self.size / 2 + torch.rand(self.npart, generator=gen, **f64) * (span - self.size)
+                    for _ in range(3)]
+        self.pval = torch.rand(self.npart, generator=gen, **f64)
+        self.gas = N.Field("SVol", n, 1)
+        self.gas.tensor.copy_(torch.rand(self.gas.tensor.shape, generator=gen, **f64))
+        self.src_field = N.Field("SVol", n, 1)
+        self.out_p = torch.empty(self.npart, **f64)
+        self.host_in = [t.cpu().pin_memory() for t in (*self.pos, self.size, self.pval, self.gas.tensor)]
+        self.host_out = [torch.empty(self.npart, dtype=torch.float64).pin_memory(),
+                         torch.empty(self.src_field.tensor.shape, dtype=torch.float64).pin_memory()]
+        self.cells = self.npart
+        self.cells_per_launch = self.npart
+        self.launches_per_step = 7  # gather, count, 3 scan kernels, fill, fold
+        self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host_in)
+        self.d2h_bytes = sum(h.numel() * h.element_size() for h in self.host_out)
+        self.metric = "particle cell<->particle exchanges/s"
+        self.unit = "Gparticle/s"
+        self.label = (f"particles: {n}^3 SVol + 1 ghost, {self.npart / 1e6:.1f} M particles (edges U(0.5,1.5) cells, "
+                      f"random order); step = CellToParticle + ParticleToCell, FP64, bit-identical to the reference")
+
+    def step(self):
+        N = self.N
+        N.cell_to_particle(self.gas, *self.pos, self.size, self.out_p, self.spacing, self.low)
+        N.particle_to_cell(self.pval, *self.pos, self.size, self.src_field, self.spacing, self.low)
+
+    def step_e2e(self):
+        for t, h in zip((*self.pos, self.size, self.pval, self.gas.tensor), self.host_in):
+            t.copy_(h, non_blocking=True)
+        self.step()
+        self.host_out[0].copy_(self.out_p, non_blocking=True)
+        self.host_out[1].copy_(self.src_field.tensor, non_blocking=True)
+
+
 def make_workload(N, name, n):
     if name in ("transport", "transport32"):
         return TransportWL(N, n, "f64" if name == "transport" else "f32")
@@ -421,6 +476,8 @@ def make_workload(N, name, n):
         return Heat(N, n, "f32")
     if name == "adjoint":
         return AdjointWL(N, 192 if n == N_DEFAULT else n)
+    if name == "particles":
+        return ParticlesWL(N, n)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -450,8 +507,31 @@ def cpu_run(workload, n_xy, nz, threads):
     return time.perf_counter() - t0
 
 
+def cpu_particles(n, npart):
+    """CellToParticle + ParticleToCell of npart particles on an n^3 field by the serial oracle;
+    returns seconds."""
+    O = _oracle()
+    from spatialops_gb300 import workloads as W
+
+    d = 1.0 / n
+    c = W.particle_inputs((n, n, n), 1, npart, axes=7, spacing=(d, d, d), low=(0.5 * d,) * 3,
+                          size_range=(0.5, 1.5), seed=12)
+    t0 = time.perf_counter()
+    O.particle_ops(c)
+    return time.perf_counter() - t0
+
+
 def cpu_baseline(workload, n, budget_s=10.0):
     """Serial oracle (1 core) on the full workload, repeated until ~budget_s of CPU work."""
+    if workload == "particles":
+        npart = 2_000_000
+        reps, total = 0, 0.0
+        while total < budget_s and reps < 20:
+            total += cpu_particles(n, npart)
+            reps += 1
+        return {"value": reps * npart / total / 1e9, "unit": "Gparticle/s", "cores": 1, "kind": "port",
+                "sample": f"{reps} x (CellToParticle + ParticleToCell of {npart} particles on the {n}^3 field), "
+                          f"serial oracle loops (the reference's operators are serial), {total:.1f} s"}
     reps, total = 0, 0.0
     while total < budget_s and reps < 20:
         total += cpu_run("deep" if workload == "deep" else "heat", n, n, 1)
@@ -468,6 +548,26 @@ def run_reference(args):
     graft._import_pkg()
     threads = os.cpu_count() or 1
     n = args.n
+    if args.workload == "particles":
+        # the reference's ParticleToCell / CellToParticle are serial loops over the particles
+        npart = 1_000_000
+        for _ in range(max(args.warmup, 0)):
+            cpu_particles(n, npart)
+        t = sum(cpu_particles(n, npart) for _ in range(args.steps))
+        value = args.steps * npart / t / 1e9
+        line = {
+            "impl": "reference", "metric": "particle cell<->particle exchanges/s", "value": value,
+            "unit": "Gparticle/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"particles on the {n}^3 field", "sample": f"{npart} particles per step"},
+            "cpu_baseline": {"value": value, "unit": "Gparticle/s", "cores": 1, "kind": "port",
+                             "sample": f"CellToParticle + ParticleToCell of {npart} particles on the {n}^3 field per "
+                                       f"step, oracle restatement of the reference's serial operator loops"},
+            "e2e": {"value": value, "unit": "Gparticle/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
     nz = 16
     workload = args.workload if args.workload in ("deep", "heat") else "heat"
     for _ in range(max(args.warmup, 0)):
@@ -500,7 +600,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="deep", choices=["deep", "heat", "heat32", "patches", "patches32", "transport",
-                                                             "transport32", "adjoint"])
+                                                             "transport32", "adjoint", "particles"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -615,7 +715,7 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu = None
-    if not args.no_cpu_baseline and W.name in ("deep", "heat", "heat32"):
+    if not args.no_cpu_baseline and W.name in ("deep", "heat", "heat32", "particles"):
         cpu = cpu_baseline(W.name, args.n)
     extra = {}
     if W.name == "adjoint":
@@ -625,7 +725,8 @@ def main():
                  "forward_value": W.cells / (fwd * 1e-3) / 1e9, "J": W.J,
                  "adjoint_over_forward_all_fp64": g64 / fwd}
     line = {
-        "metric": getattr(W, "metric", f"{W.name} cell-updates/s"), "value": value, "unit": "Gcell-upd/s",
+        "metric": getattr(W, "metric", f"{W.name} cell-updates/s"), "value": value,
+        "unit": getattr(W, "unit", "Gcell-upd/s"),
         "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if W.name.endswith("32") else "f64",
@@ -633,7 +734,7 @@ def main():
         "config": {"workload": getattr(W, "label", f"{W.name} {args.n}^3 + 1 ghost"), "cells_per_step": W.cells,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (129 MB); no flush between steps"},
-        "e2e": {"value": e2e_value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": W.h2d_bytes,
+        "e2e": {"value": e2e_value, "unit": getattr(W, "unit", "Gcell-upd/s"), "h2d_bytes_per_step": W.h2d_bytes,
                 "d2h_bytes_per_step": W.d2h_bytes, "steps": e_steps,
                 "copies": ("uploads on a copy stream into 2 alternating input sets, overlapping the previous "
                            "step's kernels" if hasattr(W, "e2e_begin") else "serial with the kernels")},

@@ -369,6 +369,7 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
   // 3 face-coefficient arrays, ~ (2 sqrt(N) + 6) fields
   const size_t nbuf = (size_t)nck + (size_t)L + 6;
   double* pool = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&pool, nbuf * bytes + 256 * sizeof(double), s));
   const int rc = gradient_impl(pool, cells, nck, L, (int)nbuf, T0, lam, Ttarget, steps, dt, exact, gT0, glam, J,
                                stream);

@@ -78,6 +78,11 @@ class LaunchScope {
   void* b_;
 };
 
+// Make the current device's default memory pool keep freed blocks (release threshold = max) so
+// that stream-ordered allocations that recur every step (work lists, entry lists) are served
+// from the pool instead of the driver.  Once per device; a process-local pool setting.
+void pool_retain();
+
 // Periodic ghost fill of one uniform-ghost patch (ghost.cu).
 int fill_periodic_any(const nebo_field* f, cudaStream_t s);
 

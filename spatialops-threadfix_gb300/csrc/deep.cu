@@ -284,6 +284,7 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
                      hi[2] != ihi[2];
   const int sblocks = shell ? num_sms() * 2 : 0;
   Acc4* partials = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&partials, sizeof(Acc4) * (fblocks + sblocks), s));
   {
     LaunchScope ls("box_filter_reduce", s);

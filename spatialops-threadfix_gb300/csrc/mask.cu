@@ -33,6 +33,7 @@ extern "C" int nebo_mask_from_points(uint32_t* words, const int32_t glob[3], con
   if (npoints == 0) return NEBO_OK;
   cudaStream_t s = (cudaStream_t)stream;
   int* bad = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&bad, sizeof(int), s));
   NEBO_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), s));
   const int threads = 256;

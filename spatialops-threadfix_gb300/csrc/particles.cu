@@ -581,6 +581,7 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
   const size_t cnt_o = 0, off_o = (cnt_b + 15) & ~(size_t)15, bs_o = off_o + ((off_b + 15) & ~(size_t)15);
   const size_t gr_o = bs_o + ((bs_b + 15) & ~(size_t)15), tot_o = gr_o + 16, ws_b = tot_o + 16;
   char* ws = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&ws, ws_b, s));
   int* cnt = (int*)(ws + cnt_o);
   int* off = (int*)(ws + off_o);
@@ -617,9 +618,15 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     }
   }
   {
-    LaunchScope ls("particle_to_cell_scan", s);
+    LaunchScope ls("particle_to_cell_scan_tiles", s);
     scan_tile_sums_kernel<<<(unsigned)ntile, SCAN_THREADS, 0, s>>>(cnt, nscan, bsum);
+  }
+  {
+    LaunchScope ls("particle_to_cell_scan_sums", s);
     scan_block_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(bsum, (int)ntile, grand);
+  }
+  {
+    LaunchScope ls("particle_to_cell_scan_apply", s);
     scan_tile_apply_kernel<<<(unsigned)ntile, SCAN_THREADS, 0, s>>>(cnt, nscan, bsum, off);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) {

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_final_kernel(const Acc* __
 // never share partials.
 int scratch_alloc(Acc** partials, double** result, cudaStream_t s) {
   void* p = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync(&p, RED_MAX_BLOCKS * sizeof(Acc) + 64, s));
   *partials = (Acc*)p;
   *result = (double*)((char*)p + RED_MAX_BLOCKS * sizeof(Acc));
@@ -383,6 +384,7 @@ extern "C" int nebo_reduce_all(const nebo_field* f, int interior, double* d_out4
   if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
   cudaStream_t s = (cudaStream_t)stream;
   Acc4* partials = nullptr;
+  pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&partials, sizeof(Acc4) * blocks, s));
   const int sy = f->glob[0];
   const long sz = (long)f->glob[0] * f->glob[1];

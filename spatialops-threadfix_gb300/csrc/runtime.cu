@@ -64,6 +64,19 @@ int check_periodic_patch(const nebo_field* f, int g, const char* what) {
   return NEBO_OK;
 }
 
+
+void pool_retain() {
+  static std::atomic<unsigned long long> done{0};  // one bit per device (first 64)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  if (done.load() & (1ull << dev)) return;
+  cudaMemPool_t pool;
+  unsigned long long thr = ~0ull;
+  cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, dev);
+  if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  if (e != cudaSuccess) cudaGetLastError();  // not fatal: allocations still work, only slower
+  done.fetch_or(1ull << dev);
+}
 }  // namespace nebo
 
 using namespace nebo;
@@ -99,6 +112,7 @@ int nebo_device_count(int* count) {
   return NEBO_OK;
 }
 
+
 int nebo_device_init(int device) {
   int n = 0;
   int rc = nebo_device_count(&n);
@@ -113,6 +127,7 @@ int nebo_alloc(size_t bytes, void** ptr, nebo_stream_t stream) {
   if (!ptr) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_alloc: null output pointer");
   *ptr = nullptr;
   if (bytes == 0) return NEBO_OK;
+  nebo::pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync(ptr, bytes, (cudaStream_t)stream));
   return NEBO_OK;
 }
