@@ -391,22 +391,43 @@ __device__ __forceinline__ bool divisor_ok(double b) {
   return __double_as_longlong(b) >= 0 && e >= 1023 - 400 && e <= 1023 + 400;
 }
 
-// RN(a / b) given y = RN(1/b) (one reciprocal serves many quotients by the same b):
-// q0 = RN(a y), then two FMA corrections q' = RN(q + (a - b q) y).  Markstein's theorem
-// (P. W. Markstein, "Computation of elementary functions on the IBM RISC System/6000
-// processor", IBM J. Res. Dev. 34(1), 1990): when y is within half an ulp of 1/b and q within
-// one ulp of a/b, a - b q is exact and q' = RN(a/b).  The first correction brings q0 (within
-// 1.5 ulps) to within one ulp; the second rounds correctly.  Applied where a / b and every
-// intermediate stay normal (b_ok: divisor_ok(b); a's exponent within 2^+-500; a zero quotient
-// is a * y); anywhere else the division itself.
+// RN(a / b) given y = RN(1/b) (one reciprocal serves many quotients by the same b).
+//
+// Main path (a, b > 0, everything normal): q0 = RN(a y) is within 1.5 ulps of a/b (y is within
+// half an ulp of 1/b).  With a = A 2^(ea-1075), b = B 2^(eb-1075), q0 = Q 2^(eq-1075) (A, B, Q
+// the 53-bit integer significands), the remainder a - q0 b equals 2^(eq+eb-2150) R with
+// R = A 2^s - Q B, s = ea - eq - eb + 1075, and (a/b - q0) / ulp(q0) = R / B.  |R| < 1.5 B < 2^55,
+// so R is exact in 64-bit integer arithmetic (modulo 2^64), and RN(a/b) = q0 + k ulp with k the
+// integer nearest R / B (a quotient of two doubles is never a tie).  When q0 lies within two
+// ulps of its binade's ends the step k ulp could cross the binade; those quotients, and every
+// other case, take the second path.
+//
+// Second path: two FMA corrections q' = RN(q + (a - b q) y).  By Markstein's theorem
+// (P. W. Markstein, "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990), when y is within half an ulp of 1/b and q within one ulp of
+// a/b, a - b q is exact and q' = RN(a/b); the first correction brings q0 within one ulp.  Used
+// where a / b and every intermediate stay normal (b_ok: divisor_ok(b); a's exponent within
+// 2^+-500; a zero quotient is a * y); anywhere else the division itself.
 __device__ __forceinline__ double div_by(double a, double b, double y, bool b_ok) {
-  const int ea = dexp(a);
+  const double q0 = __dmul_rn(a, y);
+  const long long ab = __double_as_longlong(a), bb = __double_as_longlong(b), qb = __double_as_longlong(q0);
+  const int ea = (int)((ab >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff), eq = (int)((qb >> 52) & 0x7ff);
+  const unsigned long long frac = 0xFFFFFFFFFFFFFull, one = 1ull << 52;
+  const unsigned long long mq = (unsigned long long)qb & frac;
+  const int s = ea - eq - eb + 1075;
+  if (b_ok && ab > 0 && ea >= 1 && ea <= 2046 && eq >= 1 && eq <= 2046 && mq >= 2 && mq <= frac - 2 && s >= 40 &&
+      s <= 62) {
+    const unsigned long long A = ((unsigned long long)ab & frac) | one, B = ((unsigned long long)bb & frac) | one;
+    const unsigned long long Q = mq | one;
+    const long long R = (long long)((A << s) - Q * B);
+    const long long k = (long long)(2 * R > (long long)B) - (long long)(2 * R < -(long long)B);
+    return __longlong_as_double(qb + k);
+  }
   if (b_ok && ea >= 1023 - 500 && ea <= 1023 + 500) {
-    const double q0 = __dmul_rn(a, y);
     const double q1 = __fma_rn(__fma_rn(-q0, b, a), y, q0);
     return __fma_rn(__fma_rn(-q1, b, a), y, q1);
   }
-  if (b_ok && a == 0.0) return __dmul_rn(a, y);
+  if (b_ok && a == 0.0) return q0;
   return __ddiv_rn(a, b);
 }
 #endif
