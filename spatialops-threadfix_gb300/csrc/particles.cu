@@ -182,8 +182,8 @@ __device__ __forceinline__ long win_flat(const PGeom& g, int i, int j, int k) {
 // particle, over its lanes 32 at a time, so every lane does the same work per pair whatever the
 // box sizes.  For CellToParticle the owner lane then adds its pairs' products in that order.
 constexpr int PB = 4;
-constexpr int PWARPS = 8;
-constexpr int PCAP = 128;  // CellToParticle: products held per warp before the owners add them
+constexpr int PWARPS = 8;  // warps per block
+constexpr int PCAP = 512;  // CellToParticle: products held per warp before the owners add them
 enum { PM_C2P = 0, PM_FILL = 2 };
 
 template <int MODE>
@@ -232,11 +232,12 @@ __device__ __noinline__ double serial_particle(const PGeom& g, const double* __r
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(PWARPS * 32) particles_kernel(
+__global__ void __launch_bounds__(PWARPS * 32, 2) particles_kernel(
     PGeom g, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
     const double* __restrict__ psize, long np, const double* __restrict__ cell, double* __restrict__ dest,
     const double* __restrict__ src, const int* __restrict__ off, int* __restrict__ cnt, Entry* __restrict__ ent) {
-  __shared__ WarpShared<MODE> smem[PWARPS];
+  extern __shared__ __align__(16) unsigned char particle_smem[];
+  WarpShared<MODE>* smem = reinterpret_cast<WarpShared<MODE>*>(particle_smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpShared<MODE>& sm = smem[warp];
   for (long base = ((long)blockIdx.x * PWARPS + warp) * 32; base < np; base += (long)gridDim.x * PWARPS * 32) {
@@ -534,6 +535,18 @@ int particle_blocks(long np, int per_sm = 6) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// CellToParticle's shared memory exceeds the 48 KB default; opt in once per device.
+int c2p_prepare() {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "nebo_cell_to_particle");
+  if (dev < 64 && (done.load() & (1ull << dev))) return NEBO_OK;
+  NEBO_CUDA_TRY(cudaFuncSetAttribute(particles_kernel<PM_C2P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(PWARPS * sizeof(WarpShared<PM_C2P>))));
+  if (dev < 64) done.fetch_or(1ull << dev);
+  return NEBO_OK;
+}
+
 }  // namespace
 }  // namespace nebo
 
@@ -549,9 +562,10 @@ extern "C" int nebo_cell_to_particle(const nebo_particle_mesh* mesh, const doubl
   if (nparticles == 0) return NEBO_OK;
   if (!psize || !dest) return fail(NEBO_ERR_INVALID, "Nebo error in %s: null particle size or destination", who);
   cudaStream_t s = (cudaStream_t)stream;
+  if (int rc = c2p_prepare()) return rc;
   {
     LaunchScope ls("cell_to_particle", s);
-    particles_kernel<PM_C2P><<<particle_blocks(nparticles), PWARPS * 32, 0, s>>>(
+    particles_kernel<PM_C2P><<<particle_blocks(nparticles), PWARPS * 32, PWARPS * sizeof(WarpShared<PM_C2P>), s>>>(
         g, px, py, pz, psize, (long)nparticles, static_cast<const double*>(cell->data), dest, nullptr, nullptr,
         nullptr, nullptr);
   }
@@ -640,7 +654,7 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     }
     {
       LaunchScope ls("particle_to_cell_fill", s);
-      particles_kernel<PM_FILL><<<particle_blocks(nparticles), PWARPS * 32, 0, s>>>(
+      particles_kernel<PM_FILL><<<particle_blocks(nparticles), PWARPS * 32, PWARPS * sizeof(WarpShared<PM_FILL>), s>>>(
           g, px, py, pz, psize, (long)nparticles, nullptr, nullptr, src, off, cnt, ent);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) {
