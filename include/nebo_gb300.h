@@ -254,9 +254,9 @@ int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_f
 /* ------------------------------------------------------------------ particle <-> cell operators
  * Replace Particle::CellToParticle<CellField>::apply_to_field and
  * Particle::ParticleToCell<CellField>::apply_to_field (spatialops/particles/ParticleOperators.h:
- * 319-398 and 183-246).  A particle is a cube of edge psize[p] centred at (px, py, pz)[p]; a null
+ * 313-398 and 186-273).  A particle is a cube of edge psize[p] centred at (px, py, pz)[p]; a null
  * coordinate array switches that axis off (the particle covers one cell along it, weight 1).
- * `mesh` holds the operator's state after its constructor (ParticleOperators.h:153-166): spacing
+ * `mesh` holds the operator's state after its constructor (ParticleOperators.h:152-166 and 277-291): spacing
  * already with the "spacing <= 0 becomes 1, low 0" rule applied, and the cell field's ghost
  * cells on the - faces (GhostData::get_minus of get_ghost_data()).  Cell indices run over the
  * field's window including its ghost cells, as SpatialField::operator()(i,j,k) does.

@@ -766,7 +766,7 @@ struct PartBox {
   double pvol;
 };
 
-// The box of window cells particle p touches (ParticleOperators.h:200-238 / 327-365).
+// The box of window cells particle p touches (ParticleOperators.h:214-238 / 337-361).
 void part_box(PartBox& b, const double d[3], const double low[3], const int32_t ngm[3], const int32_t glob[3],
               const int32_t nmax[3], const double* const pos[3], const double* psize, int64_t p) {
   const double rp = psize[p] * 0.5;

@@ -20,7 +20,7 @@
  *   mask bit lookup ............... spatialops/NeboMask.h:130-197, structured/BitField.h:291-333
  *   stencil fold order ............ spatialops/NeboStencils.h:280-524, 826-1046
  *   reductions (nebo_fold) ........ spatialops/NeboReductions.h:45-240
- *   particle <-> cell operators ... spatialops/particles/ParticleOperators.h:183-246, 319-398
+ *   particle <-> cell operators ... spatialops/particles/ParticleOperators.h:186-273, 313-398
  *
  * Expressions arrive as a prefix-encoded int32 program plus a table of double immediates:
  *   ORC_FIELD  idx                 field leaf (index into the field table)
@@ -123,8 +123,8 @@ void orc_heat_adjoint(const double* T0, const double* lam, double* gT, double* g
 /* Serial left fold over the ghosted window of one field (nebo_sum/max/min/norm). */
 double orc_reduce_field(const double* f, const int32_t glob[3], int32_t g, int op, int interior);
 
-/* Particle <-> cell operators (spatialops/particles/ParticleOperators.h:183-246 ParticleToCell,
- * :319-398 CellToParticle), serial loops in the reference's order.  The cell field is one
+/* Particle <-> cell operators (spatialops/particles/ParticleOperators.h:186-273 ParticleToCell,
+ * :313-398 CellToParticle), serial loops in the reference's order.  The cell field is one
  * allocation of glob points whose window (ghosts included) starts at off and spans nmax;
  * spacing / low are the operator's state after its constructor (:153-166), ngm the field's ghost
  * cells on the - faces.  px, py, pz may be NULL (axis off).  A box that leaves the window is

@@ -456,7 +456,7 @@ def _particle_args(cell, px, py, pz, psize, spacing, low, ghost_minus):
 
 
 def cell_to_particle(cell, px, py, pz, psize, dest, spacing, low, ghost_minus=None, stream=None):
-    """Particle::CellToParticle::apply_to_field (spatialops/particles/ParticleOperators.h:319-398):
+    """Particle::CellToParticle::apply_to_field (spatialops/particles/ParticleOperators.h:313-398):
     dest[p] = the particle-volume-weighted sum of the cell values its box covers.  cell is a Field
     (or a NeboField descriptor); px, py, pz (None = axis off), psize and dest are float64 device
     tensors of one value per particle; spacing / low are the operator's state after its
@@ -468,7 +468,7 @@ def cell_to_particle(cell, px, py, pz, psize, dest, spacing, low, ghost_minus=No
 
 
 def particle_to_cell(src, px, py, pz, psize, cell, spacing, low, ghost_minus=None, stream=None):
-    """Particle::ParticleToCell::apply_to_field (spatialops/particles/ParticleOperators.h:183-246):
+    """Particle::ParticleToCell::apply_to_field (spatialops/particles/ParticleOperators.h:186-273):
     every window cell of `cell` = the sum, in particle order, of src[p] x the fraction of particle
     p's volume inside it (0 where no particle reaches).  Synchronises the stream once."""
     d, m, ptr, n = _particle_args(cell, px, py, pz, psize, spacing, low, ghost_minus)

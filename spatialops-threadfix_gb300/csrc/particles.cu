@@ -1,5 +1,5 @@
-// Particle <-> cell operators (the kernels behind Particle::CellToParticle and
-// Particle::ParticleToCell, spatialops/particles/ParticleOperators.h:183-246 and :319-398).
+// Particle <-> cell operators (the kernels behind Particle::CellToParticle::apply_to_field,
+// spatialops/particles/ParticleOperators.h:313-398, and ParticleToCell::apply_to_field, :186-273).
 //
 // A particle p is a cube of edge size[p] centred at (px, py, pz)[p].  A null coordinate array
 // switches an axis off: the particle then covers one cell along it with weight 1.  For each cell
@@ -35,7 +35,7 @@ namespace {
 
 struct PGeom {
   double d[3];     // mesh spacing dx_, dy_, dz_
-  double face[3];  // low face of window cell 0: xlo_ - dx_*ngm - dx_/2 (ParticleOperators.h:202-204)
+  double face[3];  // low face of window cell 0: xlo_ - dx_*ngm - dx_/2 (ParticleOperators.h:197-199)
   double inv[3];   // RN(1/d)
   int nmax[3];     // window extent (ghosts included)
   int glob[3];     // allocation
@@ -94,7 +94,7 @@ __device__ __forceinline__ double dmin(double a, double b) { return okey(b) < ok
 __device__ __forceinline__ double dmax(double a, double b) { return okey(a) < okey(b) ? b : a; }
 
 // The cells [lo, hi) of the window the particle covers along one axis (ParticleOperators.h:
-// 200-230 / 327-357, both ends clipped to the window).
+// 214-234 / 337-357, both ends clipped to the window).
 __device__ __forceinline__ void make_axis(Axis& ax, double pos, double size, const PGeom& g, int a) {
   const double rp = __dmul_rn(size, 0.5);
   const bool on = g.on[a];
@@ -109,7 +109,7 @@ __device__ __forceinline__ void make_axis(Axis& ax, double pos, double size, con
   long long hi;
   if (on) {
     const long long th = index_quot(__dsub_rn(ax.phi, g.face[a]), g, a, nan);
-    // int() + 1 clipped to the window (ParticleOperators.h:228-230); below -1 (or NaN): empty
+    // int() + 1 clipped to the window (ParticleOperators.h:232-234); below -1 (or NaN): empty
     hi = nan || th < 0 ? 0 : (th + 1 < n ? th + 1 : n);
   } else if (g.glob[a] == 1) {
     lo = 0;  // the reference's one cell along an off axis; an allocation extent of 1 maps every

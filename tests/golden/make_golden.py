@@ -54,7 +54,7 @@ PARTICLE_CASES = {
 
 
 def particle_state(ctor):
-    """Spacing and low coordinate after the operators' constructor (ParticleOperators.h:153-166)."""
+    """Spacing and low coordinate after the operators' constructor (ParticleOperators.h:152-166 and 277-291)."""
     d, lo = [], []
     for a in range(3):
         da, la = ctor[2 * a], ctor[2 * a + 1]

@@ -253,7 +253,7 @@ def test_full_size_properties():
     out = torch.empty(npart, dtype=torch.float64, device="cuda")
     S.cell_to_particle(cell, *pos, size, out, (d, d, d), (0.5 * d,) * 3)
     # the weights come from coordinate differences, so they sum to one only to ~1e-13; the
-    # reference's debug check allows 1e-10 (ParticleOperators.h:240-243, 390-393)
+    # reference's debug check allows 1e-10 (ParticleOperators.h:270, 395)
     assert (out - 1.0).abs().max().item() < 1e-10
     cell.tensor.copy_(torch.rand(cell.tensor.shape, generator=gen, device="cuda", dtype=torch.float64))
     S.cell_to_particle(cell, *pos, size, out, (d, d, d), (0.5 * d,) * 3)
