@@ -164,6 +164,15 @@ int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, const nebo_
                            const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt,
                            double dx, int interior, double* d_out4, nebo_stream_t stream);
 
+/* filt <<= BoxFilter3D(src) alone (the filter of nebo_deep_chain; 27 points, coefficient 1/27,
+ * spatialops/NeboStencilBuilder.h:454-465) over the interior, for any FP64 field with one
+ * periodic-style ghost layer (window = allocation, no BC cells).  The 27-point sums are exact in
+ * 64-bit fixed point per plane (see deep.cu); the value is within 1e-13 relative of the
+ * reference's FP64 sum.  d_out4 non-null: {sum, max, min, norm} of dst as nebo_reduce_all gives
+ * them (ghost-inclusive unless interior), folded into the same pass. */
+int nebo_box_filter(const nebo_field* src, const nebo_field* dst, int interior, double* d_out4,
+                    nebo_stream_t stream);
+
 /* Element-wise FP64 exp (fn 0) or sin (fn 1) with the functions nebo_deep_chain uses: the
  * argument reduction's one exact product in FP64, the rest in FP32, 32-bit and 64-bit fixed
  * point (Tang's 2^(j/256) table for exp; sin/cos(k pi/256) for sin).  Within 0.52 ulp (exp,

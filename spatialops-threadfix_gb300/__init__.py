@@ -100,6 +100,7 @@ SIGNATURES = [
     ("nebo_heat_gradient", _I, [_FP, _FP, _FP, _I, _D, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_heat_gradient_ex", _I, [_FP, _FP, _FP, _I, _D, _I, _I, _FP, _FP, ctypes.POINTER(_D), _P]),
     ("nebo_fastmath_eval", _I, [_I, _P, _P, ctypes.c_size_t, _P]),
+    ("nebo_box_filter", _I, [_FP, _FP, _I, _P, _P]),
     ("nebo_cell_to_particle", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _FP, _P, _P]),
     ("nebo_particle_to_cell", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _P, _FP, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
@@ -293,6 +294,15 @@ def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None, reductions=None, 
                                         ctypes.c_void_p(words.data_ptr()), ctypes.byref(do), ctypes.byref(df),
                                         float(dx), int(interior), ctypes.c_void_p(reductions.data_ptr()),
                                         _stream(stream)))
+
+
+def box_filter(src, dst, reductions=None, interior=False, stream=None):
+    """dst <<= BoxFilter3D(src) (27 points x 1/27) on the interior; with `reductions` (a float64
+    device tensor of 4) also {sum, max, min, norm} of dst in the same pass."""
+    a, b = src.desc(), dst.desc()
+    rp = ctypes.c_void_p(reductions.data_ptr()) if reductions is not None else None
+    _check(lib().nebo_box_filter(ctypes.byref(a), ctypes.byref(b), int(bool(interior)), rp, _stream(stream)))
+    return dst
 
 
 def kernel_launch_count():

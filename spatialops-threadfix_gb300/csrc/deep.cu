@@ -59,19 +59,29 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-constexpr int FNS = 6;   // filter ring stages
+constexpr int FNS = 5;   // filter ring stages
 constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns two y-adjacent cells)
 
 // filt[x,y,z] = (sum over the 27 neighbours of out) / 27 on the interior, and with RED the
 // four reductions of the values written (one Acc4 partial per block).
+//
 // Planes of `out` (the 32 x 16 tile plus a one-cell halo) stream through a ring of FNS
 // shared-memory stages with cp.async.  Ring schedule: plane p (-1..nz) lives in stage
 // (p+1) % FNS; the prologue issues planes z0-1 .. z0+FNS-3; iteration p waits until plane p has
 // landed (at most FNS-2 groups pending), syncs, issues plane p+FNS-1 into the stage of plane p-1
 // (consumed in iteration p-1, before the sync), then sums plane p: x-sums of 3 into `rows`
-// (two neighbouring sums share their middle pair: 3 adds for 2 sums), a sync, y-sums of 3 for
-// the thread's two cells (again sharing the middle pair); the 2-D sums of planes p-2, p-1, p
-// give the outputs of plane p-1.  FP64 adds are the bound, hence the shared pairs.
+// (two neighbouring sums share their middle pair), a sync, y-sums of 3 for the thread's two
+// cells; the 2-D sums of planes p-2, p-1, p give the outputs of plane p-1.
+//
+// The sums run on the integer pipe, exactly, in 128-bit fixed point (fp64_int.cuh).  A plane
+// whose largest biased exponent is E converts each value to an integer in units of 2^(E-1144),
+// rounded to nearest: every value down to 2^-69 of the plane's largest keeps its 53 bits, each
+// term is below 2^122 and 27 of them stay below 2^127.  The three plane sums of an output are
+// aligned to the largest unit, added, rounded once to a double and multiplied by RN(1/27).
+// Error: at most 14 units of the largest plane (2^-118 of its largest |value|) before the two
+// roundings, against the reference's 27 roundings of up to 2^-53 of the running sum.  A plane
+// holding an infinity or NaN, or only values below 2^-893 (all-zero planes included), sums in
+// FP64 instead (the adds of the reference, reassociated).
 template <bool RED>
 __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
                                                             int sy, long sz, int nx, int ny, int nz, int zchunk,
@@ -80,7 +90,9 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
   constexpr int NCOPY = (PLANE + FX * FY - 1) / (FX * FY);
   constexpr int XTASKS = PH * (FX / 2);  // x-sum pairs per plane
   __shared__ __align__(16) double ring[FNS * PLANE];
-  __shared__ double rows[PH * FX];
+  __shared__ fixmath::fix128 fplane[PLANE];  // the plane in fixed point (once per value)
+  __shared__ fixmath::fix128 rows[PH * FX];  // fixed-point x-sums (or FP64 bits on a special plane)
+  __shared__ unsigned plane_exp[2];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
   const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FTY;
   const int x = x0 + tx, ya = y0 + 2 * ty;
@@ -105,15 +117,21 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
       cp_async8(st + soff[j], sp + goff[j]);
     }
   };
+  if (tid < 2) plane_exp[tid] = 0u;
 #pragma unroll 1
   for (int i = 0; i < FNS - 1; ++i) {
     issue(z0 - 1 + i);
     cp_async_commit();
   }
   const bool act0 = x < nx && ya < ny, act1 = x < nx && ya + 1 < ny;
-  double p0 = 0.0, c0 = 0.0, p1 = 0.0, c1 = 0.0;  // 2-D sums of planes p-2 and p-1, both cells
+  // 2-D sums of planes p-2 (p*) and p-1 (c*) for both cells: fixed-point integers in units of
+  // 2^u*, or FP64 bits when the plane was special (sp*)
+  fixmath::fix128 p0 = 0, c0 = 0, p1 = 0, c1 = 0;
+  int up = 0, uc = 0;
+  bool spp = false, spc = false;
   Acc4 acc = acc4_identity();
   double* out = dst + (long)x + (long)sy * ya + sz * (z0 - 1);
+  const int lane = tid & 31;
 #pragma unroll 1
   for (int p = z0 - 1; p <= z1; ++p, out += sz) {
     cp_async_wait<FNS - 2>();
@@ -121,25 +139,65 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
     issue(p + FNS - 1);
     cp_async_commit();
     const double* pl = ring + ((p + 1) % FNS) * PLANE;
+    // the plane's largest biased exponent; this thread's values stay in registers
+    constexpr int PER = (PLANE + FX * FY - 1) / (FX * FY);
+    double val[PER];
+    unsigned e = 0;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int t = tid + j * FX * FY;
+      val[j] = t < PLANE ? pl[t] : 0.0;
+      e = max(e, ((unsigned)__double2hiint(val[j]) >> 20) & 0x7ffu);
+    }
+    e = __reduce_max_sync(0xffffffffu, e);
+    if (lane == 0) atomicMax(&plane_exp[p & 1], e);
+    __syncthreads();
+    const int E = (int)plane_exp[p & 1];
+    if (tid == 0) plane_exp[(p + 1) & 1] = 0u;  // the slot of plane p+1 (last read in iteration p-1)
+    const bool special = E == 0x7ff || E < 130;
+    const int u = E - 1144;
+    if (!special) {
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        const int t = tid + j * FX * FY;
+        if (t < PLANE) fplane[t] = fixmath::to_units(val[j], E);
+      }
+      __syncthreads();
+    }
     for (int t = tid; t < XTASKS; t += FX * FY) {
       const int r = t / (FX / 2), c = 2 * (t % (FX / 2));
-      const double* q = pl + r * PW + c;
-      const double mid = q[1] + q[2];
-      rows[r * FX + c] = q[0] + mid;
-      rows[r * FX + c + 1] = mid + q[3];
+      if (!special) {
+        const fixmath::fix128* f = fplane + r * PW + c;
+        const fixmath::fix128 mid = f[1] + f[2];
+        rows[r * FX + c] = f[0] + mid;
+        rows[r * FX + c + 1] = mid + f[3];
+      } else {
+        const double* q = pl + r * PW + c;
+        const double mid = q[1] + q[2];
+        rows[r * FX + c] = __double_as_longlong(q[0] + mid);
+        rows[r * FX + c + 1] = __double_as_longlong(mid + q[3]);
+      }
     }
     __syncthreads();
-    const double* col = rows + 2 * ty * FX + tx;
-    const double mid = col[FX] + col[2 * FX];
-    const double s0 = col[0] + mid, s1 = mid + col[3 * FX];
+    const fixmath::fix128* col = rows + 2 * ty * FX + tx;
+    fixmath::fix128 s0, s1;
+    if (!special) {
+      const fixmath::fix128 mid = col[FX] + col[2 * FX];
+      s0 = col[0] + mid;
+      s1 = mid + col[3 * FX];
+    } else {
+      const double mid = __longlong_as_double((long long)col[FX]) + __longlong_as_double((long long)col[2 * FX]);
+      s0 = __double_as_longlong(__longlong_as_double((long long)col[0]) + mid);
+      s1 = __double_as_longlong(mid + __longlong_as_double((long long)col[3 * FX]));
+    }
     if (p >= z0 + 1) {
       if (act0) {
-        const double v = ((p0 + c0) + s0) * (1.0 / 27.0);
+        const double v = fixmath::box27(p0, up, spp, c0, uc, spc, s0, u, special);
         out[-sz] = v;  // plane p-1
         if (RED) acc4_add(acc, v);
       }
       if (act1) {
-        const double v = ((p1 + c1) + s1) * (1.0 / 27.0);
+        const double v = fixmath::box27(p1, up, spp, c1, uc, spc, s1, u, special);
         out[sy - sz] = v;
         if (RED) acc4_add(acc, v);
       }
@@ -148,6 +206,10 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
     c0 = s0;
     p1 = c1;
     c1 = s1;
+    up = uc;
+    uc = u;
+    spp = spc;
+    spc = special;
   }
   cp_async_wait<0>();
   if (RED) {
@@ -224,6 +286,9 @@ namespace nebo {
 void reduction_region(const nebo_field& f, int interior, int lo[3], int hi[3]);
 namespace {
 
+int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int interior, double* d_out4,
+                cudaStream_t s, const char* what);
+
 int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, const uint32_t* mask_words,
               const nebo_field* out, const nebo_field* filt, double dx, bool reduce, int interior, double* d_out4,
               cudaStream_t s, const char* what) {
@@ -236,7 +301,7 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
   interior_extent(*a, n);
   const View<const double> va = make_view<const double>(*a), vb = make_view<const double>(*b),
                            vc = make_view<const double>(*c);
-  const View<double> vo = make_view<double>(*out), vf = make_view<double>(*filt);
+  const View<double> vo = make_view<double>(*out);
   // flat window index of interior (0,0,0): used to locate mask bits
   const long mask_base = (long)(out->offset[0] + 1) + (long)out->glob[0] * (out->offset[1] + 1) +
                          (long)out->glob[0] * out->glob[1] * (out->offset[2] + 1);
@@ -253,6 +318,15 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
                                            n[0], n[1], n[2], q);
     NEBO_LAUNCH_CHECK(what);
   }
+  return filter_impl(out, filt, reduce, interior, d_out4, s, what);
+}
+
+// filt <<= BoxFilter(out) on the interior, optionally with sum/max/min/norm of filt.
+int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int interior, double* d_out4,
+                cudaStream_t s, const char* what) {
+  int n[3];
+  interior_extent(*out, n);
+  const View<double> vo = make_view<double>(*out), vf = make_view<double>(*filt);
   // filter: one full wave of blocks (z chunks from the resident-block count)
   static int per_sm[2] = {0, 0};
   if (!per_sm[reduce]) {
@@ -310,6 +384,21 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
 
 }  // namespace
 }  // namespace nebo
+
+extern "C" int nebo_box_filter(const nebo_field* src, const nebo_field* dst, int interior, double* d_out4,
+                               nebo_stream_t stream) {
+  const char* w = "nebo_box_filter";
+  int rc;
+  const nebo_field* fs[2] = {src, dst};
+  for (int i = 0; i < 2; ++i) {
+    if ((rc = check_field(fs[i], w))) return rc;
+    if (fs[i]->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: FP64 fields only", w);
+    if ((rc = check_periodic_patch(fs[i], 1, w))) return rc;
+  }
+  if ((rc = check_same_layout(src, dst, w))) return rc;
+  if (src->data == dst->data) return fail(NEBO_ERR_INVALID, "Nebo error in %s: output aliases input", w);
+  return filter_impl(src, dst, d_out4 != nullptr, interior, d_out4, (cudaStream_t)stream, w);
+}
 
 extern "C" int nebo_deep_chain(const nebo_field* a, const nebo_field* b, const nebo_field* c,
                                const uint32_t* mask_words, const nebo_field* out, const nebo_field* filt, double dx,

@@ -385,6 +385,105 @@ __device__ __forceinline__ double sin_i(double x) { return sin_fix(x, DeviceTabl
 // Biased exponent of a double (integer pipe).
 __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
 
+// 128-bit fixed point for exact sums of doubles that share one scale.  A plane (tile) whose
+// largest biased exponent is E counts in units of 2^(E-1144): |x| < 2^(E-1022) becomes an
+// integer below 2^122, 27 of them stay below 2^127, and every x down to 2^-69 of the plane's
+// largest keeps all of its 53 bits.  Integer pipe only.
+typedef __int128 fix128;
+
+__device__ __forceinline__ fix128 make128(long long hi, unsigned long long lo) {
+  return (fix128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
+// x (biased exponent <= E, not inf/NaN) in units of 2^(E-1144), rounded to nearest (halves up):
+// the 53-bit significand m lands at bit sh = e - E + 69 <= 69 of a 128-bit integer.
+__device__ __forceinline__ fix128 to_units(double x, int E) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  const int sh = (e ? e : 1) - E + 69;
+  unsigned long long hi, lo;
+  if (sh >= 64) {
+    hi = m << (sh - 64);
+    lo = 0;
+  } else if (sh > 0) {
+    hi = m >> (64 - sh);
+    lo = m << sh;
+  } else {
+    hi = 0;
+    lo = sh == 0 ? m : (-sh > 62 ? 0ull : (m + (1ull << (-sh - 1))) >> -sh);
+  }
+  const fix128 f = make128((long long)hi, lo);
+  return b < 0 ? -f : f;
+}
+
+// f (units of 2^u) in units of 2^U >= 2^u, rounded to nearest (halves up).
+__device__ __forceinline__ fix128 rescale_units(fix128 f, int u, int U) {
+  const int k = U - u;
+  if (k == 0) return f;
+  if (k > 126) return 0;
+  const fix128 g = f + ((fix128)1 << (k - 1));
+  const long long hi = (long long)(g >> 64);
+  const unsigned long long lo = (unsigned long long)g;
+  if (k >= 64) return make128(hi >> 63, (unsigned long long)(hi >> (k - 64)));
+  return make128(hi >> k, (lo >> k) | ((unsigned long long)hi << (64 - k)));
+}
+
+// RN(t 2^u) for t != 0, assuming the result is normal.
+__device__ __forceinline__ double units_to_double(fix128 t, int u) {
+  const bool neg = t < 0;
+  const unsigned __int128 a = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
+  const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
+  unsigned long long top, rest;
+  int msb;  // position of the leading bit
+  if (hi) {
+    const int lz = __clzll(hi);
+    top = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    rest = lo << lz;  // bits below `top` (only whether any is set matters)
+    msb = 127 - lz;
+  } else {
+    const int lz = __clzll(lo);
+    top = lo << lz;
+    rest = 0;
+    msb = 63 - lz;
+  }
+  unsigned long long mant = top >> 11;  // 53 bits
+  const unsigned long long rb = top & 0x7ffull;
+  const bool up = rb > 0x400ull || (rb == 0x400ull && (rest != 0 || (mant & 1ull)));
+  int ex = msb + u + 1023;
+  mant += up ? 1ull : 0ull;
+  if (mant >> 53) {
+    mant >>= 1;
+    ++ex;
+  }
+  const unsigned long long bits = ((unsigned long long)neg << 63) | ((unsigned long long)ex << 52) |
+                                  (mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+// Box value sum / 27 from three plane sums, each fixed point (units 2^u_i) or, on a special
+// plane, FP64 bits in the low word; see box_filter_kernel.
+__device__ __forceinline__ double box27(fix128 a, int ua, bool sa, fix128 b, int ub, bool sb, fix128 c, int uc,
+                                        bool sc) {
+  constexpr double C27 = 1.0 / 27.0;
+  if (!(sa || sb || sc)) {
+    int U = ua;
+    fix128 t;
+    if (ua == ub && ub == uc) {  // the three planes share a unit: no rescaling
+      t = (a + b) + c;
+    } else {
+      U = max(ua, max(ub, uc));
+      t = rescale_units(a, ua, U) + rescale_units(b, ub, U) + rescale_units(c, uc, U);
+    }
+    if (t == 0) return 0.0;
+    return __dmul_rn(units_to_double(t, U), C27);
+  }
+  auto dbl = [](fix128 f, int u, bool sp) {
+    return sp ? __longlong_as_double((long long)f) : (f == 0 ? 0.0 : units_to_double(f, u));
+  };
+  return ((dbl(a, ua, sa) + dbl(b, ub, sb)) + dbl(c, uc, sc)) * C27;
+}
+
 // A divisor whose reciprocal div_by may use: positive, exponent within 2^+-400 (integer pipe).
 __device__ __forceinline__ bool divisor_ok(double b) {
   const int e = dexp(b);

@@ -98,3 +98,94 @@ def test_fused_filter_reductions(n, interior):
     assert abs(got[0] - O.reduce_field(f2, 1, "sum", interior)) <= 1e-13 * scale
     o_norm = O.reduce_field(f2, 1, "norm", interior)
     assert abs(got[3] - o_norm) <= 1e-13 * o_norm
+
+
+# ----------------------------------------------------------------------------- standalone filter
+FILL = -7777.25
+
+
+def _filter_inputs(kind, n, seed):
+    """An XVol window (1 ghost) of one of several value distributions."""
+    rng = np.random.default_rng(seed)
+    g = O.glob_dims("XVol", n, 1, (0, 0, 0))
+    shp = (g[2], g[1], g[0])
+    if kind == "uniform":
+        return rng.uniform(-1.0, 1.0, shp)
+    if kind == "spikes":  # ambient values near 1 and a few cells 1e18 larger in the same tiles
+        a = rng.uniform(0.5, 1.5, shp)
+        idx = rng.integers(0, a.size, 40)
+        a.flat[idx] = 1e18
+        return a
+    if kind == "range20":  # |values| spread over 10^-10 .. 10^10, random signs
+        return 10.0 ** rng.uniform(-10, 10, shp) * rng.choice([-1.0, 1.0], shp)
+    if kind == "special":  # inf, -inf and NaN cells, an all-zero plane, a plane of subnormals
+        a = rng.uniform(-1.0, 1.0, shp)
+        a.flat[rng.integers(0, a.size, 3)] = np.inf
+        a.flat[rng.integers(0, a.size, 3)] = -np.inf
+        a.flat[rng.integers(0, a.size, 3)] = np.nan
+        a[4] = 0.0
+        a[7] = rng.uniform(-1.0, 1.0, a[7].shape) * 2.0 ** -1070
+        a[9] = rng.uniform(-1.0, 1.0, a[9].shape) * 2.0 ** -900
+        return a
+    raise ValueError(kind)
+
+
+def _oracle_filter(src, n):
+    db = O.OpDB(n, n)
+    lhs = O.Field("XVol", np.full_like(src, FILL), 1)
+    O.assign(lhs, db.filter()(O.Field("XVol", np.ascontiguousarray(src), 1)))
+    return lhs.data
+
+
+def _local_abs(src):
+    """sum over the 27 neighbours of |src| / 27 at every interior cell (ghost layer: 0)."""
+    a = np.abs(np.nan_to_num(src, nan=0.0, posinf=0.0, neginf=0.0))
+    out = np.zeros_like(a)
+    inner = (slice(1, -1),) * 3
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                out[inner] += a[1 + dz:a.shape[0] - 1 + dz, 1 + dy:a.shape[1] - 1 + dy, 1 + dx:a.shape[2] - 1 + dx]
+    return out / 27.0
+
+
+@pytest.mark.parametrize("kind", ["uniform", "spikes", "range20", "special"])
+def test_box_filter_matches_oracle(kind):
+    # the 128-bit fixed-point sums against the oracle's FP64 sums, cell by cell: within 1e-13 of
+    # the local magnitude sum (the scale of either side's rounding), same written cells, same
+    # infinities and NaNs
+    import torch
+
+    n = (45, 37, 21)
+    src = _filter_inputs(kind, n, 17)
+    want = _oracle_filter(src, n)
+    S = N.Field.from_numpy("XVol", src, 1)
+    D = N.Field.from_numpy("XVol", np.full_like(src, FILL), 1)
+    red = torch.zeros(4, dtype=torch.float64, device="cuda")
+    N.box_filter(S, D, reductions=red)
+    got = D.numpy()
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    fin = np.isfinite(want)
+    assert np.array_equal(got[~fin & ~np.isnan(want)], want[~fin & ~np.isnan(want)])  # signed infinities
+    tol = 1e-13 * _local_abs(src) + 1e-300
+    assert (np.abs(got[fin] - want[fin]) <= tol[fin]).all(), float(np.max(np.abs(got[fin] - want[fin]) / tol[fin]))
+    if kind != "special":
+        r = red.cpu().numpy()  # dst's ghost cells (FILL) are part of the ghost-inclusive reductions
+        assert r[1] == O.reduce_field(got, 1, "max") and r[2] == O.reduce_field(got, 1, "min")
+        assert abs(r[0] - O.reduce_field(got, 1, "sum")) <= 1e-13 * np.abs(got).sum()
+        assert abs(r[3] - O.reduce_field(got, 1, "norm")) <= 1e-13 * O.reduce_field(got, 1, "norm")
+
+
+def test_box_filter_is_the_deep_chain_filter():
+    # nebo_box_filter on the chain's `out` gives the chain's own `filt` bit for bit
+    n = (40, 24, 18)
+    a, b, c, pts = W.deep_inputs(n)
+    A = N.Field.from_numpy("SVol", a, 1)
+    B = N.Field.from_numpy("XVol", b, 1)
+    C = N.Field.from_numpy("XVol", c, 1)
+    out, filt = N.Field("XVol", n, 1), N.Field("XVol", n, 1)
+    words = N.mask_from_points(N.mask_words(out.glob), out.glob, 1, pts)
+    N.deep_chain(A, B, C, words, out, filt)
+    f2 = N.Field("XVol", n, 1)
+    N.box_filter(out, f2)
+    assert np.array_equal(filt.numpy().view(np.uint64), f2.numpy().view(np.uint64))
