@@ -320,6 +320,165 @@ __global__ void __launch_bounds__(BX* BY, 3) heat_step_f32_async_kernel(const fl
   cp_async_wait<0>();
 }
 
+// FP32 heat step on packed pairs (the 8-byte-aligned case).  Each thread owns two x-adjacent
+// cells in two rows (a 2 x 2 block; 256 threads cover the same 32 x 32 tile and the same ring
+// of NS stages as heat_step_f32_async_kernel).  The cells x, x+1 (x even) and their x
+// neighbours x-1, x+2 are the two aligned pairs A = (x-1, x) and B = (x+1, x+2) of the stage
+// row, so two 8-byte loads per field bring all four, and every flux, difference and update runs
+// as one packed FP32x2 instruction for both cells (a - b as fma(b, -1, a), exact).  The next
+// plane's pairs are loaded one iteration ahead and become the centre plane's.  Same arithmetic
+// per cell as the scalar kernel: F = (la + lb)(tb - ta) per face,
+//   T' = T + w0 (Fx+ - Fx-) + w1 (Fy+ - Fy-) + w2 (Fz+ - Fz-).
+constexpr int QX = 16, QY = 16, QCPT = 2;  // pair-columns, thread rows, rows per thread (32 x 32 tile)
+static_assert(2 * QX == BX && QY * QCPT == FTY, "the packed kernel shares the scalar kernel's tile");
+
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 pflux(float2 la, float2 lb, float2 ta, float2 tb) {
+  return __fmul2_rn(__fadd2_rn(la, lb), psub(tb, ta));
+}
+
+__global__ void __launch_bounds__(QX* QY, 3) heat_step_f32x2_kernel(const float* __restrict__ tin,
+                                                                   float* __restrict__ tout,
+                                                                   const float* __restrict__ lam, int sy, long sz,
+                                                                   int nx, int ny, int nz, int zchunk, float w0,
+                                                                   float w1, float w2) {
+  constexpr int PLANE = HX * HY;                  // floats per stage and field
+  constexpr int UNITS = (HX / 2) * HY;            // 8-byte pairs per plane and field
+  constexpr int NT = QX * QY;
+  constexpr int NCOPY = (UNITS + NT - 1) / NT;
+  __shared__ __align__(16) float sT[NS * PLANE];
+  __shared__ __align__(16) float sL[NS * PLANE];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * QX + tx;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * FTY;
+  const int z0 = blockIdx.z * zchunk;  // a multiple of NS
+  const int z1 = min(z0 + zchunk, nz);
+  int goff[NCOPY];
+  uint32_t soff[NCOPY];
+#pragma unroll
+  for (int j = 0; j < NCOPY; ++j) {
+    const int k = min(tid + j * NT, UNITS - 1);
+    const int r = k / (HX / 2), c = 2 * (k - r * (HX / 2));
+    goff[j] = min(x0 - 1 + c, nx - 1) + sy * min(y0 - 1 + r, ny);
+    soff[j] = (uint32_t)((r * HX + c) * sizeof(float));
+  }
+  const bool last_slot = tid + (NCOPY - 1) * NT < UNITS;
+  const uint32_t sT0 = (uint32_t)__cvta_generic_to_shared(sT), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
+  auto issue = [&](int p, int st) {
+    if (p <= z1) {
+      const uint32_t so = (uint32_t)st * (PLANE * sizeof(float));
+      const float* tp = tin + sz * p;
+      const float* lp = lam + sz * p;
+#pragma unroll
+      for (int j = 0; j < NCOPY; ++j) {
+        if (j == NCOPY - 1 && !last_slot) break;
+        cp_async8_s(sT0 + so + soff[j], tp + goff[j]);
+        cp_async8_s(sL0 + so + soff[j], lp + goff[j]);
+      }
+    }
+  };
+  issue(z0 - 1, NS - 1);
+  cp_async_commit();
+#pragma unroll
+  for (int i = 0; i < NS - 2; ++i) {
+    issue(z0 + i, i);
+    cp_async_commit();
+  }
+  const int x = x0 + 2 * tx, yt = y0 + QCPT * ty;
+  const int rc = QCPT * ty + 1;  // stage row of the thread's first cell
+  const int pc = rc * HX + 2 * tx;  // float index of pair A of that row (cells x-1, x)
+  bool act[QCPT], edge[QCPT];
+#pragma unroll
+  for (int k = 0; k < QCPT; ++k) {
+    act[k] = x < nx && yt + k < ny;  // nx is even: x and x+1 are both inside or both outside
+    edge[k] = x == 0 || x + 1 == nx - 1 || yt + k == 0 || yt + k == ny - 1;
+  }
+  auto pair = [](const float* st, int i) { return *reinterpret_cast<const float2*>(st + i); };
+  auto centre = [](float2 a, float2 b) { return make_float2(a.y, b.x); };
+  cp_async_wait<NS - 3>();
+  __syncthreads();
+  // centre plane z0: pairs A, B of T and lambda per row; low z faces from plane z0-1
+  float2 aT[QCPT], bT[QCPT], aL[QCPT], bL[QCPT], fz[QCPT];
+  {
+    const float* T0 = sT;
+    const float* L0 = sL;
+    const float* Tm = sT + (NS - 1) * PLANE;
+    const float* Lm = sL + (NS - 1) * PLANE;
+#pragma unroll
+    for (int k = 0; k < QCPT; ++k) {
+      const int i = pc + k * HX;
+      aT[k] = pair(T0, i);
+      bT[k] = pair(T0, i + 2);
+      aL[k] = pair(L0, i);
+      bL[k] = pair(L0, i + 2);
+      const float2 tm = centre(pair(Tm, i), pair(Tm, i + 2)), lm = centre(pair(Lm, i), pair(Lm, i + 2));
+      fz[k] = pflux(lm, centre(aL[k], bL[k]), tm, centre(aT[k], bT[k]));
+    }
+  }
+  const float2 W0 = make_float2(w0, w0), W1 = make_float2(w1, w1), W2 = make_float2(w2, w2);
+  float* out = tout + (long)x + (long)sy * yt + sz * z0;
+#pragma unroll 1
+  for (int zb = z0; zb < z1; zb += NS) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      const int z = zb + i;
+      if (z >= z1) break;
+      cp_async_wait<NS - 4>();  // planes up to z+1 have landed (this thread's copies)
+      __syncthreads();          // ... and everyone's; plane z-2's stage is no longer read
+      issue(z + NS - 2, (i + NS - 2) % NS);
+      cp_async_commit();
+      const float* T0 = sT + i * PLANE;
+      const float* L0 = sL + i * PLANE;
+      const float* Tn = sT + ((i + 1) % NS) * PLANE;
+      const float* Ln = sL + ((i + 1) % NS) * PLANE;
+      const bool zedge = z == 0 || z == nz - 1;
+      // y face below the first row (from the row above the thread's block)
+      float2 fyl;
+      {
+        const int jl = pc - HX;
+        fyl = pflux(make_float2(L0[jl + 1], L0[jl + 2]), centre(aL[0], bL[0]), make_float2(T0[jl + 1], T0[jl + 2]),
+                    centre(aT[0], bT[0]));
+      }
+#pragma unroll
+      for (int k = 0; k < QCPT; ++k) {
+        const int j = pc + k * HX;
+        const float2 tc = centre(aT[k], bT[k]), lc = centre(aL[k], bL[k]);
+        // y face above row k: row k+1 of this thread (not yet advanced) or the row beyond the block
+        float2 fyh;
+        if (k + 1 < QCPT) {
+          fyh = pflux(lc, centre(aL[k + 1], bL[k + 1]), tc, centre(aT[k + 1], bT[k + 1]));
+        } else {
+          const int jh = pc + QCPT * HX;
+          fyh = pflux(lc, make_float2(L0[jh + 1], L0[jh + 2]), tc, make_float2(T0[jh + 1], T0[jh + 2]));
+        }
+        const float2 naT = pair(Tn, j), nbT = pair(Tn, j + 2), naL = pair(Ln, j), nbL = pair(Ln, j + 2);
+        const float2 fxl = pflux(aL[k], lc, aT[k], tc);  // faces x-1/2 of both cells
+        const float2 fxh = pflux(lc, bL[k], tc, bT[k]);  // faces x+1/2
+        const float2 fzh = pflux(lc, centre(naL, nbL), tc, centre(naT, nbT));
+        float2 v = __ffma2_rn(W0, psub(fxh, fxl), tc);
+        v = __ffma2_rn(W1, psub(fyh, fyl), v);
+        v = __ffma2_rn(W2, psub(fzh, fz[k]), v);
+        if (act[k]) {
+          float* o = out + (long)sy * k;
+          o[0] = v.x;
+          o[1] = v.y;
+          if (edge[k] || zedge) {
+            store_images_only(tout, sy, sz, x, yt + k, z, nx, ny, nz, v.x);
+            store_images_only(tout, sy, sz, x + 1, yt + k, z, nx, ny, nz, v.y);
+          }
+        }
+        fz[k] = fzh;
+        fyl = fyh;
+        aT[k] = naT;
+        bT[k] = nbT;
+        aL[k] = naL;
+        bL[k] = nbL;
+      }
+      out += sz;
+    }
+  }
+  cp_async_wait<0>();
+}
+
 int check_heat(const nebo_field* T, const nebo_field* To, const nebo_field* L, const char* what) {
   int rc;
   if ((rc = check_field(T, what)) || (rc = check_field(To, what)) || (rc = check_field(L, what))) return rc;
@@ -370,7 +529,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     if (!per_sm[vec]) {
       int v = 0;
       const cudaError_t e =
-          vec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<true>, BX * BY, 0)
+          vec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32x2_kernel, QX * QY, 0)
               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<false>, BX * BY, 0);
       per_sm[vec] = (e == cudaSuccess && v > 0) ? v : 1;
     }
@@ -381,9 +540,9 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     ch = (n[2] + zc - 1) / zc;
     LaunchScope ls("heat_step_f32", s);
     if (vec)
-      heat_step_f32_async_kernel<true><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
-                                                                            vin.sz, n[0], n[1], n[2], zc, p.w[0],
-                                                                            p.w[1], p.w[2]);
+      heat_step_f32x2_kernel<<<dim3(gxb, fyb, ch), dim3(QX, QY), 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz,
+                                                                        n[0], n[1], n[2], zc, p.w[0], p.w[1],
+                                                                        p.w[2]);
     else
       heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                              vin.sz, n[0], n[1], n[2], zc, p.w[0],
