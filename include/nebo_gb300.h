@@ -185,7 +185,7 @@ int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream
 /* ------------------------------------------------------------------ batched patches
  * Many independent periodic heat-equation patches (one ghost layer, scalar lambda and dt per
  * patch) advanced together: each time step is ONE persistent launch over a device patch table
- * and a work list of (patch, tile, z-chunk) items; nebo_patchset_run captures the steps in a
+ * and a work list of (patch, tile or row strip, z-chunk) items; nebo_patchset_run captures the steps in a
  * CUDA graph.  The reference advances such patches one `<<=` at a time from the caller's patch
  * loop (one gpu_assign_kernel launch per expression and patch, spatialops/NeboLhs.h:29-41).
  *   create:   shapes = 3 ints per patch (interior nx, ny, nz >= 2); allocates two FP64 state
@@ -198,9 +198,14 @@ int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream
  *             call after loading the FP64 arena.
  *   sync:     after run, make the FP64 arena `which` hold the state (FP32: widened, FP32X2:
  *             hi + lo).
- *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest (clobbers
- *             the arenas: call it before loading data).
- *   run:      `steps` steps from arena `start`; *final_arena says where the result is.
+ *   autotune: times tile widths 16/32/64 per x-extent class and keeps the fastest; in NEBO_F32
+ *             mode (row strips of up to 1024 cells, no tile width) it picks the z extent of the
+ *             work items instead (whole patch, 32 or 16 planes).  Clobbers the arenas: call it
+ *             before loading data.
+ *   run:      `steps` steps from arena `start`; *final_arena says where the result is.  In
+ *             NEBO_F32 mode the steps read their halos from the periodic sources and write no
+ *             ghost cells; the run ends by filling the ghosts of the result arena (one launch,
+ *             part of the graph), so the result is a full window as in the other modes.
  * FP64 results are bit-identical to the reference's serial walk on a constant lambda field. */
 typedef struct nebo_patchset nebo_patchset;
 int nebo_patchset_create(nebo_patchset** ps, int npatch, const int32_t* shapes, const double* lam,
