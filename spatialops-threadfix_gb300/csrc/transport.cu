@@ -52,8 +52,10 @@ __device__ __forceinline__ T face_flux(const TrArgs<T>& a, long f, long s, const
   return a.nu * il * g4 - uf * up;
 }
 
+// Cells within G of a face: the value and its periodic images (out of line: rare, and its index
+// lists live in local memory).
 template <typename T>
-__device__ __forceinline__ void store_images2(T* base, int sy, long sz, int x, int y, int z, int n, T v) {
+__device__ __noinline__ void store_images2_edge(T* base, int sy, long sz, int x, int y, int z, int n, T v) {
   int xs[3], ys[3], zs[3];
   int cx = 0, cy = 0, cz = 0;
   xs[cx++] = x;
@@ -68,6 +70,15 @@ __device__ __forceinline__ void store_images2(T* base, int sy, long sz, int x, i
   for (int k = 0; k < cz; ++k)
     for (int j = 0; j < cy; ++j)
       for (int i = 0; i < cx; ++i) base[(long)xs[i] + (long)sy * ys[j] + sz * zs[k]] = v;
+}
+
+// The value at (x, y, z) and, for cells within G of a face, its periodic images.
+template <typename T>
+__device__ __forceinline__ void store_images2(T* base, int sy, long sz, int x, int y, int z, int n, T v) {
+  if (x >= G && x < n - G && y >= G && y < n - G && z >= G && z < n - G)
+    base[(long)x + (long)sy * y + sz * z] = v;
+  else
+    store_images2_edge(base, sy, sz, x, y, z, n, v);
 }
 
 // Ask L2 to fetch the line holding p (no register, no wait): planes are requested PFZ steps of
@@ -144,6 +155,147 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_kernel(TrArgs<T> a, in
   }
 }
 
+// FP32 stage with staged planes.  phi and lambda planes (the 32 x 8 tile plus a two-cell x/y
+// halo, 36 x 12) stream through a ring of SNS shared-memory stages with 8-byte cp.async copies
+// (the row pitch is even); each thread computes both x faces and both y faces of its cell from
+// the stage, and the z faces from its column's phi window (z-1 .. z+2) carried in registers, so
+// the only global reads per cell are the face velocities and the FP64 state.  Face arithmetic as
+// face_flux.  Ring: plane p (z0 <= p <= z1+1) lives in stage (p - z0) % SNS; the prologue issues
+// planes z0 .. z0+3; iteration z waits until planes up to z+2 have landed (one group pending),
+// syncs, issues plane z+4 into the stage of plane z-1 and reads planes z, z+1, z+2.
+constexpr int SNS = 5;
+constexpr int SPW = TX + 2 * G, SPH = TY + 2 * G;  // staged tile incl. halo
+constexpr int SPLANE = SPW * SPH;
+constexpr int SUNITS = (SPW / 2) * SPH;            // 8-byte pairs per field and plane
+constexpr int SNCOPY = (2 * SUNITS + TX * TY - 1) / (TX * TY);
+
+__device__ __forceinline__ void tcp_async8(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void tcp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void tcp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// face flux from its stencil values: la, lb = lambda[f-s], lambda[f]; pm2, pm1, p0, pp1 =
+// phi[f-2s], phi[f-s], phi[f], phi[f+s]; uf = velocity[f] (the order of face_flux)
+__device__ __forceinline__ float sflux(const TrArgs<float>& a, float la, float lb, float pm2, float pm1, float p0,
+                                       float pp1, float uf) {
+  const float il = (la + lb) * 0.5f;
+  const float g4 = ((pm2 * a.q0 + pm1 * a.q1) + p0 * a.q2) + pp1 * a.q3;
+  const float up = (uf > 0.0f) ? pm1 : p0;
+  return a.nu * il * g4 - uf * up;
+}
+
+template <bool SECOND>
+__global__ void __launch_bounds__(TX* TY) transport_stage_f32_staged_kernel(TrArgs<float> a, int zchunk) {
+  __shared__ __align__(16) float sP[SNS * SPLANE];
+  __shared__ __align__(16) float sL[SNS * SPLANE];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int n = a.n, sy = a.sy;
+  const long sz = a.sz;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, n);
+  const bool active = x < n && y < n;
+  const int xc = min(x, n), yc = min(y, n);  // column/row n is a ghost: valid memory
+  // copy slots: unit u < 2 SUNITS (phi, then lambda) -> tile row r, column pair c (clamped to
+  // the window: pairs start at most at column n, rows at most n + 1)
+  int goff[SNCOPY];
+  uint32_t soff[SNCOPY];
+  bool lamf[SNCOPY];
+  const uint32_t sP0 = (uint32_t)__cvta_generic_to_shared(sP), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
+#pragma unroll
+  for (int j = 0; j < SNCOPY; ++j) {
+    const int u = min(tid + j * TX * TY, 2 * SUNITS - 1);
+    lamf[j] = u >= SUNITS;
+    const int k = lamf[j] ? u - SUNITS : u;
+    const int r = k / (SPW / 2), c = 2 * (k - r * (SPW / 2));
+    goff[j] = min(x0 - G + c, n) + sy * min(y0 - G + r, n + 1);
+    soff[j] = (lamf[j] ? sL0 : sP0) + (uint32_t)((r * SPW + c) * sizeof(float));
+  }
+  const bool last_slot = tid + (SNCOPY - 1) * TX * TY < 2 * SUNITS;
+  auto issue = [&](int p, int st) {
+    if (p <= z1 + 1) {
+      const float* pp = a.phi + sz * p;
+      const float* lp = a.lam + sz * p;
+      const uint32_t so = (uint32_t)st * (SPLANE * sizeof(float));
+#pragma unroll
+      for (int j = 0; j < SNCOPY; ++j) {
+        if (j == SNCOPY - 1 && !last_slot) break;
+        tcp_async8(soff[j] + so, (lamf[j] ? lp : pp) + goff[j]);
+      }
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < SNS - 1; ++i) {
+    issue(z0 + i, i);
+    tcp_commit();
+  }
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+  // the column's phi window and the low z face of plane z0, from global memory
+  const long c0 = at(xc, yc, z0);
+  float pm1 = __ldg(a.phi + c0 - sz), p0 = __ldg(a.phi + c0), p1 = __ldg(a.phi + c0 + sz);
+  float fzlo = face_flux(a, c0, sz, a.w);
+  const int ci = (ty + G) * SPW + tx + G;
+  // this column's global values of plane z (velocities on its faces, the FP64 state), loaded one
+  // plane ahead so their latency overlaps the previous plane's work
+  struct Col {
+    float ul, uh, vl, vh, wh;
+    double acc, base;
+  };
+  auto load_col = [&](int z) {
+    Col q;
+    const long c = at(xc, yc, z);
+    q.ul = __ldg(a.u + c);
+    q.uh = __ldg(a.u + c + 1);
+    q.vl = __ldg(a.v + c);
+    q.vh = __ldg(a.v + c + sy);
+    q.wh = __ldg(a.w + c + sz);
+    q.acc = a.acc[c];
+    q.base = SECOND ? a.base[c] : 0.0;
+    return q;
+  };
+  Col cur = load_col(z0);
+  for (int z = z0; z < z1; ++z) {
+    const int i = z - z0;
+    const Col nxt = load_col(min(z + 1, n));  // plane n is a ghost plane: valid memory
+    tcp_wait<1>();
+    __syncthreads();
+    issue(z + SNS - 1, (i + SNS - 1) % SNS);
+    tcp_commit();
+    const float* P0 = sP + (i % SNS) * SPLANE;
+    const float* L0 = sL + (i % SNS) * SPLANE;
+    const float* L1 = sL + ((i + 1) % SNS) * SPLANE;
+    const float* P2 = sP + ((i + 2) % SNS) * SPLANE;
+    const long c = at(xc, yc, z);
+    const float p2 = P2[ci], l0 = L0[ci], l1 = L1[ci];
+    const float xm2 = P0[ci - 2], xm1 = P0[ci - 1], xp1 = P0[ci + 1], xp2 = P0[ci + 2];
+    const float ym2 = P0[ci - 2 * SPW], ym1 = P0[ci - SPW], yp1 = P0[ci + SPW], yp2 = P0[ci + 2 * SPW];
+    const float fxl = sflux(a, L0[ci - 1], l0, xm2, xm1, p0, xp1, cur.ul);
+    const float fxh = sflux(a, l0, L0[ci + 1], xm1, p0, xp1, xp2, cur.uh);
+    const float fyl = sflux(a, L0[ci - SPW], l0, ym2, ym1, p0, yp1, cur.vl);
+    const float fyh = sflux(a, l0, L0[ci + SPW], ym1, p0, yp1, yp2, cur.vh);
+    const float fzh = sflux(a, l0, l1, pm1, p0, p1, p2, cur.wh);
+    if (active) {
+      const float rhs = ((fxh - fxl) + (fyh - fyl)) + (fzh - fzlo);
+      const double rd = fixmath::f32_to_f64(rhs);
+      double r;
+      if (!SECOND)
+        r = cur.acc + a.dt * rd;
+      else
+        r = 0.5 * cur.base + 0.5 * (cur.acc + a.dt * rd);
+      a.out64[c] = r;
+      store_images2(a.outS, sy, sz, x, y, z, n, fixmath::f64_to_f32_rn(r));
+    }
+    fzlo = fzh;
+    pm1 = p0;
+    p0 = p1;
+    p1 = p2;
+    cur = nxt;
+  }
+  tcp_wait<0>();
+}
+
 __global__ void cast_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = fixmath::f64_to_f32_rn(a[i]);
@@ -166,6 +318,16 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   chunks = (n + zchunk - 1) / zchunk;
   dim3 grid(gxb, gyb, chunks), block(TX, TY);
   LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
+  if constexpr (sizeof(T) == 4) {
+    if (a.sy % 2 == 0) {  // even pitch: 8-byte plane copies
+      if (second)
+        transport_stage_f32_staged_kernel<true><<<grid, block, 0, s>>>(a, zchunk);
+      else
+        transport_stage_f32_staged_kernel<false><<<grid, block, 0, s>>>(a, zchunk);
+      NEBO_LAUNCH_CHECK("nebo_transport_run");
+      return NEBO_OK;
+    }
+  }
   if (second)
     transport_stage_kernel<T, true><<<grid, block, 0, s>>>(a, zchunk);
   else
