@@ -30,6 +30,8 @@ namespace {
 constexpr int FX = 32;  // filter tile x
 constexpr int FY = 8;   // filter tile y
 
+// A thread walks z in steps of gridDim.z; the loads of its next cell (the four a values, b, c
+// and the mask word) are issued one step ahead, so their latency overlaps this cell's exp/sin.
 __global__ void __launch_bounds__(256) deep_out_kernel(const double* __restrict__ a, const double* __restrict__ b,
                                                        const double* __restrict__ c, const uint32_t* __restrict__ mask,
                                                        long mask_base, double* __restrict__ out, int sy, long sz,
@@ -38,17 +40,40 @@ __global__ void __launch_bounds__(256) deep_out_kernel(const double* __restrict_
   const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int y = -1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   if (x >= nx || y > ny) return;
-  for (int z = -1 + (int)blockIdx.z; z <= nz; z += gridDim.z) {
-    const long i = (long)x + (long)sy * y + sz * z;
+  const int zs = gridDim.z;
+  const long row = (long)x + (long)sy * y;
+  struct Cell {
+    double am2, am1, a0, ap1, b, c;
+    uint32_t w;
+  };
+  auto load = [&](int z) {
+    Cell v;
+    const long i = row + sz * z;
     const long bit = mask_base + i;  // flat index in the window
+    v.w = __ldg(mask + (bit >> 5)) >> (bit & 31);
+    v.am2 = __ldg(a + i - 2);
+    v.am1 = __ldg(a + i - 1);
+    v.a0 = __ldg(a + i);
+    v.ap1 = __ldg(a + i + 1);
+    v.b = __ldg(b + i);
+    v.c = __ldg(c + i);
+    return v;
+  };
+  int z = -1 + (int)blockIdx.z;
+  if (z > nz) return;
+  Cell cur = load(z);
+  for (; z <= nz; z += zs) {
+    const int zn = z + zs;
+    const Cell nxt = load(zn <= nz ? zn : z);  // the last step reloads its own cell
     double v;
-    if ((__ldg(mask + (bit >> 5)) >> (bit & 31)) & 1u) {
+    if (cur.w & 1u) {
       v = 0.0;
     } else {
-      const double igi = q * ((__ldg(a + i + 1) - __ldg(a + i - 1)) + (__ldg(a + i) - __ldg(a + i - 2)));
-      v = fma(igi, fixmath::exp_i(__ldg(b + i)), fixmath::sin_i(__ldg(c + i)));
+      const double igi = q * ((cur.ap1 - cur.am1) + (cur.a0 - cur.am2));
+      v = fma(igi, fixmath::exp_i(cur.b), fixmath::sin_i(cur.c));
     }
-    out[i] = v;
+    out[row + sz * z] = v;
+    cur = nxt;
   }
 }
 
