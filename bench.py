@@ -159,7 +159,7 @@ class Deep:
         self.filt = N.Field("XVol", n, 1)
         self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
         self.cells = n ** 3
-        self.launches_per_step = 4  # chain, filter + reductions, ghost-shell reductions, final
+        self.launches_per_step = 2  # chain; filter with the four reductions (ghost shell and final merge in the same grid)
         self.label = f"deep chain {n}^3 + 1 ghost (a SVol; b, c, out, filt XVol; 5% + boundary mask), filter + 4 reductions"
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
         self.d2h_bytes = 4 * 8

@@ -84,6 +84,87 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+struct ShellArgs {
+  int on;              // 1: the shell is not empty
+  const double* base;  // filt's allocation
+  int gx;
+  long gxy;
+  int lx, hx, ly, hy, lz, hz;        // reduction box [lo, hi) (glob coordinates)
+  int ix0, ix1, iy0, iy1, iz0, iz1;  // the filter's written box, excluded
+};
+
+// The four reductions over the cells of box [lo, hi) that are not in the box [ilo, ihi): the
+// valid ghost cells of `filt`, which the filter does not write but nebo_sum/max/min/norm
+// include.  Two parts: the rows entirely outside the inner box (planes z outside it, and rows y
+// outside it within the inner z range), a warp per row; and the x ends of the rows that cross
+// the inner box, a thread per cell.  Block sb of nsb, 256 threads (tid linear).
+__device__ __forceinline__ void shell_part(Acc4& acc, const ShellArgs& sa, int sb, int nsb, int tid) {
+  const int lane = tid & 31;
+  const int nyr = sa.hy - sa.ly;
+  const int zout = (sa.iz0 - sa.lz) + (sa.hz - sa.iz1);        // planes outside the inner z range
+  const int yout = (sa.iy0 - sa.ly) + (sa.hy - sa.iy1);        // rows per inner plane outside in y
+  const int nfull = zout * nyr + (sa.iz1 - sa.iz0) * yout;
+  for (int r = sb * 8 + (tid >> 5); r < nfull; r += nsb * 8) {
+    int y, z;
+    if (r < zout * nyr) {
+      const int pz = r / nyr;
+      z = pz < sa.iz0 - sa.lz ? sa.lz + pz : sa.iz1 + (pz - (sa.iz0 - sa.lz));
+      y = sa.ly + r % nyr;
+    } else {
+      const int t = r - zout * nyr, py = t % yout;
+      z = sa.iz0 + t / yout;
+      y = py < sa.iy0 - sa.ly ? sa.ly + py : sa.iy1 + (py - (sa.iy0 - sa.ly));
+    }
+    const double* row = sa.base + (long)sa.gx * y + sa.gxy * z;
+    for (int xx = sa.lx + lane; xx < sa.hx; xx += 32) acc4_add(acc, __ldg(row + xx));
+  }
+  const int xout = (sa.ix0 - sa.lx) + (sa.hx - sa.ix1);
+  const long nedge = (long)(sa.iz1 - sa.iz0) * (sa.iy1 - sa.iy0) * xout;
+  for (long e = sb * 256L + tid; e < nedge; e += nsb * 256L) {
+    const int px = (int)(e % xout);
+    const long rr = e / xout;
+    const int y = sa.iy0 + (int)(rr % (sa.iy1 - sa.iy0)), z = sa.iz0 + (int)(rr / (sa.iy1 - sa.iy0));
+    const int xx = px < sa.ix0 - sa.lx ? sa.lx + px : sa.ix1 + (px - (sa.ix0 - sa.lx));
+    acc4_add(acc, __ldg(sa.base + xx + (long)sa.gx * y + sa.gxy * z));
+  }
+}
+
+// Writes this block's partial; the last block to do so merges all n partials into out4
+// ({sum, max, min, norm}) and resets the ticket.  No block waits for another: each fences its
+// partial before taking a ticket, and only the holder of the last ticket reads them all.
+__device__ __forceinline__ void partial_and_finish(Acc4 acc, Acc4* partials, int idx, int n, unsigned* ticket,
+                                                   double* out4, int tid, int nthreads) {
+  __shared__ bool last;
+  acc = block_reduce4(acc);
+  if (tid == 0) {
+    partials[idx] = acc;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == (unsigned)(n - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  Acc4 a = acc4_identity();
+  for (int i = tid; i < n; i += nthreads) {
+    const Acc4* q = partials + i;  // written by other blocks: read through L2
+    Acc4 b;
+    b.s = __ldcg(&q->s);
+    b.sc = __ldcg(&q->sc);
+    b.q = __ldcg(&q->q);
+    b.qc = __ldcg(&q->qc);
+    b.mx = __ldcg(&q->mx);
+    b.mn = __ldcg(&q->mn);
+    merge4(a, b);
+  }
+  a = block_reduce4(a);
+  if (tid == 0) {
+    out4[0] = a.s + a.sc;
+    out4[1] = a.mx == LLONG_MIN ? -INFINITY : from_key(a.mx);
+    out4[2] = a.mn == LLONG_MAX ? INFINITY : from_key(a.mn);
+    out4[3] = sqrt(a.q + a.qc);
+  }
+}
+
 constexpr int FNS = 5;   // filter ring stages
 constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns two y-adjacent cells)
 
@@ -107,10 +188,13 @@ constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns 
 // roundings, against the reference's 27 roundings of up to 2^-53 of the running sum.  A plane
 // holding an infinity or NaN, or only values below 2^-893 (all-zero planes included), sums in
 // FP64 instead (the adds of the reference, reassociated).
+// With RED every block also reduces a share of filt's ghost shell (shell_part) after its tile,
+// leaves its partial, and the last block merges them into out4.
 template <bool RED>
 __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
                                                             int sy, long sz, int nx, int ny, int nz, int zchunk,
-                                                            Acc4* __restrict__ partials) {
+                                                            Acc4* __restrict__ partials, ShellArgs sa,
+                                                            unsigned* __restrict__ ticket, double* __restrict__ out4) {
   constexpr int PW = FX + 2, PH = FTY + 2, PLANE = PW * PH;
   constexpr int NCOPY = (PLANE + FX * FY - 1) / (FX * FY);
   constexpr int XTASKS = PH * (FX / 2);  // x-sum pairs per plane
@@ -238,51 +322,11 @@ __global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __rest
   }
   cp_async_wait<0>();
   if (RED) {
-    acc = block_reduce4(acc);
-    if (tid == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = acc;
+    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    if (sa.on) shell_part(acc, sa, b, nb, tid);
+    partial_and_finish(acc, partials, b, nb, ticket, out4, tid, FX * FY);
   }
-}
-
-// The four reductions over the cells of box [lo, hi) that are not in the box [ilo, ihi) (glob
-// coordinates): the valid ghost cells of `filt`, which the filter does not write but
-// nebo_sum/max/min/norm include.  Two parts: the rows entirely outside the inner box (planes
-// z outside it, and rows y outside it within the inner z range), a warp per row; and the x ends
-// of the rows that cross the inner box, a thread per cell.
-__global__ void __launch_bounds__(256) shell_reduce_kernel(const double* __restrict__ base, int gx, long gxy, int lx,
-                                                           int hx, int ly, int hy, int lz, int hz, int ix0, int ix1,
-                                                           int iy0, int iy1, int iz0, int iz1,
-                                                           Acc4* __restrict__ partials) {
-  Acc4 acc = acc4_identity();
-  const int lane = threadIdx.x & 31;
-  const int nyr = hy - ly;
-  const int zout = (iz0 - lz) + (hz - iz1);                   // planes outside the inner z range
-  const int yout = (iy0 - ly) + (hy - iy1);                   // rows per inner plane outside in y
-  const int nfull = zout * nyr + (iz1 - iz0) * yout;
-  for (int r = blockIdx.x * 8 + (threadIdx.x >> 5); r < nfull; r += gridDim.x * 8) {
-    int y, z;
-    if (r < zout * nyr) {
-      const int pz = r / nyr;
-      z = pz < iz0 - lz ? lz + pz : iz1 + (pz - (iz0 - lz));
-      y = ly + r % nyr;
-    } else {
-      const int t = r - zout * nyr, py = t % yout;
-      z = iz0 + t / yout;
-      y = py < iy0 - ly ? ly + py : iy1 + (py - (iy0 - ly));
-    }
-    const double* row = base + (long)gx * y + gxy * z;
-    for (int xx = lx + lane; xx < hx; xx += 32) acc4_add(acc, __ldg(row + xx));
-  }
-  const int xout = (ix0 - lx) + (hx - ix1);
-  const long nedge = (long)(iz1 - iz0) * (iy1 - iy0) * xout;
-  for (long e = blockIdx.x * 256L + threadIdx.x; e < nedge; e += gridDim.x * 256L) {
-    const int px = (int)(e % xout);
-    const long rr = e / xout;
-    const int y = iy0 + (int)(rr % (iy1 - iy0)), z = iz0 + (int)(rr / (iy1 - iy0));
-    const int xx = px < ix0 - lx ? lx + px : ix1 + (px - (ix0 - lx));
-    acc4_add(acc, __ldg(base + xx + (long)gx * y + gxy * z));
-  }
-  acc = block_reduce4(acc);
-  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
 int check_deep(const nebo_field* a, const nebo_field* b, const nebo_field* c, const nebo_field* out,
@@ -364,11 +408,10 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
   int chunks = std::max(1, std::min(num_sms() * per_sm[reduce] / (gxb * gyb), (n[2] + 7) / 8));
   const int zchunk = (n[2] + chunks - 1) / chunks;
   chunks = (n[2] + zchunk - 1) / zchunk;
-  const int fblocks = gxb * gyb * chunks;
   if (!reduce) {
     LaunchScope ls("box_filter", s);
-    box_filter_kernel<false><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0],
-                                                                            n[1], n[2], zchunk, nullptr);
+    box_filter_kernel<false><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(
+        vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], zchunk, nullptr, ShellArgs{}, nullptr, nullptr);
     NEBO_LAUNCH_CHECK(what);
     return NEBO_OK;
   }
@@ -381,28 +424,24 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
   }
   const bool shell = lo[0] != ilo[0] || hi[0] != ihi[0] || lo[1] != ilo[1] || hi[1] != ihi[1] || lo[2] != ilo[2] ||
                      hi[2] != ihi[2];
-  const int sblocks = shell ? num_sms() * 2 : 0;
-  Acc4* partials = nullptr;
+  const ShellArgs sa{shell ? 1 : 0, (const double*)filt->data, filt->glob[0], (long)filt->glob[0] * filt->glob[1],
+                     lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], ilo[0], ihi[0], ilo[1], ihi[1], ilo[2], ihi[2]};
+  const long nblocks = (long)gxb * gyb * chunks;
+  // one allocation: the partials, then the ticket
+  const size_t pbytes = sizeof(Acc4) * nblocks;
+  char* scratch = nullptr;
   pool_retain();
-  NEBO_CUDA_TRY(cudaMallocAsync((void**)&partials, sizeof(Acc4) * (fblocks + sblocks), s));
-  {
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&scratch, pbytes + 16, s));
+  Acc4* partials = (Acc4*)scratch;
+  unsigned* ticket = (unsigned*)(scratch + pbytes);
+  cudaError_t le = cudaMemsetAsync(ticket, 0, sizeof(unsigned), s);
+  if (le == cudaSuccess) {
     LaunchScope ls("box_filter_reduce", s);
-    box_filter_kernel<true><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0],
-                                                                           n[1], n[2], zchunk, partials);
+    box_filter_kernel<true><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(
+        vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], zchunk, partials, sa, ticket, d_out4);
+    le = cudaGetLastError();
   }
-  if (shell) {
-    LaunchScope ls("shell_reduce", s);
-    shell_reduce_kernel<<<sblocks, 256, 0, s>>>((const double*)filt->data, filt->glob[0],
-                                                (long)filt->glob[0] * filt->glob[1], lo[0], hi[0], lo[1], hi[1], lo[2],
-                                                hi[2], ilo[0], ihi[0], ilo[1], ihi[1], ilo[2], ihi[2],
-                                                partials + fblocks);
-  }
-  {
-    LaunchScope ls("reduce4_final", s);
-    reduce4_final_kernel<<<1, 256, 0, s>>>(partials, fblocks + sblocks, d_out4);
-  }
-  cudaError_t le = cudaGetLastError();
-  cudaFreeAsync(partials, s);
+  cudaFreeAsync(scratch, s);
   if (le != cudaSuccess) return cuda_fail(le, what);
   return NEBO_OK;
 }
