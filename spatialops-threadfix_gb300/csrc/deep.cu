@@ -191,7 +191,7 @@ constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns 
 // With RED every block also reduces a share of filt's ghost shell (shell_part) after its tile,
 // leaves its partial, and the last block merges them into out4.
 template <bool RED>
-__global__ void __launch_bounds__(FX* FY) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
+__global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
                                                             int sy, long sz, int nx, int ny, int nz, int zchunk,
                                                             Acc4* __restrict__ partials, ShellArgs sa,
                                                             unsigned* __restrict__ ticket, double* __restrict__ out4) {
