@@ -19,6 +19,7 @@
 // points separably (x, then y from shared memory, then z from registers while marching in z),
 // optionally folding the four reductions of filt into the same pass.
 #include <algorithm>
+#include <cmath>
 
 #include "common.cuh"
 #include "fp64_int.cuh"
@@ -188,12 +189,15 @@ constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns 
 // roundings, against the reference's 27 roundings of up to 2^-53 of the running sum.  A plane
 // holding an infinity or NaN, or only values below 2^-893 (all-zero planes included), sums in
 // FP64 instead (the adds of the reference, reassociated).
-// With RED every block also reduces a share of filt's ghost shell (shell_part) after its tile,
+// Work split: the output planes of all FX x FTY tiles in a flat order (tile-major, z innermost);
+// block b of gridDim.x takes the range [b total / gridDim.x, (b+1) total / gridDim.x), one or
+// more z runs of consecutive tiles, so every resident block gets the same number of planes.
+// With RED every block also reduces a share of filt's ghost shell (shell_part) after its runs,
 // leaves its partial, and the last block merges them into out4.
 template <bool RED>
 __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __restrict__ src, double* __restrict__ dst,
-                                                            int sy, long sz, int nx, int ny, int nz, int zchunk,
-                                                            Acc4* __restrict__ partials, ShellArgs sa,
+                                                            int sy, long sz, int nx, int ny, int nz, int tiles_x,
+                                                            long total, Acc4* __restrict__ partials, ShellArgs sa,
                                                             unsigned* __restrict__ ticket, double* __restrict__ out4) {
   constexpr int PW = FX + 2, PH = FTY + 2, PLANE = PW * PH;
   constexpr int NCOPY = (PLANE + FX * FY - 1) / (FX * FY);
@@ -203,129 +207,135 @@ __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __r
   __shared__ fixmath::fix128 rows[PH * FX];  // fixed-point x-sums (or FP64 bits on a special plane)
   __shared__ unsigned plane_exp[2];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
-  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FTY;
-  const int x = x0 + tx, ya = y0 + 2 * ty;
-  const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, nz);
-  int goff[NCOPY];  // within a plane (fewer than 2^31 cells)
-  uint32_t soff[NCOPY];
-#pragma unroll
-  for (int j = 0; j < NCOPY; ++j) {
-    const int k = min(tid + j * FX * FY, PLANE - 1);
-    const int r = k / PW, c = k - r * PW;
-    goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
-    soff[j] = (uint32_t)(k * sizeof(double));
-  }
-  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(ring);
-  auto issue = [&](int p) {
-    if (p > z1) return;
-    const uint32_t st = ring0 + (uint32_t)((p + 1) % FNS) * (PLANE * sizeof(double));
-    const double* sp = src + sz * p;
+  const int lane = tid & 31;
+  // total < 2^31 (checked by the host)
+  const int beg = (int)((long)blockIdx.x * total / gridDim.x), end = (int)((long)(blockIdx.x + 1) * total / gridDim.x);
+  Acc4 acc = acc4_identity();
+#pragma unroll 1
+  for (int run = beg; run < end;) {
+    const int tile = run / nz;
+    const int x0 = (tile % tiles_x) * FX, y0 = (tile / tiles_x) * FTY;
+    const int x = x0 + tx, ya = y0 + 2 * ty;
+    const int z0 = run - tile * nz, z1 = min(nz, z0 + (end - run));
+    run += z1 - z0;
+    int goff[NCOPY];  // within a plane (fewer than 2^31 cells)
+    uint32_t soff[NCOPY];
 #pragma unroll
     for (int j = 0; j < NCOPY; ++j) {
-      if (j == NCOPY - 1 && tid + j * FX * FY >= PLANE) break;
-      cp_async8(st + soff[j], sp + goff[j]);
+      const int k = min(tid + j * FX * FY, PLANE - 1);
+      const int r = k / PW, c = k - r * PW;
+      goff[j] = min(x0 - 1 + c, nx) + sy * min(y0 - 1 + r, ny);
+      soff[j] = (uint32_t)(k * sizeof(double));
     }
-  };
-  if (tid < 2) plane_exp[tid] = 0u;
-#pragma unroll 1
-  for (int i = 0; i < FNS - 1; ++i) {
-    issue(z0 - 1 + i);
-    cp_async_commit();
-  }
-  const bool act0 = x < nx && ya < ny, act1 = x < nx && ya + 1 < ny;
-  // 2-D sums of planes p-2 (p*) and p-1 (c*) for both cells: fixed-point integers in units of
-  // 2^u*, or FP64 bits when the plane was special (sp*)
-  fixmath::fix128 p0 = 0, c0 = 0, p1 = 0, c1 = 0;
-  int up = 0, uc = 0;
-  bool spp = false, spc = false;
-  Acc4 acc = acc4_identity();
-  double* out = dst + (long)x + (long)sy * ya + sz * (z0 - 1);
-  const int lane = tid & 31;
-#pragma unroll 1
-  for (int p = z0 - 1; p <= z1; ++p, out += sz) {
-    cp_async_wait<FNS - 2>();
-    __syncthreads();
-    issue(p + FNS - 1);
-    cp_async_commit();
-    const double* pl = ring + ((p + 1) % FNS) * PLANE;
-    // the plane's largest biased exponent; this thread's values stay in registers
-    constexpr int PER = (PLANE + FX * FY - 1) / (FX * FY);
-    double val[PER];
-    unsigned e = 0;
+    const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(ring);
+    auto issue = [&](int p) {
+      if (p > z1) return;
+      const uint32_t st = ring0 + (uint32_t)((p + 1) % FNS) * (PLANE * sizeof(double));
+      const double* sp = src + sz * p;
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int t = tid + j * FX * FY;
-      val[j] = t < PLANE ? pl[t] : 0.0;
-      e = max(e, ((unsigned)__double2hiint(val[j]) >> 20) & 0x7ffu);
+      for (int j = 0; j < NCOPY; ++j) {
+        if (j == NCOPY - 1 && tid + j * FX * FY >= PLANE) break;
+        cp_async8(st + soff[j], sp + goff[j]);
+      }
+    };
+    if (tid < 2) plane_exp[tid] = 0u;
+#pragma unroll 1
+    for (int i = 0; i < FNS - 1; ++i) {
+      issue(z0 - 1 + i);
+      cp_async_commit();
     }
-    e = __reduce_max_sync(0xffffffffu, e);
-    if (lane == 0) atomicMax(&plane_exp[p & 1], e);
-    __syncthreads();
-    const int E = (int)plane_exp[p & 1];
-    if (tid == 0) plane_exp[(p + 1) & 1] = 0u;  // the slot of plane p+1 (last read in iteration p-1)
-    const bool special = E == 0x7ff || E < 130;
-    const int u = E - 1144;
-    if (!special) {
+    const bool act0 = x < nx && ya < ny, act1 = x < nx && ya + 1 < ny;
+    // 2-D sums of planes p-2 (p*) and p-1 (c*) for both cells: fixed-point integers in units of
+    // 2^u*, or FP64 bits when the plane was special (sp*)
+    fixmath::fix128 p0 = 0, c0 = 0, p1 = 0, c1 = 0;
+    int up = 0, uc = 0;
+    bool spp = false, spc = false;
+    double* out = dst + (long)x + (long)sy * ya + sz * (z0 - 1);
+#pragma unroll 1
+    for (int p = z0 - 1; p <= z1; ++p, out += sz) {
+      cp_async_wait<FNS - 2>();
+      __syncthreads();
+      issue(p + FNS - 1);
+      cp_async_commit();
+      const double* pl = ring + ((p + 1) % FNS) * PLANE;
+      // the plane's largest biased exponent; this thread's values stay in registers
+      constexpr int PER = (PLANE + FX * FY - 1) / (FX * FY);
+      double val[PER];
+      unsigned e = 0;
 #pragma unroll
       for (int j = 0; j < PER; ++j) {
         const int t = tid + j * FX * FY;
-        if (t < PLANE) fplane[t] = fixmath::to_units(val[j], E);
+        val[j] = t < PLANE ? pl[t] : 0.0;
+        e = max(e, ((unsigned)__double2hiint(val[j]) >> 20) & 0x7ffu);
+      }
+      e = __reduce_max_sync(0xffffffffu, e);
+      if (lane == 0) atomicMax(&plane_exp[p & 1], e);
+      __syncthreads();
+      const int E = (int)plane_exp[p & 1];
+      if (tid == 0) plane_exp[(p + 1) & 1] = 0u;  // the slot of plane p+1 (last read in iteration p-1)
+      const bool special = E == 0x7ff || E < 130;
+      const int u = E - 1144;
+      if (!special) {
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+          const int t = tid + j * FX * FY;
+          if (t < PLANE) fplane[t] = fixmath::to_units(val[j], E);
+        }
+        __syncthreads();
+      }
+      for (int t = tid; t < XTASKS; t += FX * FY) {
+        const int r = t / (FX / 2), c = 2 * (t % (FX / 2));
+        if (!special) {
+          const fixmath::fix128* f = fplane + r * PW + c;
+          const fixmath::fix128 mid = f[1] + f[2];
+          rows[r * FX + c] = f[0] + mid;
+          rows[r * FX + c + 1] = mid + f[3];
+        } else {
+          const double* q = pl + r * PW + c;
+          const double mid = q[1] + q[2];
+          rows[r * FX + c] = __double_as_longlong(q[0] + mid);
+          rows[r * FX + c + 1] = __double_as_longlong(mid + q[3]);
+        }
       }
       __syncthreads();
-    }
-    for (int t = tid; t < XTASKS; t += FX * FY) {
-      const int r = t / (FX / 2), c = 2 * (t % (FX / 2));
+      const fixmath::fix128* col = rows + 2 * ty * FX + tx;
+      fixmath::fix128 s0, s1;
       if (!special) {
-        const fixmath::fix128* f = fplane + r * PW + c;
-        const fixmath::fix128 mid = f[1] + f[2];
-        rows[r * FX + c] = f[0] + mid;
-        rows[r * FX + c + 1] = mid + f[3];
+        const fixmath::fix128 mid = col[FX] + col[2 * FX];
+        s0 = col[0] + mid;
+        s1 = mid + col[3 * FX];
       } else {
-        const double* q = pl + r * PW + c;
-        const double mid = q[1] + q[2];
-        rows[r * FX + c] = __double_as_longlong(q[0] + mid);
-        rows[r * FX + c + 1] = __double_as_longlong(mid + q[3]);
+        const double mid = __longlong_as_double((long long)col[FX]) + __longlong_as_double((long long)col[2 * FX]);
+        s0 = __double_as_longlong(__longlong_as_double((long long)col[0]) + mid);
+        s1 = __double_as_longlong(mid + __longlong_as_double((long long)col[3 * FX]));
       }
-    }
-    __syncthreads();
-    const fixmath::fix128* col = rows + 2 * ty * FX + tx;
-    fixmath::fix128 s0, s1;
-    if (!special) {
-      const fixmath::fix128 mid = col[FX] + col[2 * FX];
-      s0 = col[0] + mid;
-      s1 = mid + col[3 * FX];
-    } else {
-      const double mid = __longlong_as_double((long long)col[FX]) + __longlong_as_double((long long)col[2 * FX]);
-      s0 = __double_as_longlong(__longlong_as_double((long long)col[0]) + mid);
-      s1 = __double_as_longlong(mid + __longlong_as_double((long long)col[3 * FX]));
-    }
-    if (p >= z0 + 1) {
-      if (act0) {
-        const double v = fixmath::box27(p0, up, spp, c0, uc, spc, s0, u, special);
-        out[-sz] = v;  // plane p-1
-        if (RED) acc4_add(acc, v);
+      if (p >= z0 + 1) {
+        if (act0) {
+          const double v = fixmath::box27(p0, up, spp, c0, uc, spc, s0, u, special);
+          out[-sz] = v;  // plane p-1
+          if (RED) acc4_add(acc, v);
+        }
+        if (act1) {
+          const double v = fixmath::box27(p1, up, spp, c1, uc, spc, s1, u, special);
+          out[sy - sz] = v;
+          if (RED) acc4_add(acc, v);
+        }
       }
-      if (act1) {
-        const double v = fixmath::box27(p1, up, spp, c1, uc, spc, s1, u, special);
-        out[sy - sz] = v;
-        if (RED) acc4_add(acc, v);
-      }
+      p0 = c0;
+      c0 = s0;
+      p1 = c1;
+      c1 = s1;
+      up = uc;
+      uc = u;
+      spp = spc;
+      spc = special;
     }
-    p0 = c0;
-    c0 = s0;
-    p1 = c1;
-    c1 = s1;
-    up = uc;
-    uc = u;
-    spp = spc;
-    spc = special;
+    cp_async_wait<0>();
+    __syncthreads();  // the ring and plane_exp are free for the next run
   }
-  cp_async_wait<0>();
   if (RED) {
-    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    const int nb = gridDim.x * gridDim.y * gridDim.z;
-    if (sa.on) shell_part(acc, sa, b, nb, tid);
-    partial_and_finish(acc, partials, b, nb, ticket, out4, tid, FX * FY);
+    if (sa.on) shell_part(acc, sa, blockIdx.x, gridDim.x, tid);
+    partial_and_finish(acc, partials, blockIdx.x, gridDim.x, ticket, out4, tid, FX * FY);
   }
 }
 
@@ -376,11 +386,27 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
                          (long)out->glob[0] * out->glob[1] * (out->offset[2] + 1);
   const double q = 0.25 * (1.0 / dx);
   if (n[0] > 1) {
+    // z split: the whole number of resident-block waves (at most 8) with the smallest idle tail
+    static int per_sm = 0;
+    if (!per_sm) {
+      int v = 0;
+      per_sm = (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, deep_out_kernel, 256, 0) == cudaSuccess && v > 0)
+                   ? v
+                   : 1;
+    }
     dim3 block(32, 8);
     dim3 grid((n[0] - 1 + 31) / 32, (n[1] + 2 + 7) / 8, 1);
-    const long planes_blocks = (long)grid.x * grid.y;
-    int zsplit = (int)((num_sms() * 8 + planes_blocks - 1) / planes_blocks);
-    zsplit = zsplit < 1 ? 1 : (zsplit > n[2] + 2 ? n[2] + 2 : zsplit);
+    const long planes_blocks = (long)grid.x * grid.y, slots = (long)num_sms() * per_sm;
+    int zsplit = 1;
+    double best = -1.0;
+    for (int zs = 1; zs <= n[2] + 2 && planes_blocks * zs <= 8 * slots; ++zs) {
+      const double waves = (double)(planes_blocks * zs) / slots;
+      const double fill = waves / std::ceil(waves);  // fraction of the slot-waves that hold a block
+      if (fill > best + 1e-3) {
+        best = fill;
+        zsplit = zs;
+      }
+    }
     grid.z = zsplit;
     LaunchScope ls("deep_chain", s);
     deep_out_kernel<<<grid, block, 0, s>>>(va.base, vb.base, vc.base, mask_words, mask_base, vo.base, vo.sy, vo.sz,
@@ -396,7 +422,7 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
   int n[3];
   interior_extent(*out, n);
   const View<double> vo = make_view<double>(*out), vf = make_view<double>(*filt);
-  // filter: one full wave of blocks (z chunks from the resident-block count)
+  // filter: resident blocks per SM
   static int per_sm[2] = {0, 0};
   if (!per_sm[reduce]) {
     int v = 0;
@@ -404,14 +430,15 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<false>, FX * FY, 0);
     per_sm[reduce] = (e == cudaSuccess && v > 0) ? v : 1;
   }
-  const int gxb = (n[0] + FX - 1) / FX, gyb = (n[1] + FTY - 1) / FTY;
-  int chunks = std::max(1, std::min(num_sms() * per_sm[reduce] / (gxb * gyb), (n[2] + 7) / 8));
-  const int zchunk = (n[2] + chunks - 1) / chunks;
-  chunks = (n[2] + zchunk - 1) / zchunk;
+  // one wave of resident blocks, each at least 8 planes of a tile
+  const int tiles_x = (n[0] + FX - 1) / FX, tiles_y = (n[1] + FTY - 1) / FTY;
+  const long total = (long)tiles_x * tiles_y * n[2];
+  if (total >= (1L << 31)) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: more than 2^31 filter tile planes", what);
+  const int blocks = (int)std::max(1L, std::min((long)num_sms() * per_sm[reduce], (total + 7) / 8));
   if (!reduce) {
     LaunchScope ls("box_filter", s);
-    box_filter_kernel<false><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(
-        vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], zchunk, nullptr, ShellArgs{}, nullptr, nullptr);
+    box_filter_kernel<false><<<blocks, dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], tiles_x,
+                                                            total, nullptr, ShellArgs{}, nullptr, nullptr);
     NEBO_LAUNCH_CHECK(what);
     return NEBO_OK;
   }
@@ -426,7 +453,7 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
                      hi[2] != ihi[2];
   const ShellArgs sa{shell ? 1 : 0, (const double*)filt->data, filt->glob[0], (long)filt->glob[0] * filt->glob[1],
                      lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], ilo[0], ihi[0], ilo[1], ihi[1], ilo[2], ihi[2]};
-  const long nblocks = (long)gxb * gyb * chunks;
+  const long nblocks = blocks;
   // one allocation: the partials, then the ticket
   const size_t pbytes = sizeof(Acc4) * nblocks;
   char* scratch = nullptr;
@@ -437,8 +464,8 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
   cudaError_t le = cudaMemsetAsync(ticket, 0, sizeof(unsigned), s);
   if (le == cudaSuccess) {
     LaunchScope ls("box_filter_reduce", s);
-    box_filter_kernel<true><<<dim3(gxb, gyb, chunks), dim3(FX, FY), 0, s>>>(
-        vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], zchunk, partials, sa, ticket, d_out4);
+    box_filter_kernel<true><<<blocks, dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], tiles_x,
+                                                           total, partials, sa, ticket, d_out4);
     le = cudaGetLastError();
   }
   cudaFreeAsync(scratch, s);
