@@ -97,4 +97,27 @@ inline int num_sms() {
   return n;
 }
 
+// Planes per z chunk for a kernel whose blocks each walk zc planes of one (x, y) tile: the zc
+// (a multiple of `align`, at least min_planes unless nz is smaller) that minimises
+// rounds * (zc + overhead), where rounds = ceil(blocks / slots) is the number of waves of
+// `slots` resident blocks and `overhead` the planes a chunk reads beyond its own (halo, ring
+// fill).  A launch of 1.1 waves costs two rounds; this picks the split whose waves are full.
+inline int wave_zchunk(long tiles, long slots, int nz, int overhead, int min_planes, int align) {
+  if (tiles < 1) tiles = 1;
+  if (slots < 1) slots = 1;
+  const int lo = min_planes < nz ? min_planes : nz;
+  int best_zc = (nz + align - 1) / align * align;
+  long best = -1;
+  for (int zc = best_zc; zc >= lo && zc >= 1; zc -= align) {
+    const long chunks = (nz + zc - 1) / zc;
+    const long rounds = (tiles * chunks + slots - 1) / slots;
+    const long cost = rounds * (zc + overhead);
+    if (best < 0 || cost < best) {
+      best = cost;
+      best_zc = zc;
+    }
+  }
+  return best_zc;
+}
+
 }  // namespace nebo

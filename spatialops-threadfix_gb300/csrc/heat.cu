@@ -503,15 +503,21 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     p.w[i] = (T)(0.5 * dt / (sp[i] * sp[i]));
   }
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  // z chunks: enough blocks for ~4 resident blocks per SM, each chunk at least 8 planes
-  const int target = num_sms() * 8;
-  int chunks = (target + gxb * gyb - 1) / (gxb * gyb);
-  chunks = max(1, min(chunks, (n[2] + 7) / 8));
-  const int zchunk = (n[2] + chunks - 1) / chunks;
-  chunks = (n[2] + zchunk - 1) / zchunk;
-  dim3 grid(gxb, gyb, chunks), block(BX, BY);
   const bool unit = sp[0] == 1.0 && sp[1] == 1.0 && sp[2] == 1.0;
   if constexpr (sizeof(T) == 8) {
+    // z chunks in whole waves of resident blocks (a chunk re-reads one plane below it)
+    static int per_sm[2] = {0, 0};
+    if (!per_sm[unit]) {
+      int v = 0;
+      const cudaError_t e =
+          unit ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_kernel<double, ExactD, MODE_UNIT>,
+                                                               BX * BY, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_kernel<double, ExactD, MODE_REFERENCE>,
+                                                               BX * BY, 0);
+      per_sm[unit] = (e == cudaSuccess && v > 0) ? v : 1;
+    }
+    const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * per_sm[unit], n[2], 1, 8, 1);
+    dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
     LaunchScope ls("heat_step_f64", s);
     if (unit)
       heat_step_kernel<double, ExactD, MODE_UNIT><<<grid, block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy, vin.sz,
@@ -544,7 +550,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
                                                                         n[0], n[1], n[2], zc, p.w[0], p.w[1],
                                                                         p.w[2]);
     else
-      heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), block, 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
+      heat_step_f32_async_kernel<false><<<dim3(gxb, fyb, ch), dim3(BX, BY), 0, s>>>(vin.base, vout.base, vl.base, vin.sy,
                                                                              vin.sz, n[0], n[1], n[2], zc, p.w[0],
                                                                              p.w[1], p.w[2]);
   }

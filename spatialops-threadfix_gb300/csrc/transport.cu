@@ -312,11 +312,29 @@ template <typename T>
 int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   const int n = a.n;
   const int gxb = (n + TX - 1) / TX, gyb = (n + TY - 1) / TY;
-  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
-  chunks = chunks < 1 ? 1 : (chunks > (n + 7) / 8 ? (n + 7) / 8 : chunks);
-  const int zchunk = (n + chunks - 1) / chunks;
-  chunks = (n + zchunk - 1) / zchunk;
-  dim3 grid(gxb, gyb, chunks), block(TX, TY);
+  // z chunks in whole waves of resident blocks (a chunk reads 2G halo planes beyond its own)
+  const bool staged = sizeof(T) == 4 && a.sy % 2 == 0;
+  static int per_sm[2][2] = {{0, 0}, {0, 0}};
+  int& ps = per_sm[staged][second];
+  if (!ps) {
+    int v = 0;
+    cudaError_t e;
+    if constexpr (sizeof(T) == 4) {
+      if (staged)
+        e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_f32_staged_kernel<true>, TX * TY, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_f32_staged_kernel<false>, TX * TY,
+                                                                   0);
+      else
+        e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, true>, TX * TY, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, false>, TX * TY, 0);
+    } else {
+      e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, true>, TX * TY, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, false>, TX * TY, 0);
+    }
+    ps = (e == cudaSuccess && v > 0) ? v : 1;
+  }
+  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * ps, n, 2 * G, 8, 1);
+  dim3 grid(gxb, gyb, (n + zchunk - 1) / zchunk), block(TX, TY);
   LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
   if constexpr (sizeof(T) == 4) {
     if (a.sy % 2 == 0) {  // even pitch: 8-byte plane copies
