@@ -206,10 +206,11 @@ extern "C" int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ai
   const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
                      vl = make_view<double>(*lam), vg = make_view<double>(*glam);
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
-  chunks = chunks < 1 ? 1 : (chunks > (n[2] + 7) / 8 ? (n[2] + 7) / 8 : chunks);
-  const int zchunk = (n[2] + chunks - 1) / chunks;
-  chunks = (n[2] + zchunk - 1) / zchunk;
+  static int per_sm = 0;  // z chunks in whole waves of resident blocks
+  const int zchunk = wave_zchunk((long)gxb * gyb,
+                                 (long)num_sms() * blocks_per_sm(heat_adjoint_kernel<true, false>, BX * BY, per_sm),
+                                 n[2], 1, 8, 1);
+  const int chunks = (n[2] + zchunk - 1) / zchunk;
   cudaStream_t s = (cudaStream_t)stream;
   LaunchScope ls("heat_adjoint_step", s);
   heat_adjoint_kernel<true, false><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
@@ -230,10 +231,11 @@ int adjoint_step_lf(const nebo_field* Tk, const nebo_field* Ain, const nebo_fiel
   const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
                      vg = make_view<double>(*glam);
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  int chunks = (num_sms() * 8 + gxb * gyb - 1) / (gxb * gyb);
-  chunks = chunks < 1 ? 1 : (chunks > (n[2] + 7) / 8 ? (n[2] + 7) / 8 : chunks);
-  const int zchunk = (n[2] + chunks - 1) / chunks;
-  chunks = (n[2] + zchunk - 1) / zchunk;
+  static int per_sm[2] = {0, 0};  // z chunks in whole waves of resident blocks
+  const int bps = exact ? blocks_per_sm(heat_adjoint_kernel<true, true>, BX * BY, per_sm[1])
+                        : blocks_per_sm(heat_adjoint_kernel<false, true>, BX * BY, per_sm[0]);
+  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);
+  const int chunks = (n[2] + zchunk - 1) / zchunk;
   LaunchScope ls("heat_adjoint_step", s);
   if (exact)
     heat_adjoint_kernel<true, true><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(

@@ -97,25 +97,43 @@ inline int num_sms() {
   return n;
 }
 
+// Resident blocks per SM of `kernel` at `threads` threads and no dynamic shared memory, kept in
+// the caller's `cache` after the first query.
+template <class K>
+inline int blocks_per_sm(K kernel, int threads, int& cache) {
+  if (!cache) {
+    int v = 0;
+    cache = (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) == cudaSuccess && v > 0) ? v : 1;
+  }
+  return cache;
+}
+
 // Planes per z chunk for a kernel whose blocks each walk zc planes of one (x, y) tile: the zc
 // (a multiple of `align`, at least min_planes unless nz is smaller) that minimises
 // rounds * (zc + overhead), where rounds = ceil(blocks / slots) is the number of waves of
 // `slots` resident blocks and `overhead` the planes a chunk reads beyond its own (halo, ring
-// fill).  A launch of 1.1 waves costs two rounds; this picks the split whose waves are full.
+// fill).  Splits of at least six waves are preferred when the field allows them: blocks that
+// start at staggered times keep every SM busy to the end (a sweep of zc on the FP64 heat step
+// at 192^3 and 256^3 and the FP32 transport stage at 256^3 found the fastest split there).
 inline int wave_zchunk(long tiles, long slots, int nz, int overhead, int min_planes, int align) {
   if (tiles < 1) tiles = 1;
   if (slots < 1) slots = 1;
   const int lo = min_planes < nz ? min_planes : nz;
-  int best_zc = (nz + align - 1) / align * align;
-  long best = -1;
-  for (int zc = best_zc; zc >= lo && zc >= 1; zc -= align) {
-    const long chunks = (nz + zc - 1) / zc;
-    const long rounds = (tiles * chunks + slots - 1) / slots;
-    const long cost = rounds * (zc + overhead);
-    if (best < 0 || cost < best) {
-      best = cost;
-      best_zc = zc;
+  const int top = (nz + align - 1) / align * align;
+  int best_zc = top;
+  for (int min_rounds = 6; min_rounds >= 1; min_rounds -= 5) {
+    long best = -1;
+    for (int zc = top; zc >= lo && zc >= 1; zc -= align) {
+      const long chunks = (nz + zc - 1) / zc;
+      const long rounds = (tiles * chunks + slots - 1) / slots;
+      if (rounds < min_rounds) continue;
+      const long cost = rounds * (zc + overhead);
+      if (best < 0 || cost < best) {
+        best = cost;
+        best_zc = zc;
+      }
     }
+    if (best >= 0) break;
   }
   return best_zc;
 }

@@ -507,16 +507,9 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
   if constexpr (sizeof(T) == 8) {
     // z chunks in whole waves of resident blocks (a chunk re-reads one plane below it)
     static int per_sm[2] = {0, 0};
-    if (!per_sm[unit]) {
-      int v = 0;
-      const cudaError_t e =
-          unit ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_kernel<double, ExactD, MODE_UNIT>,
-                                                               BX * BY, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_kernel<double, ExactD, MODE_REFERENCE>,
-                                                               BX * BY, 0);
-      per_sm[unit] = (e == cudaSuccess && v > 0) ? v : 1;
-    }
-    const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * per_sm[unit], n[2], 1, 8, 1);
+    const int bps = unit ? blocks_per_sm(heat_step_kernel<double, ExactD, MODE_UNIT>, BX * BY, per_sm[1])
+                         : blocks_per_sm(heat_step_kernel<double, ExactD, MODE_REFERENCE>, BX * BY, per_sm[0]);
+    const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);
     dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
     LaunchScope ls("heat_step_f64", s);
     if (unit)

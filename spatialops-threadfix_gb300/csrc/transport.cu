@@ -315,24 +315,14 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   // z chunks in whole waves of resident blocks (a chunk reads 2G halo planes beyond its own)
   const bool staged = sizeof(T) == 4 && a.sy % 2 == 0;
   static int per_sm[2][2] = {{0, 0}, {0, 0}};
-  int& ps = per_sm[staged][second];
-  if (!ps) {
-    int v = 0;
-    cudaError_t e;
-    if constexpr (sizeof(T) == 4) {
-      if (staged)
-        e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_f32_staged_kernel<true>, TX * TY, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_f32_staged_kernel<false>, TX * TY,
-                                                                   0);
-      else
-        e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, true>, TX * TY, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, false>, TX * TY, 0);
-    } else {
-      e = second ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, true>, TX * TY, 0)
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, transport_stage_kernel<T, false>, TX * TY, 0);
-    }
-    ps = (e == cudaSuccess && v > 0) ? v : 1;
-  }
+  int& cache = per_sm[staged][second];
+  int ps;
+  if (staged)
+    ps = second ? blocks_per_sm(transport_stage_f32_staged_kernel<true>, TX * TY, cache)
+                : blocks_per_sm(transport_stage_f32_staged_kernel<false>, TX * TY, cache);
+  else
+    ps = second ? blocks_per_sm(transport_stage_kernel<T, true>, TX * TY, cache)
+                : blocks_per_sm(transport_stage_kernel<T, false>, TX * TY, cache);
   const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * ps, n, 2 * G, 8, 1);
   dim3 grid(gxb, gyb, (n + zchunk - 1) / zchunk), block(TX, TY);
   LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
