@@ -166,9 +166,10 @@ int nebo_deep_chain_reduce(const nebo_field* a, const nebo_field* b, const nebo_
 
 /* filt <<= BoxFilter3D(src) alone (the filter of nebo_deep_chain; 27 points, coefficient 1/27,
  * spatialops/NeboStencilBuilder.h:454-465) over the interior, for any FP64 field with one
- * periodic-style ghost layer (window = allocation, no BC cells).  The 27-point sums are exact in
- * 64-bit fixed point per plane (see deep.cu); the value is within 1e-13 relative of the
- * reference's FP64 sum.  d_out4 non-null: {sum, max, min, norm} of dst as nebo_reduce_all gives
+ * periodic-style ghost layer (window = allocation, no BC cells).  The 9-point sum of each plane
+ * is exact in 128-bit fixed point and rounded once; the three plane sums add in FP64 (see
+ * deep.cu); the value is within 1e-13 of the reference's FP64 sum, relative to the sum of the
+ * 27 magnitudes.  d_out4 non-null: {sum, max, min, norm} of dst as nebo_reduce_all gives
  * them (ghost-inclusive unless interior), folded into the same pass. */
 int nebo_box_filter(const nebo_field* src, const nebo_field* dst, int interior, double* d_out4,
                     nebo_stream_t stream);

@@ -180,15 +180,15 @@ constexpr int FTY = 16;  // filter tile y (each thread of the 32 x 8 block owns 
 // (two neighbouring sums share their middle pair), a sync, y-sums of 3 for the thread's two
 // cells; the 2-D sums of planes p-2, p-1, p give the outputs of plane p-1.
 //
-// The sums run on the integer pipe, exactly, in 128-bit fixed point (fp64_int.cuh).  A plane
-// whose largest biased exponent is E converts each value to an integer in units of 2^(E-1144),
-// rounded to nearest: every value down to 2^-69 of the plane's largest keeps its 53 bits, each
-// term is below 2^122 and 27 of them stay below 2^127.  The three plane sums of an output are
-// aligned to the largest unit, added, rounded once to a double and multiplied by RN(1/27).
-// Error: at most 14 units of the largest plane (2^-118 of its largest |value|) before the two
-// roundings, against the reference's 27 roundings of up to 2^-53 of the running sum.  A plane
-// holding an infinity or NaN, or only values below 2^-893 (all-zero planes included), sums in
-// FP64 instead (the adds of the reference, reassociated).
+// The 9-point (x, y) sums of a plane run on the integer pipe, exactly, in 128-bit fixed point
+// (fp64_int.cuh).  A plane whose largest biased exponent is E converts each value to an integer
+// in units of 2^(E-1144), rounded to nearest: every value down to 2^-69 of the plane's largest
+// keeps its 53 bits, each term is below 2^122 and 9 of them stay below 2^126.  Each cell's plane
+// sum is rounded once to a double; an output adds its three plane sums in FP64 and multiplies
+// by RN(1/27): four roundings of up to 2^-53 of the partial sums (plus 9 units of 2^-122 of the
+// plane's largest |value|), against the reference's 27 roundings.  A plane holding an infinity
+// or NaN, only values below 2^-893 (all-zero planes included) or values above 2^1017 sums in
+// FP64 instead (the adds of the reference, reassociated; IEEE overflow to infinity).
 // Work split: the output planes of all FX x FTY tiles in a flat order (tile-major, z innermost);
 // block b of gridDim.x takes the range [b total / gridDim.x, (b+1) total / gridDim.x), one or
 // more z runs of consecutive tiles, so every resident block gets the same number of planes.
@@ -245,11 +245,8 @@ __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __r
       cp_async_commit();
     }
     const bool act0 = x < nx && ya < ny, act1 = x < nx && ya + 1 < ny;
-    // 2-D sums of planes p-2 (p*) and p-1 (c*) for both cells: fixed-point integers in units of
-    // 2^u*, or FP64 bits when the plane was special (sp*)
-    fixmath::fix128 p0 = 0, c0 = 0, p1 = 0, c1 = 0;
-    int up = 0, uc = 0;
-    bool spp = false, spc = false;
+    // 9-point (x, y) sums of planes p-2 (p*) and p-1 (c*) for both cells
+    double p0 = 0.0, c0 = 0.0, p1 = 0.0, c1 = 0.0;
     double* out = dst + (long)x + (long)sy * ya + sz * (z0 - 1);
 #pragma unroll 1
     for (int p = z0 - 1; p <= z1; ++p, out += sz) {
@@ -273,7 +270,7 @@ __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __r
       __syncthreads();
       const int E = (int)plane_exp[p & 1];
       if (tid == 0) plane_exp[(p + 1) & 1] = 0u;  // the slot of plane p+1 (last read in iteration p-1)
-      const bool special = E == 0x7ff || E < 130;
+      const bool special = E == 0x7ff || E < 130 || E > 2040;
       const int u = E - 1144;
       if (!special) {
 #pragma unroll
@@ -299,24 +296,26 @@ __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __r
       }
       __syncthreads();
       const fixmath::fix128* col = rows + 2 * ty * FX + tx;
-      fixmath::fix128 s0, s1;
+      double s0, s1;
       if (!special) {
         const fixmath::fix128 mid = col[FX] + col[2 * FX];
-        s0 = col[0] + mid;
-        s1 = mid + col[3 * FX];
+        s0 = fixmath::units_to_double0(col[0] + mid, u);
+        s1 = fixmath::units_to_double0(mid + col[3 * FX], u);
       } else {
-        const double mid = __longlong_as_double((long long)col[FX]) + __longlong_as_double((long long)col[2 * FX]);
-        s0 = __double_as_longlong(__longlong_as_double((long long)col[0]) + mid);
-        s1 = __double_as_longlong(mid + __longlong_as_double((long long)col[3 * FX]));
+        auto d = [](fixmath::fix128 f) { return __longlong_as_double((long long)f); };
+        const double mid = __dadd_rn(d(col[FX]), d(col[2 * FX]));
+        s0 = __dadd_rn(d(col[0]), mid);
+        s1 = __dadd_rn(mid, d(col[3 * FX]));
       }
       if (p >= z0 + 1) {
+        constexpr double C27 = 1.0 / 27.0;
         if (act0) {
-          const double v = fixmath::box27(p0, up, spp, c0, uc, spc, s0, u, special);
+          const double v = __dmul_rn(__dadd_rn(__dadd_rn(p0, c0), s0), C27);
           out[-sz] = v;  // plane p-1
           if (RED) acc4_add(acc, v);
         }
         if (act1) {
-          const double v = fixmath::box27(p1, up, spp, c1, uc, spc, s1, u, special);
+          const double v = __dmul_rn(__dadd_rn(__dadd_rn(p1, c1), s1), C27);
           out[sy - sz] = v;
           if (RED) acc4_add(acc, v);
         }
@@ -325,10 +324,6 @@ __global__ void __launch_bounds__(FX* FY, 4) box_filter_kernel(const double* __r
       c0 = s0;
       p1 = c1;
       c1 = s1;
-      up = uc;
-      uc = u;
-      spp = spc;
-      spc = special;
     }
     cp_async_wait<0>();
     __syncthreads();  // the ring and plane_exp are free for the next run

@@ -417,18 +417,6 @@ __device__ __forceinline__ fix128 to_units(double x, int E) {
   return b < 0 ? -f : f;
 }
 
-// f (units of 2^u) in units of 2^U >= 2^u, rounded to nearest (halves up).
-__device__ __forceinline__ fix128 rescale_units(fix128 f, int u, int U) {
-  const int k = U - u;
-  if (k == 0) return f;
-  if (k > 126) return 0;
-  const fix128 g = f + ((fix128)1 << (k - 1));
-  const long long hi = (long long)(g >> 64);
-  const unsigned long long lo = (unsigned long long)g;
-  if (k >= 64) return make128(hi >> 63, (unsigned long long)(hi >> (k - 64)));
-  return make128(hi >> k, (lo >> k) | ((unsigned long long)hi << (64 - k)));
-}
-
 // RN(t 2^u) for t != 0, assuming the result is normal.
 __device__ __forceinline__ double units_to_double(fix128 t, int u) {
   const bool neg = t < 0;
@@ -461,28 +449,8 @@ __device__ __forceinline__ double units_to_double(fix128 t, int u) {
   return __longlong_as_double((long long)bits);
 }
 
-// Box value sum / 27 from three plane sums, each fixed point (units 2^u_i) or, on a special
-// plane, FP64 bits in the low word; see box_filter_kernel.
-__device__ __forceinline__ double box27(fix128 a, int ua, bool sa, fix128 b, int ub, bool sb, fix128 c, int uc,
-                                        bool sc) {
-  constexpr double C27 = 1.0 / 27.0;
-  if (!(sa || sb || sc)) {
-    int U = ua;
-    fix128 t;
-    if (ua == ub && ub == uc) {  // the three planes share a unit: no rescaling
-      t = (a + b) + c;
-    } else {
-      U = max(ua, max(ub, uc));
-      t = rescale_units(a, ua, U) + rescale_units(b, ub, U) + rescale_units(c, uc, U);
-    }
-    if (t == 0) return 0.0;
-    return __dmul_rn(units_to_double(t, U), C27);
-  }
-  auto dbl = [](fix128 f, int u, bool sp) {
-    return sp ? __longlong_as_double((long long)f) : (f == 0 ? 0.0 : units_to_double(f, u));
-  };
-  return ((dbl(a, ua, sa) + dbl(b, ub, sb)) + dbl(c, uc, sc)) * C27;
-}
+// RN(t 2^u), +0 for t == 0, assuming a nonzero result is normal.
+__device__ __forceinline__ double units_to_double0(fix128 t, int u) { return t == 0 ? 0.0 : units_to_double(t, u); }
 
 // A divisor whose reciprocal div_by may use: positive, exponent within 2^+-400 (integer pipe).
 __device__ __forceinline__ bool divisor_ok(double b) {
