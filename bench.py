@@ -136,6 +136,19 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workloads
+def deep_label(n):
+    return f"deep chain {n}^3 + 1 ghost (a SVol; b, c, out, filt XVol; 5% + boundary mask), filter + 4 reductions"
+
+
+def heat_label(n, dtype):
+    return f"heat {n}^3 + 1 ghost, {'FP64 bit-exact' if dtype == 'f64' else 'FP32'} fused RHS + Euler update"
+
+
+def particles_label(n, npart):
+    return (f"particles: {n}^3 SVol + 1 ghost, {npart / 1e6:.1f} M particles (edges U(0.5,1.5) cells, "
+            f"random order); step = CellToParticle + ParticleToCell, FP64, bit-identical to the reference")
+
+
 class Deep:
     name = "deep"
 
@@ -160,7 +173,7 @@ class Deep:
         self.red = torch.zeros(4, dtype=torch.float64, device="cuda")
         self.cells = n ** 3
         self.launches_per_step = 2  # chain; filter with the four reductions (ghost shell and final merge in the same grid)
-        self.label = f"deep chain {n}^3 + 1 ghost (a SVol; b, c, out, filt XVol; 5% + boundary mask), filter + 4 reductions"
+        self.label = deep_label(n)
         self.h2d_bytes = sum(h.numel() * h.element_size() for h in self.host) + self.host_mask.numel() * 4
         self.d2h_bytes = 4 * 8
         self.host_red = torch.zeros(4, dtype=torch.float64).pin_memory()
@@ -218,7 +231,7 @@ class Heat:
         from spatialops_gb300 import workloads as W
 
         self.name = "heat" if dtype == "f64" else "heat32"
-        self.label = f"heat {n}^3 + 1 ghost, {'FP64 bit-exact' if dtype == 'f64' else 'FP32'} fused RHS + Euler update"
+        self.label = heat_label(n, dtype)
         self.N, self.n = N, n
         lam, T0, dt = W.heat_inputs((n, n, n))
         self.dt = dt
@@ -447,8 +460,7 @@ class ParticlesWL:
         self.d2h_bytes = sum(h.numel() * h.element_size() for h in self.host_out)
         self.metric = "particle cell<->particle exchanges/s"
         self.unit = "Gparticle/s"
-        self.label = (f"particles: {n}^3 SVol + 1 ghost, {self.npart / 1e6:.1f} M particles (edges U(0.5,1.5) cells, "
-                      f"random order); step = CellToParticle + ParticleToCell, FP64, bit-identical to the reference")
+        self.label = particles_label(n, self.npart)
 
     def step(self):
         N = self.N
@@ -560,7 +572,7 @@ def run_reference(args):
             "unit": "Gparticle/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"particles on the {n}^3 field", "sample": f"{npart} particles per step"},
+            "config": {"workload": particles_label(n, n ** 3), "sample": f"{npart} particles per step"},
             "cpu_baseline": {"value": value, "unit": "Gparticle/s", "cores": 1, "kind": "port",
                              "sample": f"CellToParticle + ParticleToCell of {npart} particles on the {n}^3 field per "
                                        f"step, oracle restatement of the reference's serial operator loops"},
@@ -582,7 +594,8 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if workload != "heat32" else "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"{workload} {n}^3", "sample": f"{n}x{n}x{nz} slab per step"},
+        "config": {"workload": deep_label(n) if workload == "deep" else heat_label(n, "f64"),
+                   "cells_per_step": n * n * nz, "sample": f"{n}x{n}x{nz} slab per step"},
         "cpu_baseline": {"value": value, "unit": "Gcell-upd/s", "cores": threads, "kind": "port",
                          "sample": f"{n}x{n}x{nz} slab of the {n}^3 {workload} workload per step, "
                                    f"oracle restatement of the reference's serial walk, z-slabs over {threads} threads"},
