@@ -51,7 +51,9 @@ def test_mask_words_match_bitfield_layout():
     assert (words.cpu().numpy().view(np.uint32) == ref).all()
 
 
-@pytest.mark.parametrize("n", [(64, 64, 64), (45, 30, 17)])
+# thin and ragged shapes: one or two tiles, runs of the filter's flat split crossing tiles, a
+# chain z split larger than a block's plane count
+@pytest.mark.parametrize("n", [(64, 64, 64), (45, 30, 17), (33, 5, 2), (130, 3, 9), (8, 70, 3)])
 def test_deep_vs_oracle(n):
     a, b, c, pts = W.deep_inputs(n)
     out, filt, _ = _gpu(a, b, c, pts, n)
@@ -60,7 +62,8 @@ def test_deep_vs_oracle(n):
     assert _relerr(filt.numpy(), o_filt) <= TOL
 
 
-@pytest.mark.parametrize("n,interior", [((64, 64, 64), False), ((45, 30, 17), False), ((45, 30, 17), True)])
+@pytest.mark.parametrize("n,interior", [((64, 64, 64), False), ((45, 30, 17), False), ((45, 30, 17), True),
+                                        ((33, 5, 2), False), ((130, 3, 9), True), ((8, 70, 3), False)])
 def test_fused_filter_reductions(n, interior):
     """nebo_deep_chain_reduce: filt bit-identical to the unfused chain; {sum, max, min, norm} of
     filt (its stale ghost cells included unless interior) equal to the one-pass reductions of
