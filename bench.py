@@ -393,14 +393,14 @@ class AdjointWL:
         self.J, self.gT, self.gl = self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt,
                                                         products=self.products)
 
-    def gradient_ms(self, products):
-        """Device time of one gradient with the given face-product precision."""
+    def gradient_ms(self, products, checkpoint_every=0):
+        """Device time of one gradient with the given face-product precision and checkpoints."""
         import torch
 
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record()
-        self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt, products=products)
+        self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt, checkpoint_every, products=products)
         e1.record()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
@@ -740,9 +740,12 @@ def main():
     if W.name == "adjoint":
         fwd = W.forward_ms()
         g64 = W.gradient_ms("f64")
+        W.gradient_ms("f32", W.N.CHECKPOINT_AUTO)  # warm: the pool grows to hold every state
+        gall = W.gradient_ms("f32", W.N.CHECKPOINT_AUTO)
         extra = {"adjoint_over_forward": (ms / args.steps) / fwd, "forward_ms": fwd,
                  "forward_value": W.cells / (fwd * 1e-3) / 1e9, "J": W.J,
-                 "adjoint_over_forward_all_fp64": g64 / fwd}
+                 "adjoint_over_forward_all_fp64": g64 / fwd,
+                 "adjoint_over_forward_every_state_kept": gall / fwd}
     line = {
         "metric": getattr(W, "metric", f"{W.name} cell-updates/s"), "value": value,
         "unit": getattr(W, "unit", "Gcell-upd/s"),

@@ -245,8 +245,12 @@ int nebo_transport_run(double* phi, const void* u, const void* v, const void* w,
  *   Inputs need periodic ghost images (T_k, A_{k+1}, lambda); Aout gets images.
  * nebo_heat_gradient: forward sweep keeping every L-th state (L = checkpoint_every, or
  *   ceil(sqrt(steps)) when <= 0), then the reverse sweep recomputing each segment from its
- *   checkpoint: device memory ~ (steps/L + L) fields.  Writes gT0 = dJ/dT_0 (window with
- *   images), glam = dJ/dlambda (interior; ghosts zero) and *J. */
+ *   checkpoint: device memory ~ (steps/L + L) fields.  checkpoint_every = NEBO_CHECKPOINT_AUTO
+ *   keeps every state (L = 1, no recomputation: one forward sweep instead of two) when
+ *   steps + 7 fields fit in 80 % of the free device memory, else takes ceil(sqrt(steps)).
+ *   Writes gT0 = dJ/dT_0 (window with images), glam = dJ/dlambda (interior; ghosts zero)
+ *   and *J; the results do not depend on L. */
+enum { NEBO_CHECKPOINT_AUTO = -1 };
 /* nebo_heat_gradient with a choice of face-product precision in the lambda gradient:
  *   NEBO_PRODUCTS_F64  as nebo_heat_gradient (every operation FP64);
  *   NEBO_PRODUCTS_F32  the per-face products (T_b - T_a)(A_b - A_a) of the lambda gradient are

@@ -418,9 +418,13 @@ class Transport:
                                         ctypes.c_void_p(self.work.data_ptr()), _stream(stream)))
 
 
+CHECKPOINT_AUTO = -1  # NEBO_CHECKPOINT_AUTO: keep every state when they fit in device memory
+
+
 def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None, products="f64"):
     """(J, dJ/dT0, dJ/dlambda) for J = 1/2 sum (T_N - T_target)^2 (fields: SVol, 1 ghost, FP64).
 
+    checkpoint_every: 0 = ceil(sqrt(steps)); CHECKPOINT_AUTO = every state when they fit.
     products="f32": the lambda gradient's face products in FP32 (nebo_heat_gradient_ex)."""
     gT = Field(T0.loc, T0.n, T0.ghost)
     gl = Field(T0.loc, T0.n, T0.ghost)

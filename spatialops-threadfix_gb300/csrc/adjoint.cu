@@ -363,10 +363,19 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
   }
   if (steps < 1) return fail(NEBO_ERR_INVALID, "Nebo error in %s: steps < 1", what);
   cudaStream_t s = (cudaStream_t)stream;
-  const int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
-  const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
   const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
   const size_t bytes = cells * sizeof(double);
+  int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
+  if (checkpoint_every == NEBO_CHECKPOINT_AUTO) {
+    // every state kept (no recomputation) when steps + 7 fields fit in 80 % of the free memory
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+      if (((size_t)steps + 7) * bytes <= free_b / 10 * 8) L = 1;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
   // device memory: nck checkpoints + L segment states + 2 adjoint states + 1 forward temp +
   // 3 face-coefficient arrays, ~ (2 sqrt(N) + 6) fields
   const size_t nbuf = (size_t)nck + (size_t)L + 6;
@@ -382,7 +391,8 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
 
 // Full gradient with sqrt(N) checkpointing.  T0, lam, Ttarget: windows (1 ghost, periodic patch);
 // gT0, glam: outputs (windows; interiors written, glam overwritten); J: host result.
-// checkpoint_every <= 0 selects ceil(sqrt(steps)).
+// checkpoint_every 0 (or below, other than NEBO_CHECKPOINT_AUTO) selects ceil(sqrt(steps));
+// NEBO_CHECKPOINT_AUTO keeps every state when they fit in device memory.
 extern "C" int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
                                   double dt, int checkpoint_every, const nebo_field* gT0, const nebo_field* glam,
                                   double* J, nebo_stream_t stream) {

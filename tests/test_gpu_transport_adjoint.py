@@ -65,7 +65,7 @@ def _gpu_grad(lam, T0, Tt, steps, dt, every=0):
     return J, gT.numpy(), gl.numpy()
 
 
-@pytest.mark.parametrize("every", [0, 1, 4, 50])
+@pytest.mark.parametrize("every", [0, 1, 4, 50, N.CHECKPOINT_AUTO])
 def test_adjoint_matches_oracle_adjoint(every):
     n, steps = (10, 9, 8), 13
     lam, T0, dt, Tt = _setup(n, steps)
@@ -78,6 +78,17 @@ def test_adjoint_matches_oracle_adjoint(every):
     assert abs(J - 0.5 * float((r[I] ** 2).sum())) <= 1e-12 * max(J, 1e-300)
     assert _rel(gT[I], ref_gT[I]) <= 1e-12
     assert _rel(gl[I], ref_gl[I]) <= 1e-12
+
+
+def test_adjoint_checkpointing_does_not_change_the_gradient():
+    # sqrt(N) checkpoints (recomputed segments) and every state kept give the same bits
+    n, steps = (12, 10, 9), 17
+    lam, T0, dt, Tt = _setup(n, steps)
+    J0, gT0, gl0 = _gpu_grad(lam, T0, Tt, steps, dt, 0)
+    J1, gT1, gl1 = _gpu_grad(lam, T0, Tt, steps, dt, N.CHECKPOINT_AUTO)
+    assert J0 == J1
+    assert np.array_equal(gT0.view(np.uint64), gT1.view(np.uint64))
+    assert np.array_equal(gl0.view(np.uint64), gl1.view(np.uint64))
 
 
 def test_adjoint_dense_jacobian_8cubed():
