@@ -296,6 +296,163 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_f32_staged_kernel(TrAr
   tcp_wait<0>();
 }
 
+// FP32 stage, two x-adjacent cells (x, x+1; x even) per thread: the 32 x 8 tile of the staged
+// kernel with 16 x 8 threads, the same plane ring and copy layout, and every face flux, difference
+// and stencil value as a packed FP32x2 pair (__ffma2_rn / __fadd2_rn / __fmul2_rn), so one packed
+// instruction serves both cells.  Pairs in the stage and in the fields start at even columns
+// (8-byte loads): with Pm = (x-2, x-1), P = (x, x+1), Pp = (x+2, x+3) the low x faces of the two
+// cells (x-1/2, x+1/2) and their high x faces (x+1/2, x+3/2) each take one packed flux (the
+// shared face x+1/2 is evaluated twice, identically); y and z faces take one packed flux each.
+// The RK combination, the FP64 state and the stencil copy with its images stay per cell.
+// Needs n even (even pitch) and 8-byte aligned field bases.
+constexpr int PTX = TX / 2;  // threads per tile row
+
+__device__ __forceinline__ float2 tsub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 tld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+__device__ __forceinline__ float2 tsh2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+
+// sflux for two faces at once (same operand order).
+__device__ __forceinline__ float2 sflux2(float2 nu, float2 q0, float2 q1, float2 q2, float2 q3, float2 la, float2 lb,
+                                         float2 pm2, float2 pm1, float2 p0, float2 pp1, float2 uf) {
+  const float2 il = __fmul2_rn(__fadd2_rn(la, lb), make_float2(0.5f, 0.5f));
+  float2 g4 = __fmul2_rn(pm2, q0);
+  g4 = __ffma2_rn(pm1, q1, g4);
+  g4 = __ffma2_rn(p0, q2, g4);
+  g4 = __ffma2_rn(pp1, q3, g4);
+  const float2 up = make_float2(uf.x > 0.0f ? pm1.x : p0.x, uf.y > 0.0f ? pm1.y : p0.y);
+  return __ffma2_rn(make_float2(-uf.x, -uf.y), up, __fmul2_rn(__fmul2_rn(nu, il), g4));
+}
+
+// The pair (x, x+1) at (y, z) of the stencil copy, with periodic images for cells within G of a face.
+__device__ __forceinline__ void store_images2_pair(float* base, int sy, long sz, int x, int y, int z, int n, float v0,
+                                                   float v1) {
+  if (x >= G && x + 1 < n - G && y >= G && y < n - G && z >= G && z < n - G) {
+    *reinterpret_cast<float2*>(base + (long)x + (long)sy * y + sz * z) = make_float2(v0, v1);
+  } else {
+    store_images2_edge(base, sy, sz, x, y, z, n, v0);
+    store_images2_edge(base, sy, sz, x + 1, y, z, n, v1);
+  }
+}
+
+template <bool SECOND>
+__global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArgs<float> a, int zchunk) {
+  constexpr int NT = PTX * TY;
+  constexpr int NCP = (2 * SUNITS + NT - 1) / NT;
+  __shared__ __align__(16) float sP[SNS * SPLANE];
+  __shared__ __align__(16) float sL[SNS * SPLANE];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * PTX + tx;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int n = a.n, sy = a.sy;
+  const long sz = a.sz;
+  const int x = x0 + 2 * tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, n);
+  const bool active = x < n && y < n;            // n even: x + 1 < n as well
+  const int xc = min(x, n - 2), yc = min(y, n);  // idle lanes read valid cells (x + 3 <= n + 1)
+  int goff[NCP];
+  uint32_t soff[NCP];
+  bool lamf[NCP];
+  const uint32_t sP0 = (uint32_t)__cvta_generic_to_shared(sP), sL0 = (uint32_t)__cvta_generic_to_shared(sL);
+#pragma unroll
+  for (int j = 0; j < NCP; ++j) {
+    const int u = min(tid + j * NT, 2 * SUNITS - 1);
+    lamf[j] = u >= SUNITS;
+    const int k = lamf[j] ? u - SUNITS : u;
+    const int r = k / (SPW / 2), c = 2 * (k - r * (SPW / 2));
+    goff[j] = min(x0 - G + c, n) + sy * min(y0 - G + r, n + 1);
+    soff[j] = (lamf[j] ? sL0 : sP0) + (uint32_t)((r * SPW + c) * sizeof(float));
+  }
+  const bool last_slot = tid + (NCP - 1) * NT < 2 * SUNITS;
+  auto issue = [&](int p, int st) {
+    if (p <= z1 + 1) {
+      const float* pp = a.phi + sz * p;
+      const float* lp = a.lam + sz * p;
+      const uint32_t so = (uint32_t)st * (SPLANE * sizeof(float));
+#pragma unroll
+      for (int j = 0; j < NCP; ++j) {
+        if (j == NCP - 1 && !last_slot) break;
+        tcp_async8(soff[j] + so, (lamf[j] ? lp : pp) + goff[j]);
+      }
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < SNS - 1; ++i) {
+    issue(z0 + i, i);
+    tcp_commit();
+  }
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+  const long c0 = at(xc, yc, z0);
+  float2 pm1 = tld2(a.phi + c0 - sz), p0 = tld2(a.phi + c0), p1 = tld2(a.phi + c0 + sz);
+  float2 fzlo = make_float2(face_flux(a, c0, sz, a.w), face_flux(a, c0 + 1, sz, a.w));
+  const int ci = (ty + G) * SPW + 2 * tx + G;  // even: 8-byte aligned pairs
+  struct Col {
+    float2 ul, vl, vh, wh;
+    float u2;
+    double acc0, acc1, base0, base1;
+  };
+  auto load_col = [&](int z) {
+    Col q;
+    const long c = at(xc, yc, z);
+    q.ul = tld2(a.u + c);  // faces x-1/2, x+1/2
+    q.u2 = __ldg(a.u + c + 2);  // face x+3/2
+    q.vl = tld2(a.v + c);
+    q.vh = tld2(a.v + c + sy);
+    q.wh = tld2(a.w + c + sz);
+    q.acc0 = a.acc[c];
+    q.acc1 = a.acc[c + 1];
+    q.base0 = SECOND ? a.base[c] : 0.0;
+    q.base1 = SECOND ? a.base[c + 1] : 0.0;
+    return q;
+  };
+  const float2 NU = make_float2(a.nu, a.nu), Q0 = make_float2(a.q0, a.q0), Q1 = make_float2(a.q1, a.q1),
+               Q2 = make_float2(a.q2, a.q2), Q3 = make_float2(a.q3, a.q3);
+  Col cur = load_col(z0);
+  for (int z = z0; z < z1; ++z) {
+    const int i = z - z0;
+    const Col nxt = load_col(min(z + 1, n));  // plane n is a ghost plane: valid memory
+    tcp_wait<1>();
+    __syncthreads();
+    issue(z + SNS - 1, (i + SNS - 1) % SNS);
+    tcp_commit();
+    const float* P0 = sP + (i % SNS) * SPLANE + ci;
+    const float* L0 = sL + (i % SNS) * SPLANE + ci;
+    const float* L1 = sL + ((i + 1) % SNS) * SPLANE + ci;
+    const float* P2 = sP + ((i + 2) % SNS) * SPLANE + ci;
+    const float2 p2 = tsh2(P2), l0 = tsh2(L0), l1 = tsh2(L1);
+    const float2 pxm = tsh2(P0 - 2), pxp = tsh2(P0 + 2), lxm = tsh2(L0 - 2), lxp = tsh2(L0 + 2);
+    const float2 pym2 = tsh2(P0 - 2 * SPW), pym1 = tsh2(P0 - SPW), pyp1 = tsh2(P0 + SPW), pyp2 = tsh2(P0 + 2 * SPW);
+    const float2 lym = tsh2(L0 - SPW), lyp = tsh2(L0 + SPW);
+    const float2 pmid = make_float2(pxm.y, p0.x), pmid2 = make_float2(p0.y, pxp.x);  // (x-1, x), (x+1, x+2)
+    const float2 fxl = sflux2(NU, Q0, Q1, Q2, Q3, make_float2(lxm.y, l0.x), l0, pxm, pmid, p0, pmid2, cur.ul);
+    const float2 fxh = sflux2(NU, Q0, Q1, Q2, Q3, l0, make_float2(l0.y, lxp.x), pmid, p0, pmid2, pxp,
+                              make_float2(cur.ul.y, cur.u2));
+    const float2 fyl = sflux2(NU, Q0, Q1, Q2, Q3, lym, l0, pym2, pym1, p0, pyp1, cur.vl);
+    const float2 fyh = sflux2(NU, Q0, Q1, Q2, Q3, l0, lyp, pym1, p0, pyp1, pyp2, cur.vh);
+    const float2 fzh = sflux2(NU, Q0, Q1, Q2, Q3, l0, l1, pm1, p0, p1, p2, cur.wh);
+    if (active) {
+      const float2 rhs = __fadd2_rn(__fadd2_rn(tsub(fxh, fxl), tsub(fyh, fyl)), tsub(fzh, fzlo));
+      const double rd0 = fixmath::f32_to_f64(rhs.x), rd1 = fixmath::f32_to_f64(rhs.y);
+      double r0, r1;
+      if (!SECOND) {
+        r0 = cur.acc0 + a.dt * rd0;
+        r1 = cur.acc1 + a.dt * rd1;
+      } else {
+        r0 = 0.5 * cur.base0 + 0.5 * (cur.acc0 + a.dt * rd0);
+        r1 = 0.5 * cur.base1 + 0.5 * (cur.acc1 + a.dt * rd1);
+      }
+      const long c = at(x, y, z);
+      a.out64[c] = r0;
+      a.out64[c + 1] = r1;
+      store_images2_pair(a.outS, sy, sz, x, y, z, n, fixmath::f64_to_f32_rn(r0), fixmath::f64_to_f32_rn(r1));
+    }
+    fzlo = fzh;
+    pm1 = p0;
+    p0 = p1;
+    p1 = p2;
+    cur = nxt;
+  }
+  tcp_wait<0>();
+}
+
 __global__ void cast_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = fixmath::f64_to_f32_rn(a[i]);
@@ -312,12 +469,22 @@ template <typename T>
 int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   const int n = a.n;
   const int gxb = (n + TX - 1) / TX, gyb = (n + TY - 1) / TY;
+  // FP32 kernels: 2 = cell pairs (even pitch, every float field 8-byte aligned), 1 = staged
+  // planes (even pitch, phi and lambda 8-byte aligned), 0 = the generic kernel
+  auto al8 = [](const void* p) { return ((uintptr_t)p & 7u) == 0; };
+  int kind = 0;
+  if (sizeof(T) == 4 && a.sy % 2 == 0 && al8(a.phi) && al8(a.lam)) {
+    kind = 1;
+    if (al8(a.u) && al8(a.v) && al8(a.w) && al8(a.outS)) kind = 2;
+  }
   // z chunks in whole waves of resident blocks (a chunk reads 2G halo planes beyond its own)
-  const bool staged = sizeof(T) == 4 && a.sy % 2 == 0;
-  static int per_sm[2][2] = {{0, 0}, {0, 0}};
-  int& cache = per_sm[staged][second];
+  static int per_sm[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  int& cache = per_sm[kind][second];
   int ps;
-  if (staged)
+  if (kind == 2)
+    ps = second ? blocks_per_sm(transport_stage_f32_pair_kernel<true>, PTX * TY, cache)
+                : blocks_per_sm(transport_stage_f32_pair_kernel<false>, PTX * TY, cache);
+  else if (kind == 1)
     ps = second ? blocks_per_sm(transport_stage_f32_staged_kernel<true>, TX * TY, cache)
                 : blocks_per_sm(transport_stage_f32_staged_kernel<false>, TX * TY, cache);
   else
@@ -327,7 +494,15 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   dim3 grid(gxb, gyb, (n + zchunk - 1) / zchunk), block(TX, TY);
   LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
   if constexpr (sizeof(T) == 4) {
-    if (a.sy % 2 == 0) {  // even pitch: 8-byte plane copies
+    if (kind == 2) {
+      if (second)
+        transport_stage_f32_pair_kernel<true><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk);
+      else
+        transport_stage_f32_pair_kernel<false><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk);
+      NEBO_LAUNCH_CHECK("nebo_transport_run");
+      return NEBO_OK;
+    }
+    if (kind == 1) {
       if (second)
         transport_stage_f32_staged_kernel<true><<<grid, block, 0, s>>>(a, zchunk);
       else
