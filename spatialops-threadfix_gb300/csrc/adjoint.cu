@@ -206,7 +206,7 @@ extern "C" int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ai
   const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
                      vl = make_view<double>(*lam), vg = make_view<double>(*glam);
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  static int per_sm = 0;  // z chunks in whole waves of resident blocks
+  static std::atomic<int> per_sm{0};  // z chunks in whole waves of resident blocks
   const int zchunk = wave_zchunk((long)gxb * gyb,
                                  (long)num_sms() * blocks_per_sm(heat_adjoint_kernel<true, false>, BX * BY, per_sm),
                                  n[2], 1, 8, 1);
@@ -231,7 +231,7 @@ int adjoint_step_lf(const nebo_field* Tk, const nebo_field* Ain, const nebo_fiel
   const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
                      vg = make_view<double>(*glam);
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  static int per_sm[2] = {0, 0};  // z chunks in whole waves of resident blocks
+  static std::atomic<int> per_sm[2];  // z chunks in whole waves of resident blocks (zero: not queried)
   const int bps = exact ? blocks_per_sm(heat_adjoint_kernel<true, true>, BX * BY, per_sm[1])
                         : blocks_per_sm(heat_adjoint_kernel<false, true>, BX * BY, per_sm[0]);
   const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);

@@ -86,26 +86,34 @@ void pool_retain();
 // Periodic ghost fill of one uniform-ghost patch (ghost.cu).
 int fill_periodic_any(const nebo_field* f, cudaStream_t s);
 
+// SM count of the current device, queried once (callers on several threads may race to the
+// first query; they store the same value).
 inline int num_sms() {
-  static int n = 0;
+  static std::atomic<int> cached{0};
+  int n = cached.load(std::memory_order_relaxed);
   if (!n) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (n <= 0) n = 152;
+    cached.store(n, std::memory_order_relaxed);
   }
   return n;
 }
 
 // Resident blocks per SM of `kernel` at `threads` threads and no dynamic shared memory, kept in
-// the caller's `cache` after the first query.
+// the caller's `cache` after the first query (same race rule as num_sms).
 template <class K>
-inline int blocks_per_sm(K kernel, int threads, int& cache) {
-  if (!cache) {
-    int v = 0;
-    cache = (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) == cudaSuccess && v > 0) ? v : 1;
+inline int blocks_per_sm(K kernel, int threads, std::atomic<int>& cache) {
+  int v = cache.load(std::memory_order_relaxed);
+  if (!v) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 1;
+    }
+    cache.store(v, std::memory_order_relaxed);
   }
-  return cache;
+  return v;
 }
 
 // Planes per z chunk for a kernel whose blocks each walk zc planes of one (x, y) tile: the zc

@@ -382,13 +382,8 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
   const double q = 0.25 * (1.0 / dx);
   if (n[0] > 1) {
     // z split: the whole number of resident-block waves (at most 8) with the smallest idle tail
-    static int per_sm = 0;
-    if (!per_sm) {
-      int v = 0;
-      per_sm = (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, deep_out_kernel, 256, 0) == cudaSuccess && v > 0)
-                   ? v
-                   : 1;
-    }
+    static std::atomic<int> per_sm_cache{0};
+    const int per_sm = blocks_per_sm(deep_out_kernel, 256, per_sm_cache);
     dim3 block(32, 8);
     dim3 grid((n[0] - 1 + 31) / 32, (n[1] + 2 + 7) / 8, 1);
     const long planes_blocks = (long)grid.x * grid.y, slots = (long)num_sms() * per_sm;
@@ -418,18 +413,14 @@ int filter_impl(const nebo_field* out, const nebo_field* filt, bool reduce, int 
   interior_extent(*out, n);
   const View<double> vo = make_view<double>(*out), vf = make_view<double>(*filt);
   // filter: resident blocks per SM
-  static int per_sm[2] = {0, 0};
-  if (!per_sm[reduce]) {
-    int v = 0;
-    cudaError_t e = reduce ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<true>, FX * FY, 0)
-                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, box_filter_kernel<false>, FX * FY, 0);
-    per_sm[reduce] = (e == cudaSuccess && v > 0) ? v : 1;
-  }
+  static std::atomic<int> per_sm_cache[2];  // zero: not queried
+  const int per_sm = reduce ? blocks_per_sm(box_filter_kernel<true>, FX * FY, per_sm_cache[1])
+                            : blocks_per_sm(box_filter_kernel<false>, FX * FY, per_sm_cache[0]);
   // one wave of resident blocks, each at least 8 planes of a tile
   const int tiles_x = (n[0] + FX - 1) / FX, tiles_y = (n[1] + FTY - 1) / FTY;
   const long total = (long)tiles_x * tiles_y * n[2];
   if (total >= (1L << 31)) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: more than 2^31 filter tile planes", what);
-  const int blocks = (int)std::max(1L, std::min((long)num_sms() * per_sm[reduce], (total + 7) / 8));
+  const int blocks = (int)std::max(1L, std::min((long)num_sms() * per_sm, (total + 7) / 8));
   if (!reduce) {
     LaunchScope ls("box_filter", s);
     box_filter_kernel<false><<<blocks, dim3(FX, FY), 0, s>>>(vo.base, vf.base, vo.sy, vo.sz, n[0], n[1], n[2], tiles_x,

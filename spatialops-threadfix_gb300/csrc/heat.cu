@@ -506,7 +506,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
   const bool unit = sp[0] == 1.0 && sp[1] == 1.0 && sp[2] == 1.0;
   if constexpr (sizeof(T) == 8) {
     // z chunks in whole waves of resident blocks (a chunk re-reads one plane below it)
-    static int per_sm[2] = {0, 0};
+    static std::atomic<int> per_sm[2];  // zero: not queried
     const int bps = unit ? blocks_per_sm(heat_step_kernel<double, ExactD, MODE_UNIT>, BX * BY, per_sm[1])
                          : blocks_per_sm(heat_step_kernel<double, ExactD, MODE_REFERENCE>, BX * BY, per_sm[0]);
     const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);
@@ -524,16 +524,11 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     const bool vec = (vin.sy % 2 == 0) && ((uintptr_t)(vin.base - 1) % 8 == 0) && ((uintptr_t)(vl.base - 1) % 8 == 0);
     // one full wave: as many z chunks as the resident blocks allow (each chunk re-reads two
     // halo planes and fills the ring once, so more chunks than slots only cost)
-    static int per_sm[2] = {0, 0};
-    if (!per_sm[vec]) {
-      int v = 0;
-      const cudaError_t e =
-          vec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32x2_kernel, QX * QY, 0)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, heat_step_f32_async_kernel<false>, BX * BY, 0);
-      per_sm[vec] = (e == cudaSuccess && v > 0) ? v : 1;
-    }
+    static std::atomic<int> per_sm[2];  // zero: not queried
+    const int bps = vec ? blocks_per_sm(heat_step_f32x2_kernel, QX * QY, per_sm[1])
+                        : blocks_per_sm(heat_step_f32_async_kernel<false>, BX * BY, per_sm[0]);
     const int fyb = (n[1] + FTY - 1) / FTY;
-    int ch = max(1, min(num_sms() * per_sm[vec] / (gxb * fyb), (n[2] + 7) / 8));
+    int ch = max(1, min(num_sms() * bps / (gxb * fyb), (n[2] + 7) / 8));
     int zc = (n[2] + ch - 1) / ch;
     zc = (zc + NS - 1) / NS * NS;  // chunks start on a multiple of NS: constant ring stages
     ch = (n[2] + zc - 1) / zc;

@@ -478,8 +478,8 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
     if (al8(a.u) && al8(a.v) && al8(a.w) && al8(a.outS)) kind = 2;
   }
   // z chunks in whole waves of resident blocks (a chunk reads 2G halo planes beyond its own)
-  static int per_sm[3][2] = {{0, 0}, {0, 0}, {0, 0}};
-  int& cache = per_sm[kind][second];
+  static std::atomic<int> per_sm[3][2];  // zero: not queried
+  std::atomic<int>& cache = per_sm[kind][second];
   int ps;
   if (kind == 2)
     ps = second ? blocks_per_sm(transport_stage_f32_pair_kernel<true>, PTX * TY, cache)
