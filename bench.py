@@ -612,6 +612,17 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------- main
+def max_over_ranks(x, dist, device):
+    """x reduced with MAX over the ranks of dist's default group (x itself without a group)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -680,10 +691,7 @@ def main():
     prof = N.profile_report(reset=True)
     N.profile_enable(False)
     clocks = sampler.stop()
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, "cuda")
     value = world * W.cells * args.steps / (ms * 1e-3) / 1e9
 
     # e2e: host buffers, copies inside the timed region
@@ -703,10 +711,7 @@ def main():
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     e2e_value = world * W.cells * e_steps / (e2e_ms * 1e-3) / 1e9
 
     dom = DOMINANT[W.name]
@@ -734,7 +739,7 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu = None
-    if not args.no_cpu_baseline and W.name in ("deep", "heat", "heat32", "particles"):
+    if not args.no_cpu_baseline and world == 1 and W.name in ("deep", "heat", "heat32", "particles"):
         cpu = cpu_baseline(W.name, args.n)
     extra = {}
     if W.name == "adjoint":
