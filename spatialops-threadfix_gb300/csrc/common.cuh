@@ -80,7 +80,8 @@ class LaunchScope {
 
 // Make the current device's default memory pool keep freed blocks (release threshold = max) so
 // that stream-ordered allocations that recur every step (work lists, entry lists) are served
-// from the pool instead of the driver.  Once per device; a process-local pool setting.
+// from the pool instead of new CUDA driver allocations.  Once per device; a process-local pool
+// setting.
 void pool_retain();
 
 // Periodic ghost fill of one uniform-ghost patch (ghost.cu).

@@ -15,7 +15,7 @@ runs it on small seeded inputs and stores inputs and outputs as compressed .npz 
   particles.npz         CellToParticle / ParticleToCell (oracle/_ref/ref_particles) on the cases
                         of PARTICLE_CASES, incl. the reference's own 1-D test scene
 
-The GPU machine has no reference tree; it only reads these files.
+Machines without the reference tree (where the GPU tests run) only read these files.
 """
 from __future__ import annotations
 
