@@ -1,0 +1,67 @@
+"""The oracle's staggered operators against the reference's own convergence and filter tests
+(spatialops/structured/stencil/test/test_stencil2.cpp: Interpolant, Gradient and Divergence
+between a volume and its faces converge at second order in each direction; test_filter.cpp:
+the box filter keeps a constant field).  A check of the operator table's points and
+coefficients that does not go through golden vectors."""
+import numpy as np
+import pytest
+
+import oracle_dsl as O
+
+L = 10.0
+K = 2.0 * np.pi / L
+
+
+def _coord(loc, n, ghost, axis):
+    """Coordinate along `axis` of every window point (cell centres at (i + 1/2) dx; a location
+    staggered by -1/2 cell on an axis sits on the low faces)."""
+    g = O.glob_dims(loc, n, ghost, (0, 0, 0))[axis]
+    dx = L / n[axis]
+    return (np.arange(g) - ghost + 0.5 + 0.5 * O.OFFSET[loc][axis]) * dx
+
+
+def _field(loc, n, ghost, axis, fn):
+    gdims = O.glob_dims(loc, n, ghost, (0, 0, 0))
+    shape = (gdims[2], gdims[1], gdims[0])
+    c = _coord(loc, n, ghost, axis)
+    bshape = [1, 1, 1]
+    bshape[2 - axis] = len(c)
+    return np.broadcast_to(fn(c).reshape(bshape), shape).copy()
+
+
+def _max_error(op, axis, N):
+    n = [3, 3, 3]
+    n[axis] = N
+    n = tuple(n)
+    ghost = 1
+    db = O.OpDB(n, (L, L, L))
+    face = ("SSurfX", "SSurfY", "SSurfZ")[axis]
+    src, dst = ("SVol", face) if op != "div" else (face, "SVol")
+    # source sin(K x); exact result sin(K x) (interpolant) or K cos(K x) (gradient, divergence)
+    a = O.Field(src, _field(src, n, ghost, axis, lambda x: np.sin(K * x)), ghost)
+    exact = (lambda x: np.sin(K * x)) if op == "interp" else (lambda x: K * np.cos(K * x))
+    want = _field(dst, n, ghost, axis, exact)
+    stencil = {"interp": db.interp, "grad": db.grad, "div": db.div}[op](src, dst)
+    lhs = O.Field(dst, np.full_like(want, np.nan), ghost)
+    O.assign(lhs, stencil(a), use_ghost=False)
+    inner = (slice(ghost, -ghost),) * 3
+    return float(np.max(np.abs(lhs.data[inner] - want[inner])))
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("op", ["interp", "grad", "div"])
+def test_second_order_convergence(op, axis):
+    e = [_max_error(op, axis, N) for N in (16, 32, 64)]
+    orders = [np.log2(e[i] / e[i + 1]) for i in range(2)]
+    assert min(orders) > 1.9, (op, axis, e, orders)
+
+
+def test_box_filter_keeps_constants():
+    n, ghost = (9, 7, 5), 1
+    db = O.OpDB(n, (L, L, L))
+    g = O.glob_dims("SVol", n, ghost, (0, 0, 0))
+    a = O.Field("SVol", np.full((g[2], g[1], g[0]), 3.25), ghost)
+    lhs = O.Field("SVol", np.zeros((g[2], g[1], g[0])), ghost)
+    O.assign(lhs, db.filter()(a), use_ghost=False)
+    inner = (slice(ghost, -ghost),) * 3
+    assert np.max(np.abs(lhs.data[inner] - 3.25)) <= 1e-15 * 3.25
