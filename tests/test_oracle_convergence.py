@@ -65,3 +65,49 @@ def test_box_filter_keeps_constants():
     O.assign(lhs, db.filter()(a), use_ghost=False)
     inner = (slice(ghost, -ghost),) * 3
     assert np.max(np.abs(lhs.data[inner] - 3.25)) <= 1e-15 * 3.25
+
+
+def _field3(loc, n, ghost, fn):
+    gd = O.glob_dims(loc, n, ghost, (0, 0, 0))
+    cs = [_coord(loc, n, ghost, a) for a in range(3)]
+    z, y, x = np.meshgrid(cs[2], cs[1], cs[0], indexing="ij")
+    return np.ascontiguousarray(fn(x, y, z)).reshape(gd[2], gd[1], gd[0])
+
+
+@pytest.mark.parametrize("src,dst", [("XVol", "YVol"), ("XVol", "ZVol"), ("YVol", "ZVol"), ("SSurfX", "SSurfY")])
+def test_four_point_interpolant_second_order(src, dst):
+    # the reference's test_stencil4.cpp: interpolants staggered in two directions (4 points, 1/4)
+    fn = lambda x, y, z: np.sin(K * x) * np.cos(K * y) * np.sin(K * z + 0.3)
+    e = []
+    for N in (16, 32, 64):
+        n, ghost = (N, N, N), 1
+        db = O.OpDB(n, (L, L, L))
+        assert len(db.stencil4_points(src, dst)) == 4
+        a = O.Field(src, _field3(src, n, ghost, fn), ghost)
+        want = _field3(dst, n, ghost, fn)
+        lhs = O.Field(dst, np.full_like(want, np.nan), ghost)
+        O.assign(lhs, db.interp(src, dst)(a), use_ghost=False)
+        inner = (slice(ghost, -ghost),) * 3
+        e.append(float(np.max(np.abs(lhs.data[inner] - want[inner]))))
+    orders = [np.log2(e[i] / e[i + 1]) for i in range(2)]
+    assert min(orders) > 1.9, (src, dst, e, orders)
+
+
+def test_chained_stencils_equal_materialised():
+    # the reference's test_chain_stencil.cpp: Interp(Grad(a)) evaluated in one assignment equals
+    # the same two steps through a materialised intermediate field, bit for bit
+    n, ghost = (11, 9, 7), 1
+    db = O.OpDB(n, (L, 7.0, 5.0))
+    rng = np.random.default_rng(3)
+    gs = O.glob_dims("SVol", n, ghost, (0, 0, 0))
+    a = O.Field("SVol", rng.uniform(-1, 1, (gs[2], gs[1], gs[0])), ghost)
+    gx = O.glob_dims("SSurfX", n, ghost, (0, 0, 0))
+    tmp = O.Field("SSurfX", np.full((gx[2], gx[1], gx[0]), np.nan), ghost)
+    O.assign(tmp, db.grad("SVol", "SSurfX")(a))
+    two = O.Field("SVol", np.full((gs[2], gs[1], gs[0]), np.nan), ghost)
+    O.assign(two, db.interp("SSurfX", "SVol")(tmp))
+    one = O.Field("SVol", np.full((gs[2], gs[1], gs[0]), np.nan), ghost)
+    O.assign(one, db.interp("SSurfX", "SVol")(db.grad("SVol", "SSurfX")(a)))
+    written = ~np.isnan(one.data)
+    assert np.array_equal(written, ~np.isnan(two.data)) and written.any()
+    assert np.array_equal(one.data[written].view(np.uint64), two.data[written].view(np.uint64))
