@@ -111,3 +111,36 @@ def test_chained_stencils_equal_materialised():
     written = ~np.isnan(one.data)
     assert np.array_equal(written, ~np.isnan(two.data)) and written.any()
     assert np.array_equal(one.data[written].view(np.uint64), two.data[written].view(np.uint64))
+
+
+def test_deep_chain_equals_stepwise():
+    # the reference's test/StencilTestDeepChain.cpp: the deep chain
+    #   out <<= cond(mask, 0)(I(G(I(a))) * exp(b) + sin(c))
+    # evaluated in one assignment equals the same chain through materialised intermediates,
+    # bit for bit, on every cell both write
+    n, ghost = (10, 8, 6), 1
+    db = O.OpDB(n, (L, 8.0, 6.0))
+    rng = np.random.default_rng(5)
+
+    def fld(loc, fill=None):
+        g = O.glob_dims(loc, n, ghost, (0, 0, 0))
+        data = rng.uniform(-1, 1, (g[2], g[1], g[0])) if fill is None else np.full((g[2], g[1], g[0]), fill)
+        return O.Field(loc, data, ghost)
+
+    a, b, c = fld("SVol"), fld("XVol"), fld("XVol")
+    g = O.glob_dims("XVol", n, ghost, (0, 0, 0))
+    pts = [(1, 1, 1), (3, 2, 0), (0, 0, 4), (7, 5, 2)]
+    mask = O.Mask.from_points("XVol", pts, g, ghost)
+    I1, G1, I2 = db.interp("SVol", "XVol"), db.grad("XVol", "SVol"), db.interp("SVol", "XVol")
+    fused = fld("XVol", np.nan)
+    O.assign(fused, O.cond(mask, 0.0, I2(G1(I1(a))) * O.exp(b) + O.sin(c)))
+    t1, t2 = fld("XVol", np.nan), fld("SVol", np.nan)
+    O.assign(t1, I1(a))
+    O.assign(t2, G1(t1))
+    t3 = fld("XVol", np.nan)
+    O.assign(t3, I2(t2))
+    step = fld("XVol", np.nan)
+    O.assign(step, O.cond(mask, 0.0, t3 * O.exp(b) + O.sin(c)))
+    both = ~np.isnan(fused.data) & ~np.isnan(step.data)
+    assert both.sum() >= 0.5 * np.prod(n)
+    assert np.array_equal(fused.data[both].view(np.uint64), step.data[both].view(np.uint64))
