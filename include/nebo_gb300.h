@@ -229,7 +229,10 @@ int nebo_patchset_run(nebo_patchset* ps, int start, int steps, int use_graph, in
  * u, v, w (XVol/YVol/ZVol face velocities) and lambda: windows of the same shape in `dtype`.
  * dtype NEBO_F32: FP32 storage and stencil arithmetic, FP64 time accumulation (phi stays FP64);
  * dtype NEBO_F64: everything FP64.  work: device scratch of nebo_transport_work_bytes bytes.
- * Each RK stage is one kernel. */
+ * Each RK stage is one kernel.  FP32 with n even: staged planes (8-byte copies), and with every
+ * float field 8-byte aligned two cells per thread in packed FP32x2 arithmetic; odd n or
+ * unaligned fields take a one-cell kernel (same results within FP32 rounding).  The coefficient
+ * ghost fills and the FP32 copy of the state are made once per call: run many steps per call. */
 size_t nebo_transport_work_bytes(int n, int dtype);
 int nebo_transport_run(double* phi, const void* u, const void* v, const void* w, const void* lam,
                        int n, int steps, double dt, double nu, int dtype, void* work,
