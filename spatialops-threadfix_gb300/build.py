@@ -46,11 +46,14 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, obj, extra=()):
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+def _compile(src, obj, extra=(), resources=False):
+    cmd = [nvcc(), *NVCC_FLAGS, *extra, *(["-Xptxas", "-v"] if resources else []), "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stderr}")
+    if resources:  # ptxas's register / shared memory / spill report per kernel, beside the object
+        with open(obj + ".resources.txt", "w") as f:
+            f.write(r.stderr)
     return obj
 
 
@@ -106,7 +109,7 @@ def build_library(verbose=False, extra_flags=()):
         for s in srcs:
             o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
             if _stale(o, [s, *hdrs, __file__]):
-                jobs.append(ex.submit(_compile, s, o, extra_flags))
+                jobs.append(ex.submit(_compile, s, o, extra_flags, True))
         for j in jobs:
             j.result()
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
