@@ -387,18 +387,19 @@ __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlo
 
 // 128-bit fixed point for exact sums of doubles that share one scale.  A plane (tile) whose
 // largest biased exponent is E counts in units of 2^(E-1144): |x| < 2^(E-1022) becomes an
-// integer below 2^122, 27 of them stay below 2^127, and every x down to 2^-69 of the plane's
-// largest keeps all of its 53 bits.  Integer pipe only.
+// integer below 2^122, sums of up to 32 of them stay below 2^127, and every x down to 2^-69 of
+// the plane's largest keeps all of its 53 bits.  Integer pipe only; host and device (the host
+// build is what tests/cpp/fixpoint_host.cu checks against exact rational arithmetic).
 typedef __int128 fix128;
 
-__device__ __forceinline__ fix128 make128(long long hi, unsigned long long lo) {
+__host__ __device__ __forceinline__ fix128 make128(long long hi, unsigned long long lo) {
   return (fix128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
 }
 
 // x (biased exponent <= E, not inf/NaN) in units of 2^(E-1144), rounded to nearest (halves up):
 // the 53-bit significand m lands at bit sh = e - E + 69 <= 69 of a 128-bit integer.
-__device__ __forceinline__ fix128 to_units(double x, int E) {
-  const long long b = __double_as_longlong(x);
+__host__ __device__ __forceinline__ fix128 to_units(double x, int E) {
+  const long long b = (long long)bits(x);
   const int e = (int)((b >> 52) & 0x7ff);
   const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
   const int sh = (e ? e : 1) - E + 69;
@@ -418,19 +419,19 @@ __device__ __forceinline__ fix128 to_units(double x, int E) {
 }
 
 // RN(t 2^u) for t != 0, assuming the result is normal.
-__device__ __forceinline__ double units_to_double(fix128 t, int u) {
+__host__ __device__ __forceinline__ double units_to_double(fix128 t, int u) {
   const bool neg = t < 0;
   const unsigned __int128 a = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
   const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
   unsigned long long top, rest;
   int msb;  // position of the leading bit
   if (hi) {
-    const int lz = __clzll(hi);
+    const int lz = clz64(hi);
     top = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
     rest = lo << lz;  // bits below `top` (only whether any is set matters)
     msb = 127 - lz;
   } else {
-    const int lz = __clzll(lo);
+    const int lz = clz64(lo);
     top = lo << lz;
     rest = 0;
     msb = 63 - lz;
@@ -444,13 +445,15 @@ __device__ __forceinline__ double units_to_double(fix128 t, int u) {
     mant >>= 1;
     ++ex;
   }
-  const unsigned long long bits = ((unsigned long long)neg << 63) | ((unsigned long long)ex << 52) |
-                                  (mant & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long out = ((unsigned long long)neg << 63) | ((unsigned long long)ex << 52) |
+                                 (mant & 0xFFFFFFFFFFFFFull);
+  return from_bits(out);
 }
 
 // RN(t 2^u), +0 for t == 0, assuming a nonzero result is normal.
-__device__ __forceinline__ double units_to_double0(fix128 t, int u) { return t == 0 ? 0.0 : units_to_double(t, u); }
+__host__ __device__ __forceinline__ double units_to_double0(fix128 t, int u) {
+  return t == 0 ? 0.0 : units_to_double(t, u);
+}
 
 // A divisor whose reciprocal div_by may use: positive, exponent within 2^+-400 (integer pipe).
 __device__ __forceinline__ bool divisor_ok(double b) {
