@@ -144,6 +144,21 @@ def heat_label(n, dtype):
     return f"heat {n}^3 + 1 ghost, {'FP64 bit-exact' if dtype == 'f64' else 'FP32'} fused RHS + Euler update"
 
 
+def transport_label(n, dtype):
+    return (f"transport {n}^3 + 2 ghosts, Heun RK2 step, "
+            f"{'FP64' if dtype == 'f64' else 'FP32 storage, FP64 state accumulation'}")
+
+
+def patches_label(count, cells, dtype):
+    return (f"{count} heat patches, edges ~ U{{16..96}}, 1 ghost, {cells / 1e6:.1f} M cells, "
+            f"{'FP64' if dtype == 'f64' else 'FP32'}; one persistent launch per step")
+
+
+def adjoint_label(n, steps):
+    return (f"adjoint {n}^3 + 1 ghost, {steps} FP64 steps, sqrt(N) checkpoints; FP64 adjoint state, "
+            f"FP32 face products in dJ/dlambda")
+
+
 def particles_label(n, npart):
     return (f"particles: {n}^3 SVol + 1 ghost, {npart / 1e6:.1f} M particles (edges U(0.5,1.5) cells, "
             f"random order); step = CellToParticle + ParticleToCell, FP64, bit-identical to the reference")
@@ -287,8 +302,7 @@ class Patches:
         self.ps.arena(0).copy_(self.host)
         self.ps.fill_ghosts(0)
         self.cells = int(np.prod(shapes.astype(np.int64), axis=1).sum())
-        self.label = (f"{count} heat patches, edges ~ U{{16..96}}, 1 ghost, {self.cells / 1e6:.1f} M cells, "
-                      f"{'FP64' if dtype == 'f64' else 'FP32'}; one persistent launch per step")
+        self.label = patches_label(count, self.cells, dtype)
         self.launches_per_step = 1
         self.h2d_bytes = self.host.numel() * self.host.element_size()
         self.d2h_bytes = 8
@@ -321,8 +335,7 @@ class TransportWL:
         from spatialops_gb300 import workloads as W
 
         self.name = "transport" if dtype == "f64" else "transport32"
-        self.label = (f"transport {n}^3 + 2 ghosts, Heun RK2 step, "
-                      f"{'FP64' if dtype == 'f64' else 'FP32 storage, FP64 state accumulation'}")
+        self.label = transport_label(n, dtype)
         self.N, self.n = N, n
         phi, u, v, w, lam, dt, nu = W.transport_inputs_device(n)
         self.t = N.Transport(np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)), np.zeros((1, 1, 1)),
@@ -384,8 +397,7 @@ class AdjointWL:
         self.d2h_bytes = 8
         self.J = 0.0
         self.products = "f32"
-        self.label = (f"adjoint {n}^3 + 1 ghost, {steps} FP64 steps, sqrt(N) checkpoints; FP64 adjoint state, "
-                      f"FP32 face products in dJ/dlambda")
+        self.label = adjoint_label(n, steps)
         self.metric = "adjoint gradient forward-cell-steps/s"
         self.cells_per_launch = n ** 3
 
@@ -539,6 +551,56 @@ def cpu_particles(n, npart):
     return time.perf_counter() - t0
 
 
+def cpu_transport(m):
+    """A sampler: one Heun RK2 step of the FP64 transport on an m^3 periodic patch by the oracle
+    (inputs made once); sampler(threads) returns seconds."""
+    O = _oracle()
+    from spatialops_gb300 import workloads as W
+
+    phi, u, v, w, lam, dt, nu = W.transport_inputs(m)
+
+    def run(threads):
+        t0 = time.perf_counter()
+        O.transport_run(phi, u, v, w, lam, m, 1, dt, nu, threads)
+        return time.perf_counter() - t0
+
+    return run
+
+
+def cpu_gradient(m, steps):
+    """A sampler: the heat gradient (forward run plus the reverse sweep) over `steps` steps on an
+    m^3 patch by the serial oracle (inputs made once); sampler(threads) returns seconds."""
+    O = _oracle()
+    from spatialops_gb300 import workloads as W
+
+    n = (m, m, m)
+    lam, T0, dt, _ = W.adjoint_inputs(n)
+
+    def run(threads):
+        t0 = time.perf_counter()
+        TN = O.heat_run(lam, T0, n, steps, dt)
+        O.heat_adjoint(T0, lam, TN - T0, n, steps, dt)
+        return time.perf_counter() - t0
+
+    return run
+
+
+# One bounded sample of each workload by the oracle: (function(threads) -> seconds, units, what).
+# Slab and cube sizes keep a sample well under a second of host time per thread.
+def cpu_sample(workload, n):
+    if workload in ("deep", "heat", "heat32", "patches", "patches32"):
+        kind = "deep" if workload == "deep" else "heat"
+        what = f"{n}x{n}x16 slab of {kind} steps"
+        return (lambda th: cpu_run(kind, n, 16, th)), n * n * 16, what
+    if workload in ("transport", "transport32"):
+        m = 128
+        return cpu_transport(m), m ** 3, f"one FP64 RK2 step on a {m}^3 periodic patch"
+    if workload == "adjoint":
+        m, steps = 48, 20
+        return cpu_gradient(m, steps), m ** 3 * steps, f"gradient over {steps} steps of a {m}^3 patch"
+    raise ValueError(workload)
+
+
 def cpu_baseline(workload, n, budget_s=10.0):
     """Serial oracle (1 core) on the full workload, repeated until ~budget_s of CPU work."""
     if workload == "particles":
@@ -550,13 +612,21 @@ def cpu_baseline(workload, n, budget_s=10.0):
         return {"value": reps * npart / total / 1e9, "unit": "Gparticle/s", "cores": 1, "kind": "port",
                 "sample": f"{reps} x (CellToParticle + ParticleToCell of {npart} particles on the {n}^3 field), "
                           f"serial oracle loops (the reference's operators are serial), {total:.1f} s"}
+    if workload in ("deep", "heat", "heat32"):
+        reps, total = 0, 0.0
+        while total < budget_s and reps < 20:
+            total += cpu_run("deep" if workload == "deep" else "heat", n, n, 1)
+            reps += 1
+        cells = reps * n ** 3
+        return {"value": cells / total / 1e9, "unit": "Gcell-upd/s", "cores": 1, "kind": "port",
+                "sample": f"{reps} full {n}^3 step(s) of the {workload} workload, serial oracle walk, {total:.1f} s"}
+    fn, units, what = cpu_sample(workload, n)
     reps, total = 0, 0.0
-    while total < budget_s and reps < 20:
-        total += cpu_run("deep" if workload == "deep" else "heat", n, n, 1)
+    while total < budget_s and reps < 50:
+        total += fn(1)
         reps += 1
-    cells = reps * n ** 3
-    return {"value": cells / total / 1e9, "unit": "Gcell-upd/s", "cores": 1, "kind": "port",
-            "sample": f"{reps} full {n}^3 step(s) of the {workload} workload, serial oracle walk, {total:.1f} s"}
+    return {"value": reps * units / total / 1e9, "unit": "Gcell-upd/s", "cores": 1, "kind": "port",
+            "sample": f"{reps} x ({what}), serial oracle, {total:.1f} s"}
 
 
 def run_reference(args):
@@ -586,25 +656,36 @@ def run_reference(args):
         }
         print(json.dumps(line), flush=True)
         return 0
-    nz = 16
-    workload = args.workload if args.workload in ("deep", "heat") else "heat"
+    fn, units, what = cpu_sample(args.workload, n)
     for _ in range(max(args.warmup, 0)):
-        cpu_run(workload, n, nz, threads)
+        fn(threads)
     t = 0.0
     for _ in range(args.steps):
-        t += cpu_run(workload, n, nz, threads)
-    cells = args.steps * n * n * nz
-    value = cells / t / 1e9
+        t += fn(threads)
+    value = args.steps * units / t / 1e9
+    w = args.workload
+    if w in ("deep", "heat", "heat32"):
+        label = deep_label(n) if w == "deep" else heat_label(n, "f64" if w == "heat" else "f32")
+    elif w in ("transport", "transport32"):
+        label = transport_label(n, "f64" if w == "transport" else "f32")
+    elif w in ("patches", "patches32"):
+        from spatialops_gb300 import workloads as W
+
+        cells = int(np.prod(W.patch_shapes(512).astype(np.int64), axis=1).sum())
+        label = patches_label(512, cells, "f64" if w == "patches" else "f32")
+    else:
+        label = adjoint_label(192 if n == N_DEFAULT else n, 500)
+    metric = "adjoint gradient forward-cell-steps/s" if w == "adjoint" else f"{w} cell-updates/s"
     line = {
-        "impl": "reference", "metric": f"{workload} cell-updates/s", "value": value, "unit": "Gcell-upd/s",
+        "impl": "reference", "metric": metric, "value": value, "unit": "Gcell-upd/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if workload != "heat32" else "f32", "data": "synthetic (seeded)",
-        "config": {"workload": deep_label(n) if workload == "deep" else heat_label(n, "f64"),
-                   "cells_per_step": n * n * nz, "sample": f"{n}x{n}x{nz} slab per step"},
-        "cpu_baseline": {"value": value, "unit": "Gcell-upd/s", "cores": threads, "kind": "port",
-                         "sample": f"{n}x{n}x{nz} slab of the {n}^3 {workload} workload per step, "
-                                   f"oracle restatement of the reference's serial walk, z-slabs over {threads} threads"},
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": label, "cells_per_step": units, "sample": what + " per step"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-upd/s", "cores": 1 if w == "adjoint" else threads,
+                         "kind": "port",
+                         "sample": f"{what} per step, oracle restatement of the reference's serial walk"
+                                   + (", serial" if w == "adjoint" else f", z-slabs over {threads} threads")},
         "e2e": {"value": value, "unit": "Gcell-upd/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -739,7 +820,7 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu = None
-    if not args.no_cpu_baseline and world == 1 and W.name in ("deep", "heat", "heat32", "particles"):
+    if not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(W.name, args.n)
     extra = {}
     if W.name == "adjoint":

@@ -19,7 +19,7 @@ def _line(*args):
     return json.loads(lines[0])
 
 
-@pytest.mark.parametrize("workload", ["deep", "particles"])
+@pytest.mark.parametrize("workload", ["deep", "particles", "heat32", "transport32", "patches", "adjoint"])
 def test_reference_arm_line(workload):
     sys.path.insert(0, REPO)
     import bench
@@ -36,5 +36,14 @@ def test_reference_arm_line(workload):
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     n = bench.N_DEFAULT
-    want = bench.deep_label(n) if workload == "deep" else bench.particles_label(n, n ** 3)
+    bench.graft._import_pkg()
+    from spatialops_gb300 import workloads as W
+
+    cells = int(sum(int(a) * int(b) * int(c) for a, b, c in W.patch_shapes(512)))
+    want = {"deep": bench.deep_label(n), "particles": bench.particles_label(n, n ** 3),
+            "heat32": bench.heat_label(n, "f32"), "transport32": bench.transport_label(n, "f32"),
+            "patches": bench.patches_label(512, cells, "f64"), "adjoint": bench.adjoint_label(192, 500)}[workload]
     assert d["config"]["workload"] == want
+    metric = {"particles": "particle cell<->particle exchanges/s",
+              "adjoint": "adjoint gradient forward-cell-steps/s"}.get(workload, f"{workload} cell-updates/s")
+    assert d["metric"] == metric
