@@ -120,10 +120,12 @@ int nebo_reduce_all(const nebo_field* f, int interior, double* d_out4, nebo_stre
  * framework that reserved the device memory up front in its own pool, so another allocation
  * fails or breaks its accounting; code running where the allocator may not be entered).  The
  * block partials live in a fixed device array of 1024 slots (16 KiB, held on every GPU that
- * loads the library until exit); a reduction that would need more slots is rejected with
- * NEBO_ERR_INVALID.  The first call on a device looks the array up (cudaGetSymbolAddress) with
- * that device current and should come before any stream capture.  All calls share the array:
- * calls whose kernels overlap on the GPU race on it.  The result is written to d_result. */
+ * loads the library until exit); a reduction takes at most 1024 blocks, one slot each, whatever
+ * the GPU's SM count.  A region of more than 2^31 - 1 rows (y * z extent) is rejected with
+ * NEBO_ERR_INVALID before any CUDA call.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) with that device current and should come before any stream capture;
+ * the address is cached, and a cudaDeviceReset voids it.  All calls share the array: calls whose
+ * kernels overlap on the GPU race on it.  The result is written to d_result. */
 int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, double* d_result,
                         nebo_stream_t stream);
 

@@ -13,6 +13,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <spatialops/NeboCore.h>
 #include <spatialops/NeboOperators.h>
 
@@ -39,14 +41,24 @@ __global__ void __launch_bounds__(256) nebo_masked_assign_kernel(T* __restrict__
   }
 }
 
+// SM count of the current device, cached per device.  Relaxed atomics: several host threads may
+// launch at once; each either reads 0 (and queries) or a value some thread stored.
 inline int device_sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
   }
+  const bool cached = dev >= 0 && dev < kMaxDevices;
+  int n = cached ? cache[dev].load(std::memory_order_relaxed) : 0;
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = 152;
+  }
+  if (cached) cache[dev].store(n, std::memory_order_relaxed);
   return n;
 }
 
@@ -76,7 +88,8 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
   typedef typename F::value_type T;
   int32_t lim[6];
   if (!write_region(lhs, rhs, useGhost, lim)) return;
-  const auto dev = rhs.device();  // uploads any input edited on the host
+  LaunchStreamScope scope(lhs.get_stream());
+  const auto dev = rhs.device();  // uploads any input edited on the host; orders other streams' writes
   T* out = lhs.device_values_for_write() + lhs.interior_origin();
   const int sy = (int)lhs.window_with_ghost().glob_dim(0);
   const long sz = (long)lhs.window_with_ghost().glob_dim(0) * (long)lhs.window_with_ghost().glob_dim(1);
@@ -100,6 +113,7 @@ void masked(const SpatialMask<F>& mask, F& lhs, const Node& rhs) {
   typedef typename F::value_type T;
   const int np = mask.num_points();
   if (np == 0) return;
+  LaunchStreamScope scope(lhs.get_stream());
   auto dev = rhs.device();
   T* out = lhs.device_values_for_write() + lhs.interior_origin();
   const int sy = (int)lhs.window_with_ghost().glob_dim(0);

@@ -24,6 +24,7 @@
 #include <limits>
 #include <sstream>
 #include <stdexcept>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -377,6 +378,36 @@ struct DSumStencil {
   __device__ __forceinline__ T eval(int x, int y, int z) const { return StencilFold<Pts>::template sum<T>(a, x, y, z); }
 };
 
+// ============================================================================ stream order
+// The stream of the kernel being lowered.  A launching call (assign, masked, a reduction, a BC
+// builder) names it for the duration of its lowering; every field leaf read on another stream
+// then makes it wait for that stream's work, so a kernel never reads a field that an earlier
+// call on another stream is still writing.
+inline nebo_stream_t& launch_stream() {
+  static thread_local nebo_stream_t s = nullptr;
+  return s;
+}
+struct LaunchStreamScope {
+  nebo_stream_t saved;
+  explicit LaunchStreamScope(nebo_stream_t s) : saved(launch_stream()) { launch_stream() = s; }
+  ~LaunchStreamScope() { launch_stream() = saved; }
+};
+inline void order_read(nebo_stream_t field_stream) {
+  const nebo_stream_t s = launch_stream();
+  if (field_stream == s) return;
+  cudaEvent_t e;
+  cudaError_t rc = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  if (rc == cudaSuccess) {
+    rc = cudaEventRecord(e, (cudaStream_t)field_stream);
+    if (rc == cudaSuccess) rc = cudaStreamWaitEvent((cudaStream_t)s, e, 0);
+    cudaEventDestroy(e);
+  }
+  if (rc != cudaSuccess) {
+    cudaGetLastError();
+    throw std::runtime_error(std::string("Nebo error in Nebo Assignment (stream order):\n") + cudaGetErrorString(rc));
+  }
+}
+
 // ============================================================================ host nodes
 // Ghost-analysis interface of every node (NeboRhs.h / NeboOperators.h "Initial" mode).
 template <typename T>
@@ -406,6 +437,7 @@ struct FieldNode {
   void prepare() const { f.device_values_for_read(); }
   DField<value_type> device() const {
     const value_type* base = f.device_values_for_read();
+    order_read(f.get_stream());
     return DField<value_type>{base + f.interior_origin(), (int)f.window_with_ghost().glob_dim(0),
                               (long)f.window_with_ghost().glob_dim(0) * (long)f.window_with_ghost().glob_dim(1)};
   }

@@ -88,6 +88,7 @@ double fold_expr(const Node& e, bool useGhost, int op) {
   double r0 = op == NEBO_RED_MAX ? -std::numeric_limits<double>::infinity()
               : op == NEBO_RED_MIN ? std::numeric_limits<double>::infinity() : 0.0;
   if (nrows <= 0 || hi[0] <= lo[0]) return op == NEBO_RED_NORM ? 0.0 : r0;
+  LaunchStreamScope scope(nullptr);  // the fold runs on the default stream
   const auto dev = e.device();
   int blocks = (int)(nrows < 4L * device_sm_count() ? nrows : 4L * device_sm_count());
   void* p = nullptr;

@@ -377,7 +377,8 @@ struct NeboBoundaryConditionBuilder {
     typedef nebo_detail::BinNode<nebo_detail::OpDiv, Diff, nebo_detail::ScalarNode<T>> Rhs;
     const Rhs rhs(Diff(GS(g, NeboStencilCoefCollection<1>(1.0)), PS(nebo_detail::FieldNode<PhiFieldType>(phi), pc)),
                   nebo_detail::ScalarNode<T>((T)coef));
-    const auto dev = rhs.device();  // uploads any input edited on the host
+    nebo_detail::LaunchStreamScope scope(phi.get_stream());
+    const auto dev = rhs.device();  // uploads any input edited on the host; orders other streams' writes
     T* out = phi.device_values_for_write() + phi.interior_origin();
     const int sy = (int)phi.window_with_ghost().glob_dim(0);
     const long sz = (long)phi.window_with_ghost().glob_dim(0) * (long)phi.window_with_ghost().glob_dim(1);

@@ -366,6 +366,7 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
   const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
   const size_t bytes = cells * sizeof(double);
   int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
+  if (L > steps) L = steps;  // a segment never holds more than the run's states
   if (checkpoint_every == NEBO_CHECKPOINT_AUTO) {
     // every state kept (no recomputation) when steps + 7 fields fit in 80 % of the free memory
     size_t free_b = 0, total_b = 0;

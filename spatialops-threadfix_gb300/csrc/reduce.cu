@@ -260,7 +260,9 @@ extern "C" int nebo_reduce(const nebo_field* f, int op, int interior, double* re
 // The array lives in this module's device memory for every GPU that loads the library, until the
 // process exits.  Host code cannot use the symbol's name as a device address, so the first call
 // on each device (with that device current) looks the address up with cudaGetSymbolAddress and
-// caches it; that first call should come before any stream capture.  All calls share the array
+// caches it (a cudaDeviceReset voids the cached address: a process that resets a device must not
+// call this entry point on it afterwards); that first call should come before any stream capture.
+// A reduction takes at most 1024 blocks, one slot each.  All calls share the array
 // and it keeps the last call's contents: pass 1 writes every slot that pass 2 reads, so nothing
 // needs clearing, but calls whose kernels overlap on the GPU (different streams, no ordering
 // between them) race on it.
@@ -268,6 +270,7 @@ namespace nebo {
 namespace {
 
 constexpr int NOALLOC_MAX_PARTIALS = 1024;  // 16 KiB: one (sum, compensation) pair per block
+constexpr long NOALLOC_MAX_ROWS = 2147483647L;  // rows (y * z) of the reduced region
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static __device__ __align__(256) Acc g_noalloc_partials[NOALLOC_MAX_PARTIALS];
 
@@ -303,12 +306,15 @@ extern "C" int nebo_reduce_noalloc(const nebo_field* f, int op, int interior, do
   reduction_region(*f, interior, lo, hi);
   const long nrows = (long)(hi[1] - lo[1]) * (hi[2] - lo[2]);
   if (nrows <= 0 || hi[0] <= lo[0]) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_reduce_noalloc: empty region");
-  const long want = nrows < (long)num_sms() * 4 ? nrows : (long)num_sms() * 4;
-  if (want > NOALLOC_MAX_PARTIALS)
+  // The row walk takes an int row count; larger regions are refused before any CUDA call.
+  if (nrows > NOALLOC_MAX_ROWS)
     return fail(NEBO_ERR_INVALID,
-                "Nebo error in nebo_reduce_noalloc: the reduction needs %ld partial slots but the static scratch "
-                "holds %d",
-                want, NOALLOC_MAX_PARTIALS);
+                "Nebo error in nebo_reduce_noalloc: the region has %ld rows, more than the %ld this entry point takes",
+                nrows, (long)NOALLOC_MAX_ROWS);
+  // One partial slot per block, and never more blocks than slots: the grid-stride row walk covers
+  // any region with fewer blocks, so the fixed array suffices whatever the SM count.
+  long want = nrows < (long)num_sms() * 4 ? nrows : (long)num_sms() * 4;
+  if (want > NOALLOC_MAX_PARTIALS) want = NOALLOC_MAX_PARTIALS;
   const int blocks = (int)want;
   Acc* partials = nullptr;
   if ((rc = noalloc_partials(&partials))) return rc;

@@ -107,7 +107,7 @@ def run(cmd):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("NEBO_REFERENCE", "/root/reference"))
     args = ap.parse_args()
     run(["make", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}"])
     drv = os.path.join(REPO, "oracle", "_ref", "ref_driver")
