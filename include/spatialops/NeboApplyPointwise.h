@@ -23,11 +23,15 @@ namespace nebo_detail {
 template <class... D>
 struct DTuple;
 template <>
-struct DTuple<> {};
+struct DTuple<> {
+  __device__ __forceinline__ void rebase(int, int, int) {}
+  template <int K> __device__ __forceinline__ void fill(int, int, int) const {}
+};
 template <class H, class... R>
 struct DTuple<H, R...> {
   H h;
   DTuple<R...> r;
+  NEBO_TWO_CHILDREN(h, r)
 };
 
 inline DTuple<> make_dtuple() { return DTuple<>(); }
@@ -56,6 +60,7 @@ template <typename T, class Fn, class... D>
 struct DApply {
   DTuple<D...> ops;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return ApplyCall<T, Fn>::go(ops, x, y, z); }
+  NEBO_ONE_CHILD(ops)
 };
 
 template <class... F>

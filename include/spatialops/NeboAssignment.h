@@ -5,9 +5,14 @@
 //   1. the write region: calculate_actual_ghost(lhs ghosts, lhs BC, expr.ghosts_with_bc())
 //      (nebo_write_limits in the C ABI, the reference's rule, spatialops/NeboBasic.h:61-100);
 //   2. every field the expression reads is made current on the GPU;
-//   3. ONE kernel, nebo_assign_kernel<T, Functor>, evaluates the fused tree over the region.
-// The launch geometry: 32 lanes along x (coalesced), 8 warps along y, and enough z-chunks for
-// about 8 resident blocks per SM; each thread marches its chunk of z planes.
+//   3. ONE kernel evaluates the fused tree over the region:
+//      * an expression with a stencil of an expression (a nested chain, a divergence of face
+//        fluxes) runs as nebo_tiled_assign_kernel (NeboTiled.h): 32 x 8 x TZ tiles, each inner
+//        level materialised once per tile in shared memory;
+//      * any other runs as nebo_assign_kernel<T, Functor>: 32 lanes along x (coalesced), 8 warps
+//        along y, and enough z-chunks for about 8 resident blocks per SM; each thread marches its
+//        chunk of z planes.
+//   NEBO_UNTILED keeps every expression on the second form (for comparisons).
 #ifndef SpatialOps_NeboAssignment_h
 #define SpatialOps_NeboAssignment_h
 
@@ -17,6 +22,7 @@
 
 #include <spatialops/NeboCore.h>
 #include <spatialops/NeboOperators.h>
+#include <spatialops/NeboTiled.h>
 
 namespace SpatialOps {
 namespace nebo_detail {
@@ -83,6 +89,9 @@ bool write_region(const F& lhs, const Node& rhs, bool useGhost, int32_t lim[6]) 
   return lim[1] > lim[0] && lim[3] > lim[2] && lim[5] > lim[4];
 }
 
+template <typename T, class D>
+void assign_plain(T* out, int sy, long sz, const int32_t lim[6], const D& dev, cudaStream_t s);
+
 template <class F, class Node>
 void assign(F& lhs, const Node& rhs, bool useGhost) {
   typedef typename F::value_type T;
@@ -94,6 +103,35 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
   const int sy = (int)lhs.window_with_ghost().glob_dim(0);
   const long sz = (long)lhs.window_with_ghost().glob_dim(0) * (long)lhs.window_with_ghost().glob_dim(1);
   const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
+  cudaStream_t s = (cudaStream_t)lhs.get_stream();
+  typedef typename std::decay<decltype(dev)>::type D;
+#ifndef NEBO_UNTILED
+  if constexpr (TilePlan<D>::tz > 0) {
+    // nested stencils: one block per 32 x 8 x TZ tile, inner levels materialised in shared memory
+    constexpr int TZ = TilePlan<D>::tz;
+    typedef typename TileAt<D, TZ>::type Plan;
+    typedef typename Plan::type DT;
+    const DT dt = Plan::make(dev);
+    constexpr int smem = Plan::end;
+    auto kern = nebo_tiled_assign_kernel<T, DT, TZ, Plan::rounds>;
+    if (smem > 48 * 1024)
+      throw_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                 "Nebo Assignment (shared memory)");
+    const dim3 grid((nx + kTileX - 1) / kTileX, (ny + kTileY - 1) / kTileY, (nz + TZ - 1) / TZ);
+    kern<<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(out, sy, sz, lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], dt);
+    throw_cuda(cudaGetLastError(), "Nebo Assignment (kernel launch)");
+  } else {
+    assign_plain<T>(out, sy, sz, lim, dev, s);
+  }
+#else
+  assign_plain<T>(out, sy, sz, lim, dev, s);
+#endif
+}
+
+// The one-pass form: one thread per (x, y) column of a z-chunk.
+template <typename T, class D>
+void assign_plain(T* out, int sy, long sz, const int32_t lim[6], const D& dev, cudaStream_t s) {
+  const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
   dim3 block(32, 8, 1);
   dim3 grid((nx + 31) / 32, (ny + 7) / 8, 1);
   const long plane_blocks = (long)grid.x * grid.y;
@@ -102,8 +140,7 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
   if (chunks > nz) chunks = nz;
   const int zchunk = (int)((nz + chunks - 1) / chunks);
   grid.z = (unsigned)((nz + zchunk - 1) / zchunk);
-  cudaStream_t s = (cudaStream_t)lhs.get_stream();
-  nebo_assign_kernel<T, typename std::decay<decltype(dev)>::type><<<grid, block, 0, s>>>(
+  nebo_assign_kernel<T, D><<<grid, block, 0, s>>>(
       out, sy, sz, lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], zchunk, dev);
   throw_cuda(cudaGetLastError(), "Nebo Assignment (kernel launch)");
 }

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include <nebo_gb300.h>
+#include <spatialops/NeboFixMath.h>
 #include <spatialops/structured/FVStaggeredFieldTypes.h>
 #include <spatialops/structured/GhostData.h>
 #include <spatialops/structured/IndexTriplet.h>
@@ -105,10 +106,22 @@ struct OpMin { template <class T> static __device__ __forceinline__ T apply(T a,
 #define NEBO_UNARY_FN(NAME, EXPR) \
   struct NAME { template <class T> static __device__ __forceinline__ T apply(T a) { return EXPR; } };
 NEBO_UNARY_FN(FnNeg, -a)
-NEBO_UNARY_FN(FnSin, sin(a))
 NEBO_UNARY_FN(FnCos, cos(a))
 NEBO_UNARY_FN(FnTan, tan(a))
-NEBO_UNARY_FN(FnExp, exp(a))
+// exp and sin of doubles: the fixed-point forms of NeboFixMath.h (within 0.52 and 1.1 ulp, off
+// the FP64 pipe); NEBO_CUDA_LIBM selects CUDA's functions instead.
+struct FnExp {
+  template <class T> static __device__ __forceinline__ T apply(T a) { return exp(a); }
+#ifndef NEBO_CUDA_LIBM
+  static __device__ __forceinline__ double apply(double a) { return nebo::fixmath::exp_i(a); }
+#endif
+};
+struct FnSin {
+  template <class T> static __device__ __forceinline__ T apply(T a) { return sin(a); }
+#ifndef NEBO_CUDA_LIBM
+  static __device__ __forceinline__ double apply(double a) { return nebo::fixmath::sin_i(a); }
+#endif
+};
 NEBO_UNARY_FN(FnTanh, tanh(a))
 NEBO_UNARY_FN(FnAbs, fabs(a))
 NEBO_UNARY_FN(FnSqrt, sqrt(a))
@@ -133,10 +146,35 @@ struct LogAnd { static __device__ __forceinline__ bool apply(bool a, bool b) { r
 struct LogOr { static __device__ __forceinline__ bool apply(bool a, bool b) { return a || b; } };
 
 // ============================================================================ device functors
+// Every device functor evaluates at interior-relative (x,y,z) (eval for values, check for
+// booleans) and has two hooks for the tiled lowering (NeboTiled.h):
+//   rebase(x0,y0,z0)   moves its leaves' origin to (x0,y0,z0), so that later coordinates are
+//                      relative to a tile;
+//   fill<H>(tx,ty,tz)  fills the shared-memory buffers of round H below it (tx,ty,tz: how much
+//                      a partial tile is short of the full tile on each axis).
+#define NEBO_ONE_CHILD(A)                                                                       \
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) { A.rebase(x0, y0, z0); }      \
+  template <int Round_>                                                                         \
+  __device__ __forceinline__ void fill(int tx, int ty, int tz) const {                          \
+    A.template fill<Round_>(tx, ty, tz);                                                        \
+  }
+#define NEBO_TWO_CHILDREN(A, B)                                                                 \
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) {                              \
+    A.rebase(x0, y0, z0);                                                                       \
+    B.rebase(x0, y0, z0);                                                                       \
+  }                                                                                             \
+  template <int Round_>                                                                         \
+  __device__ __forceinline__ void fill(int tx, int ty, int tz) const {                          \
+    A.template fill<Round_>(tx, ty, tz);                                                        \
+    B.template fill<Round_>(tx, ty, tz);                                                        \
+  }
+
 template <typename T>
 struct DScalar {
   T v;
   __device__ __forceinline__ T eval(int, int, int) const { return v; }
+  __device__ __forceinline__ void rebase(int, int, int) {}
+  template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
 };
 
 template <typename T>
@@ -145,6 +183,8 @@ struct DField {
   int sy;
   long sz;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return __ldg(p + ((long)x + (long)sy * y + sz * z)); }
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) { p += (long)x0 + (long)sy * y0 + sz * z0; }
+  template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
 };
 
 struct DMask {
@@ -156,6 +196,8 @@ struct DMask {
     const long f = origin + (long)x + (long)sy * y + sz * z;
     return (__ldg(w + (f >> 5)) >> (f & 31)) & 1u;
   }
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) { origin += (long)x0 + (long)sy * y0 + sz * z0; }
+  template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
 };
 
 template <class Op, typename T, class A, class B>
@@ -163,12 +205,14 @@ struct DBin {
   A a;
   B b;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return Op::apply(a.eval(x, y, z), b.eval(x, y, z)); }
+  NEBO_TWO_CHILDREN(a, b)
 };
 
 template <class Fn, typename T, class A>
 struct DUn {
   A a;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return Fn::apply(a.eval(x, y, z)); }
+  NEBO_ONE_CHILD(a)
 };
 
 template <typename T, class A>
@@ -176,6 +220,7 @@ struct DPowInt {
   A a;
   int e;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return pow(a.eval(x, y, z), (T)e); }
+  NEBO_ONE_CHILD(a)
 };
 
 template <class Op, class A, class B>
@@ -183,6 +228,7 @@ struct DCmp {
   A a;
   B b;
   __device__ __forceinline__ bool check(int x, int y, int z) const { return Op::apply(a.eval(x, y, z), b.eval(x, y, z)); }
+  NEBO_TWO_CHILDREN(a, b)
 };
 
 template <class Op, class A, class B>
@@ -190,12 +236,14 @@ struct DLogic {
   A a;
   B b;
   __device__ __forceinline__ bool check(int x, int y, int z) const { return Op::apply(a.check(x, y, z), b.check(x, y, z)); }
+  NEBO_TWO_CHILDREN(a, b)
 };
 
 template <class A>
 struct DNot {
   A a;
   __device__ __forceinline__ bool check(int x, int y, int z) const { return !a.check(x, y, z); }
+  NEBO_ONE_CHILD(a)
 };
 
 // cond: first true clause wins (NeboCond.h:408-413)
@@ -205,6 +253,16 @@ struct DCond {
   Val v;
   Rest r;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return t.check(x, y, z) ? v.eval(x, y, z) : r.eval(x, y, z); }
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) {
+    t.rebase(x0, y0, z0);
+    v.rebase(x0, y0, z0);
+    r.rebase(x0, y0, z0);
+  }
+  template <int H> __device__ __forceinline__ void fill(int tx, int ty, int tz) const {
+    t.template fill<H>(tx, ty, tz);
+    v.template fill<H>(tx, ty, tz);
+    r.template fill<H>(tx, ty, tz);
+  }
 };
 
 }  // namespace nebo_detail
@@ -370,12 +428,14 @@ struct DStencil {
   A a;
   double c[Pts::length];
   __device__ __forceinline__ T eval(int x, int y, int z) const { return StencilFold<Pts>::template weighted<T>(a, c, x, y, z); }
+  NEBO_ONE_CHILD(a)
 };
 
 template <typename T, class Pts, class A>
 struct DSumStencil {
   A a;
   __device__ __forceinline__ T eval(int x, int y, int z) const { return StencilFold<Pts>::template sum<T>(a, x, y, z); }
+  NEBO_ONE_CHILD(a)
 };
 
 // ============================================================================ stream order
@@ -466,6 +526,7 @@ template <class P>
 struct DMaskShift {
   DMask m;
   __device__ __forceinline__ bool check(int x, int y, int z) const { return m.check(x + P::X, y + P::Y, z + P::Z); }
+  NEBO_ONE_CHILD(m)
 };
 template <class P, class F>
 struct MaskShiftNode {

@@ -1,0 +1,369 @@
+// Tiled lowering of `<<=` (the evaluation that replaces spatialops/NeboLhs.h:29-41 and 592-699,
+// the reference's one-thread-per-column walks).
+//
+// The reference evaluates a nested stencil by recomputing its argument at every point of every
+// enclosing stencil: Interp(Grad(Interp(a))) reads `a` eight times per output and computes the
+// inner interpolant four times (spatialops/NeboStencils.h:407-448).  Here a block of 32 x 8
+// threads owns a tile of 32 x 8 x TZ output cells.  Before the output pass, the argument of every
+// stencil whose argument is itself an expression (not a field leaf or a scalar) is materialised
+// ONCE per tile in shared memory, over the tile grown by the reach of that stencil and of every
+// stencil above it; the stencil then reads its neighbours from shared memory.  Inner levels are
+// filled first (fill rounds 1..H, one barrier per round), so each level of a deep chain is
+// computed once per point.  Field leaves are read with coalesced read-only loads (a tile's
+// neighbours hit L1 and L2, so each input is read from HBM about once).
+//
+// Everything is decided at compile time from the expression's type: which nodes are
+// materialised, each buffer's box (per-axis reach of the point collections, summed through
+// nested stencils), its shared-memory offset, the fill round, and the tile depth TZ (8, 4, 2
+// or 1: the deepest whose buffers fit the budget).  An expression without such a stencil keeps
+// the plain one-pass kernel.
+//
+// Values: each materialised point is the same functor evaluated at the same point with the same
+// operations in the same order, and the stencil folds its points in the reference's order, so
+// the results are bit for bit those of the plain kernel (and, with NEBO_EXACT_ARITHMETIC, of the
+// reference's serial walk).
+//
+// Bounds: a buffer point is computed only when some output cell of the (possibly partial) tile
+// reads it; the write region (calculate_actual_ghost) guarantees that every such point's reads
+// lie inside the fields' valid windows, because the windows are boxes and each buffer covers the
+// box hull of the reads.
+#ifndef SpatialOps_NeboTiled_h
+#define SpatialOps_NeboTiled_h
+
+#include <cuda_runtime.h>
+
+#include <spatialops/NeboCore.h>
+
+#ifdef __CUDACC__
+#include <spatialops/NeboApplyPointwise.h>
+#endif
+
+namespace SpatialOps {
+namespace nebo_detail {
+
+constexpr int kTileX = 32;
+constexpr int kTileY = 8;
+constexpr int kTileThreads = kTileX * kTileY;
+#ifndef NEBO_TILE_SMEM_BUDGET
+#define NEBO_TILE_SMEM_BUDGET (64 * 1024)
+#endif
+constexpr int kTileSmemBudget = NEBO_TILE_SMEM_BUDGET;
+
+constexpr int cmin(int a, int b) { return a < b ? a : b; }
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+// A box of local (tile-relative) coordinates, bounds inclusive.
+template <int XL, int XH, int YL, int YH, int ZL, int ZH>
+struct TBox {
+  enum { xl = XL, xh = XH, yl = YL, yh = YH, zl = ZL, zh = ZH };
+  enum { nx = XH - XL + 1, ny = YH - YL + 1, nz = ZH - ZL + 1 };
+  enum { n = nx * ny * nz };
+};
+
+// Per-axis hull of a point collection.
+template <class Pts>
+struct PtsHull;
+template <class P>
+struct PtsHull<NeboStencilPointCollection<P, NeboNil>> {
+  enum { xl = P::X, xh = P::X, yl = P::Y, yh = P::Y, zl = P::Z, zh = P::Z };
+};
+template <class P, class R>
+struct PtsHull<NeboStencilPointCollection<P, R>> {
+  typedef PtsHull<R> H;
+  enum {
+    xl = cmin(P::X, H::xl), xh = cmax(P::X, H::xh),
+    yl = cmin(P::Y, H::yl), yh = cmax(P::Y, H::yh),
+    zl = cmin(P::Z, H::zl), zh = cmax(P::Z, H::zh)
+  };
+};
+
+// The box an argument is needed on: the stencil's box grown by its points.
+template <class B, class Pts>
+struct GrowBox {
+  typedef PtsHull<Pts> H;
+  typedef TBox<B::xl + H::xl, B::xh + H::xh, B::yl + H::yl, B::yh + H::yh, B::zl + H::zl, B::zh + H::zh> type;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned char* tile_smem() {
+  extern __shared__ __align__(16) unsigned char nebo_tile_dyn_smem[];
+  return nebo_tile_dyn_smem;
+}
+#endif
+
+// Read access to a buffer over box R at byte offset Off.
+template <typename T, class R, int Off>
+struct SmemView {
+#ifdef __CUDACC__
+  __device__ __forceinline__ T eval(int x, int y, int z) const {
+    const T* buf = reinterpret_cast<const T*>(tile_smem() + Off);
+    return buf[(x - R::xl) + R::nx * ((y - R::yl) + R::ny * (z - R::zl))];
+  }
+#endif
+};
+
+// A stencil whose argument is materialised over box R at byte offset Off in fill round Round.
+template <typename T, class Pts, class A, class R, int Off, int Round, bool Sum>
+struct DStencilSmem {
+  A a;
+  double c[Pts::length];
+#ifdef __CUDACC__
+  __device__ __forceinline__ T eval(int x, int y, int z) const {
+    return Sum ? StencilFold<Pts>::template sum<T>(SmemView<T, R, Off>(), x, y, z)
+               : StencilFold<Pts>::template weighted<T>(SmemView<T, R, Off>(), c, x, y, z);
+  }
+  __device__ __forceinline__ void rebase(int x0, int y0, int z0) { a.rebase(x0, y0, z0); }
+  template <int H>
+  __device__ __forceinline__ void fill(int tx, int ty, int tz) const {
+    a.template fill<H>(tx, ty, tz);
+    if (H != Round) return;
+    T* buf = reinterpret_cast<T*>(tile_smem() + Off);
+    // points read by the tile's output cells: the box, its upper ends cut by the partial tile
+    const int hx = R::xh - tx, hy = R::yh - ty, hz = R::zh - tz;
+    const int tid = (int)(threadIdx.x + blockDim.x * threadIdx.y);
+#pragma unroll 2
+    for (int i = tid; i < R::n; i += kTileThreads) {
+      const int lx = R::xl + i % R::nx;
+      const int r = i / R::nx;
+      const int ly = R::yl + r % R::ny;
+      const int lz = R::zl + r / R::ny;
+      if (lx <= hx && ly <= hy && lz <= hz) buf[i] = a.eval(lx, ly, lz);
+    }
+  }
+#endif
+};
+
+// ---------------------------------------------------------------------------- the transform
+// Tile<D, R, Off>: D evaluated over box R with its buffers from byte offset Off.
+//   type   the functor with every materialised stencil replaced by DStencilSmem
+//   end    byte offset after the subtree's buffers
+//   rounds fill rounds the subtree needs (0: no buffer)
+//   make   copies the run-time values (pointers, strides, coefficients, scalars)
+template <class D>
+struct IsLeaf : std::false_type {};
+template <typename T>
+struct IsLeaf<DField<T>> : std::true_type {};
+template <typename T>
+struct IsLeaf<DScalar<T>> : std::true_type {};
+
+template <class D, class R, int Off, class Enable = void>
+struct Tile {  // leaves, masks and anything without children that matter
+  typedef D type;
+  enum { end = Off, rounds = 0 };
+  static type make(const D& d) { return d; }
+};
+
+template <class Op, typename T, class A, class B, class R, int Off>
+struct Tile<DBin<Op, T, A, B>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef Tile<B, R, TA::end> TB;
+  typedef DBin<Op, T, typename TA::type, typename TB::type> type;
+  enum { end = TB::end, rounds = cmax(TA::rounds, TB::rounds) };
+  static type make(const DBin<Op, T, A, B>& d) { return type{TA::make(d.a), TB::make(d.b)}; }
+};
+
+template <class Fn, typename T, class A, class R, int Off>
+struct Tile<DUn<Fn, T, A>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef DUn<Fn, T, typename TA::type> type;
+  enum { end = TA::end, rounds = TA::rounds };
+  static type make(const DUn<Fn, T, A>& d) { return type{TA::make(d.a)}; }
+};
+
+template <typename T, class A, class R, int Off>
+struct Tile<DPowInt<T, A>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef DPowInt<T, typename TA::type> type;
+  enum { end = TA::end, rounds = TA::rounds };
+  static type make(const DPowInt<T, A>& d) { return type{TA::make(d.a), d.e}; }
+};
+
+template <class Op, class A, class B, class R, int Off>
+struct Tile<DCmp<Op, A, B>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef Tile<B, R, TA::end> TB;
+  typedef DCmp<Op, typename TA::type, typename TB::type> type;
+  enum { end = TB::end, rounds = cmax(TA::rounds, TB::rounds) };
+  static type make(const DCmp<Op, A, B>& d) { return type{TA::make(d.a), TB::make(d.b)}; }
+};
+
+template <class Op, class A, class B, class R, int Off>
+struct Tile<DLogic<Op, A, B>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef Tile<B, R, TA::end> TB;
+  typedef DLogic<Op, typename TA::type, typename TB::type> type;
+  enum { end = TB::end, rounds = cmax(TA::rounds, TB::rounds) };
+  static type make(const DLogic<Op, A, B>& d) { return type{TA::make(d.a), TB::make(d.b)}; }
+};
+
+template <class A, class R, int Off>
+struct Tile<DNot<A>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef DNot<typename TA::type> type;
+  enum { end = TA::end, rounds = TA::rounds };
+  static type make(const DNot<A>& d) { return type{TA::make(d.a)}; }
+};
+
+template <typename T, class Test, class Val, class Rest, class R, int Off>
+struct Tile<DCond<T, Test, Val, Rest>, R, Off> {
+  typedef Tile<Test, R, Off> TT;
+  typedef Tile<Val, R, TT::end> TV;
+  typedef Tile<Rest, R, TV::end> TR;
+  typedef DCond<T, typename TT::type, typename TV::type, typename TR::type> type;
+  enum { end = TR::end, rounds = cmax(TT::rounds, cmax(TV::rounds, TR::rounds)) };
+  static type make(const DCond<T, Test, Val, Rest>& d) { return type{TT::make(d.t), TV::make(d.v), TR::make(d.r)}; }
+};
+
+// a stencil of a leaf: reads its neighbours directly
+template <typename T, class Pts, class A, class R, int Off>
+struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<IsLeaf<A>::value>::type> {
+  typedef DStencil<T, Pts, A> type;
+  enum { end = Off, rounds = 0 };
+  static type make(const type& d) { return d; }
+};
+template <typename T, class Pts, class A, class R, int Off>
+struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<IsLeaf<A>::value>::type> {
+  typedef DSumStencil<T, Pts, A> type;
+  enum { end = Off, rounds = 0 };
+  static type make(const type& d) { return d; }
+};
+
+constexpr int round16(int b) { return (b + 15) / 16 * 16; }
+
+// a stencil of an expression: the argument is materialised over the grown box
+template <typename T, class Pts, class A, class R, int Off, bool Sum>
+struct TileSmemStencil {
+  typedef typename GrowBox<R, Pts>::type RA;
+  typedef Tile<A, RA, Off> TA;
+  enum { my_off = TA::end, end = TA::end + round16(RA::n * (int)sizeof(T)), rounds = TA::rounds + 1 };
+  typedef DStencilSmem<T, Pts, typename TA::type, RA, my_off, rounds, Sum> type;
+};
+template <typename T, class Pts, class A, class R, int Off>
+struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::value>::type>
+    : TileSmemStencil<T, Pts, A, R, Off, false> {
+  typedef TileSmemStencil<T, Pts, A, R, Off, false> B;
+  static typename B::type make(const DStencil<T, Pts, A>& d) {
+    typename B::type t;
+    t.a = B::TA::make(d.a);
+    for (int i = 0; i < Pts::length; ++i) t.c[i] = d.c[i];
+    return t;
+  }
+};
+template <typename T, class Pts, class A, class R, int Off>
+struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::value>::type>
+    : TileSmemStencil<T, Pts, A, R, Off, true> {
+  typedef TileSmemStencil<T, Pts, A, R, Off, true> B;
+  static typename B::type make(const DSumStencil<T, Pts, A>& d) {
+    typename B::type t;
+    t.a = B::TA::make(d.a);
+    for (int i = 0; i < Pts::length; ++i) t.c[i] = 0.0;
+    return t;
+  }
+};
+
+#ifdef __CUDACC__
+// apply_pointwise operands
+template <class Tup, class R, int Off>
+struct TileTuple;
+template <class R, int Off>
+struct TileTuple<DTuple<>, R, Off> {
+  typedef DTuple<> type;
+  enum { end = Off, rounds = 0 };
+  static type make(const DTuple<>&) { return type(); }
+};
+template <class H, class... Rest, class R, int Off>
+struct TileTuple<DTuple<H, Rest...>, R, Off> {
+  typedef Tile<H, R, Off> TH;
+  typedef TileTuple<DTuple<Rest...>, R, TH::end> TR;
+  typedef DTuple<typename TH::type, typename TR::type> Dummy;
+  enum { end = TR::end, rounds = cmax(TH::rounds, TR::rounds) };
+  template <class TRT>
+  struct Cons;
+  template <class... X>
+  struct Cons<DTuple<X...>> {
+    typedef DTuple<typename TH::type, X...> type;
+  };
+  typedef typename Cons<typename TR::type>::type type;
+  static type make(const DTuple<H, Rest...>& t) {
+    type o;
+    o.h = TH::make(t.h);
+    o.r = TR::make(t.r);
+    return o;
+  }
+};
+template <typename T, class Fn, class... D, class R, int Off>
+struct Tile<DApply<T, Fn, D...>, R, Off> {
+  typedef TileTuple<DTuple<D...>, R, Off> TT;
+  template <class TupT>
+  struct Of;
+  template <class... X>
+  struct Of<DTuple<X...>> {
+    typedef DApply<T, Fn, X...> type;
+  };
+  typedef typename Of<typename TT::type>::type type;
+  enum { end = TT::end, rounds = TT::rounds };
+  static type make(const DApply<T, Fn, D...>& d) {
+    type o;
+    o.ops = TT::make(d.ops);
+    return o;
+  }
+};
+#endif
+
+// The plan for a functor: the tile depth TZ whose buffers fit the budget, or 0 when no stencil
+// needs a buffer (or none fits): the plain kernel then runs.
+template <class D, int TZ>
+struct TileAt {
+  typedef Tile<D, TBox<0, kTileX - 1, 0, kTileY - 1, 0, TZ - 1>, 0> type;
+};
+template <class D>
+struct TilePlan {
+  enum {
+    rounds = TileAt<D, 8>::type::rounds,
+    tz = rounds == 0 ? 0
+         : (int)TileAt<D, 8>::type::end <= kTileSmemBudget ? 8
+         : (int)TileAt<D, 4>::type::end <= kTileSmemBudget ? 4
+         : (int)TileAt<D, 2>::type::end <= kTileSmemBudget ? 2
+         : (int)TileAt<D, 1>::type::end <= kTileSmemBudget ? 1 : 0
+  };
+};
+
+#ifdef __CUDACC__
+template <int H>
+struct FillRounds {
+  template <class F>
+  static __device__ __forceinline__ void run(const F& f, int tx, int ty, int tz) {
+    FillRounds<H - 1>::run(f, tx, ty, tz);
+    f.template fill<H>(tx, ty, tz);
+    __syncthreads();
+  }
+};
+template <>
+struct FillRounds<0> {
+  template <class F>
+  static __device__ __forceinline__ void run(const F&, int, int, int) {}
+};
+
+// One block per 32 x 8 x TZ tile of the write region (interior-relative limits).
+template <typename T, class DT, int TZ, int ROUNDS>
+__global__ void __launch_bounds__(kTileThreads) nebo_tiled_assign_kernel(T* __restrict__ out, int sy, long sz, int xlo,
+                                                                        int xhi, int ylo, int yhi, int zlo, int zhi,
+                                                                        DT rhs) {
+  const int x0 = xlo + (int)blockIdx.x * kTileX;
+  const int y0 = ylo + (int)blockIdx.y * kTileY;
+  const int z0 = zlo + (int)blockIdx.z * TZ;
+  const int nx = cmin(kTileX, xhi - x0), ny = cmin(kTileY, yhi - y0), nz = cmin(TZ, zhi - z0);
+  DT f = rhs;
+  f.rebase(x0, y0, z0);
+  FillRounds<ROUNDS>::run(f, kTileX - nx, kTileY - ny, TZ - nz);
+  const int lx = (int)threadIdx.x, ly = (int)threadIdx.y;
+  if (lx >= nx || ly >= ny) return;
+  T* o = out + ((long)x0 + lx) + (long)sy * (y0 + ly) + sz * z0;
+#pragma unroll 1
+  for (int lz = 0; lz < nz; ++lz) o[sz * lz] = f.eval(lx, ly, lz);
+}
+#endif
+
+}  // namespace nebo_detail
+}  // namespace SpatialOps
+#endif

@@ -66,6 +66,12 @@ PROGRAMS = {
     "catalog_gpu_fast": ("catalog_gpu.cu", []),
     # particle <-> cell scenes (tests/cpp/particles_scene.h) on the drop-in headers
     "particles_gpu": ("particles_gpu.cu", []),
+    # `<<=` timing against the hand-fused kernels: the default lowering, the reference GPU
+    # kernel's design (one thread per column, CUDA's exp/sin), and the tiled lowering with CUDA's
+    # exp/sin
+    "assign_timing": ("assign_timing.cu", []),
+    "assign_timing_untiled": ("assign_timing.cu", ["-DNEBO_UNTILED", "-DNEBO_CUDA_LIBM"]),
+    "assign_timing_libm": ("assign_timing.cu", ["-DNEBO_CUDA_LIBM"]),
 }
 
 

@@ -370,7 +370,6 @@ int deep_impl(const nebo_field* a, const nebo_field* b, const nebo_field* c, con
   if (rc) return rc;
   if (!mask_words) return fail(NEBO_ERR_INVALID, "Nebo error in %s: null mask", what);
   if (reduce && !d_out4) return fail(NEBO_ERR_INVALID, "Nebo error in %s: null result pointer", what);
-  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in %s: math tables upload", what);
   int n[3];
   interior_extent(*a, n);
   const View<const double> va = make_view<const double>(*a), vb = make_view<const double>(*b),
@@ -510,7 +509,6 @@ __global__ void fastmath_kernel(int fn, const double* __restrict__ x, double* __
 
 extern "C" int nebo_fastmath_eval(int fn, const double* x, double* y, size_t n, nebo_stream_t stream) {
   if (fn < 0 || fn > 3 || (n && (!x || !y))) return fail(NEBO_ERR_INVALID, "Nebo error in nebo_fastmath_eval");
-  if (fixmath::tables_init()) return fail(NEBO_ERR_LAUNCH, "Nebo error in nebo_fastmath_eval: math tables upload");
   if (!n) return NEBO_OK;
   cudaStream_t s = (cudaStream_t)stream;
   LaunchScope ls("fastmath_eval", s);

@@ -2,8 +2,9 @@
 cases (the chain's z split, the filter's one-wave flat runs, the transport pair kernel's tiles,
 the patch work list).  Each test states the error it measures; tolerances are in the asserts.
 
-* deep chain 256^3: out / filt within 1e-13 relative max-norm of the oracle, max/min exact,
-  sum/norm within 1e-13 * sum|x|; the written-cell set of `out` (pre-filled with a NaN payload)
+* deep chain 256^3: out / filt within 1e-13 relative max-norm of the oracle; the fused max/min
+  exactly those of the written filt and within 1e-13 of the oracle's; sum/norm within
+  1e-13 * sum|x|; the written-cell set of `out` (pre-filled with a NaN payload)
   is exactly the reference's write region (calculate_actual_ghost, restated by the oracle);
 * FP32 transport 512^3 + 2 ghosts, 50 RK2 steps: relative max-norm error against the FP64 GPU
   transport (which equals the oracle to 1e-13 on the small cases), and conservation of sum(phi);
@@ -84,7 +85,12 @@ def test_deep_chain_256_vs_oracle_with_written_cells():
     assert err_out <= 1e-13 and err_filt <= 1e-13
     r = red.cpu().numpy()
     mag = float(np.abs(o_filt).sum())
-    assert r[1] == O.reduce_field(o_filt, 1, "max") and r[2] == O.reduce_field(o_filt, 1, "min")
+    # max/min: exactly those of the field the filter wrote (ghosts included), and within the
+    # field's tolerance of the oracle's (the filter rounds 4 times where the reference rounds 27)
+    assert r[1] == f.max() and r[2] == f.min()
+    for k, op in ((1, "max"), (2, "min")):
+        ref = O.reduce_field(o_filt, 1, op)
+        assert abs(r[k] - ref) <= 1e-13 * float(np.abs(o_filt).max()), (op, r[k], ref)
     assert abs(r[0] - O.reduce_field(o_filt, 1, "sum")) <= 1e-13 * mag
     assert abs(r[3] - O.reduce_field(o_filt, 1, "norm")) <= 1e-13 * O.reduce_field(o_filt, 1, "norm")
 
