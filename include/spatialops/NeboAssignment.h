@@ -183,6 +183,19 @@ const SpatialField<L, T>& operator<<=(SpatialField<L, T>& lhs, const NeboExpress
   return lhs;
 }
 
+// SingleValue right-hand sides: the value broadcast over the write region
+// (spatialops/NeboAssignment.h:61-133)
+template <typename L, typename T, class = typename std::enable_if<!std::is_same<L, SingleValue>::value>::type>
+const SpatialField<L, T>& operator<<=(SpatialField<L, T>& lhs, const SpatialField<SingleValue, T>& rhs) {
+  nebo_detail::assign(lhs, nebo_detail::SingleValueNode<SpatialField<SingleValue, T>>(rhs), true);
+  return lhs;
+}
+template <typename E, typename L, typename T>
+const SpatialField<L, T>& operator<<=(SpatialField<L, T>& lhs, const NeboSingleValueExpression<E, T>& rhs) {
+  nebo_detail::assign(lhs, rhs.expr(), true);
+  return lhs;
+}
+
 // ------------------------------------------------------------------ interior_assign
 template <typename L, typename T>
 const SpatialField<L, T>& interior_assign(SpatialField<L, T>& lhs, const typename std::common_type<T>::type& rhs) {
@@ -196,6 +209,17 @@ const SpatialField<L, T>& interior_assign(SpatialField<L, T>& lhs, const Spatial
 }
 template <typename E, typename L, typename T>
 const SpatialField<L, T>& interior_assign(SpatialField<L, T>& lhs, const NeboExpression<E, SpatialField<L, T>>& rhs) {
+  nebo_detail::assign(lhs, rhs.expr(), false);
+  return lhs;
+}
+
+template <typename L, typename T, class = typename std::enable_if<!std::is_same<L, SingleValue>::value>::type>
+const SpatialField<L, T>& interior_assign(SpatialField<L, T>& lhs, const SpatialField<SingleValue, T>& rhs) {
+  nebo_detail::assign(lhs, nebo_detail::SingleValueNode<SpatialField<SingleValue, T>>(rhs), false);
+  return lhs;
+}
+template <typename E, typename L, typename T>
+const SpatialField<L, T>& interior_assign(SpatialField<L, T>& lhs, const NeboSingleValueExpression<E, T>& rhs) {
   nebo_detail::assign(lhs, rhs.expr(), false);
   return lhs;
 }

@@ -61,6 +61,31 @@ struct NeboBooleanExpression {
   Operand expr_;
 };
 
+// Expressions whose value is one number held on the device (SingleValue fields combined with
+// each other and with scalars; spatialops/NeboBasic.h:211-275).  Where they meet a field they
+// broadcast, like a scalar.
+template <typename Operand, typename T>
+struct NeboSingleValueExpression {
+  typedef SpatialField<SingleValue, T> field_type;
+  typedef Operand Expression;
+  explicit NeboSingleValueExpression(const Operand& e) : expr_(e) {}
+  const Operand& expr() const { return expr_; }
+
+ private:
+  Operand expr_;
+};
+
+template <typename Operand, typename T>
+struct NeboBooleanSingleValueExpression {
+  typedef SpatialField<SingleValue, T> field_type;
+  typedef Operand Expression;
+  explicit NeboBooleanSingleValueExpression(const Operand& e) : expr_(e) {}
+  const Operand& expr() const { return expr_; }
+
+ private:
+  Operand expr_;
+};
+
 struct NeboNil {
   enum { length = 0 };
 };
@@ -173,6 +198,23 @@ template <typename T>
 struct DScalar {
   T v;
   __device__ __forceinline__ T eval(int, int, int) const { return v; }
+  __device__ __forceinline__ void rebase(int, int, int) {}
+  template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
+};
+
+// a SingleValue field: the one value, wherever it is read (NeboRhs.h:330-482)
+template <typename T>
+struct DSingleValue {
+  const T* p;
+  __device__ __forceinline__ T eval(int, int, int) const { return __ldg(p); }
+  __device__ __forceinline__ void rebase(int, int, int) {}
+  template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
+};
+
+// a boolean scalar (a cond clause tested with true or false)
+struct DBoolScalar {
+  bool b;
+  __device__ __forceinline__ bool check(int, int, int) const { return b; }
   __device__ __forceinline__ void rebase(int, int, int) {}
   template <int H> __device__ __forceinline__ void fill(int, int, int) const {}
 };
@@ -482,6 +524,38 @@ struct ScalarNode {
   IntVec has_bc() const { return IntVec(0, 0, 0); }
   void prepare() const {}
   DScalar<T> device() const { return DScalar<T>{v}; }
+};
+
+// A SingleValue field leaf: no ghost limit (like a scalar), its value read on the device.
+template <typename F>
+struct SingleValueNode {
+  typedef typename F::value_type value_type;
+  F f;
+  explicit SingleValueNode(const F& f_) : f(f_) {}
+  GhostData ghosts_with_bc() const { return GhostData(GHOST_MAX); }
+  GhostData ghosts_without_bc() const { return GhostData(GHOST_MAX); }
+  bool has_extents() const { return false; }
+  IntVec extents() const { return IntVec(0, 0, 0); }
+  IntVec has_bc() const { return IntVec(0, 0, 0); }
+  void prepare() const { f.device_values_for_read(); }
+  DSingleValue<value_type> device() const {
+    const value_type* base = f.device_values_for_read();
+    order_read(f.get_stream());
+    return DSingleValue<value_type>{base + f.interior_origin()};
+  }
+};
+
+struct BoolScalarNode {
+  typedef bool value_type;
+  bool b;
+  explicit BoolScalarNode(bool b_) : b(b_) {}
+  GhostData ghosts_with_bc() const { return GhostData(GHOST_MAX); }
+  GhostData ghosts_without_bc() const { return GhostData(GHOST_MAX); }
+  bool has_extents() const { return false; }
+  IntVec extents() const { return IntVec(0, 0, 0); }
+  IntVec has_bc() const { return IntVec(0, 0, 0); }
+  void prepare() const {}
+  DBoolScalar device() const { return DBoolScalar{b}; }
 };
 
 template <typename F>

@@ -43,10 +43,38 @@ struct Operand<NeboExpression<E, F>, void> {
   typedef F field_type;
   template <class T> static E node(const NeboExpression<E, F>& e) { return e.expr(); }
 };
+// SingleValue fields and expressions: field type SpatialField<SingleValue, V>, which gives way
+// to any other field type they meet (MergeField)
+template <class V>
+struct Operand<SpatialField<SingleValue, V>, void> {
+  static constexpr bool ok = true;
+  static constexpr bool scalar = false;
+  typedef SpatialField<SingleValue, V> field_type;
+  template <class T> static SingleValueNode<field_type> node(const field_type& f) { return SingleValueNode<field_type>(f); }
+};
+template <class E, class V>
+struct Operand<NeboSingleValueExpression<E, V>, void> {
+  static constexpr bool ok = true;
+  static constexpr bool scalar = false;
+  typedef SpatialField<SingleValue, V> field_type;
+  template <class T> static E node(const NeboSingleValueExpression<E, V>& e) { return e.expr(); }
+};
 
 template <class X>
 struct BoolOperand {
   static constexpr bool ok = false;
+};
+template <>
+struct BoolOperand<bool> {
+  static constexpr bool ok = true;
+  typedef void field_type;
+  static BoolScalarNode node(bool b) { return BoolScalarNode(b); }
+};
+template <class E, class V>
+struct BoolOperand<NeboBooleanSingleValueExpression<E, V>> {
+  static constexpr bool ok = true;
+  typedef SpatialField<SingleValue, V> field_type;
+  static E node(const NeboBooleanSingleValueExpression<E, V>& e) { return e.expr(); }
 };
 template <class E, class F>
 struct BoolOperand<NeboBooleanExpression<E, F>> {
@@ -61,15 +89,52 @@ struct BoolOperand<SpatialMask<F>> {
   static MaskNode<F> node(const SpatialMask<F>& m) { return MaskNode<F>(m); }
 };
 
-// field type of a combination (void for two scalars)
-template <class FA, class FB>
+// field type of a combination (void for two scalars; a SingleValue field gives way to any other
+// field type, as the reference's Field x SingleValue overloads do)
+template <class F>
+struct IsSingleValue : std::false_type {};
+template <class V>
+struct IsSingleValue<SpatialField<SingleValue, V>> : std::true_type {};
+
+template <class FA, class FB,
+          int K = (std::is_void<FA>::value || std::is_void<FB>::value) ? 0
+                  : (IsSingleValue<FA>::value && !IsSingleValue<FB>::value) ? 1
+                  : (IsSingleValue<FB>::value && !IsSingleValue<FA>::value) ? 2 : 0>
 struct MergeField {
   static_assert(std::is_same<FA, FB>::value, "Nebo: operands of one expression must have the same field type");
   typedef FA type;
 };
-template <class FB> struct MergeField<void, FB> { typedef FB type; };
-template <class FA> struct MergeField<FA, void> { typedef FA type; };
-template <> struct MergeField<void, void> { typedef void type; };
+template <class FA, class FB> struct MergeField<FA, FB, 1> {
+  static_assert(std::is_same<typename FA::value_type, typename FB::value_type>::value,
+                "Nebo: a SingleValue field must have the value type of the field it meets");
+  typedef FB type;
+};
+template <class FA, class FB> struct MergeField<FA, FB, 2> {
+  static_assert(std::is_same<typename FA::value_type, typename FB::value_type>::value,
+                "Nebo: a SingleValue field must have the value type of the field it meets");
+  typedef FA type;
+};
+template <class FB> struct MergeField<void, FB, 0> { typedef FB type; };
+template <class FA> struct MergeField<FA, void, 0> { typedef FA type; };
+template <> struct MergeField<void, void, 0> { typedef void type; };
+
+// the wrapper of a value / boolean expression of field type F
+template <class N, class F>
+struct Wrap {
+  typedef NeboExpression<N, F> type;
+};
+template <class N, class V>
+struct Wrap<N, SpatialField<SingleValue, V>> {
+  typedef NeboSingleValueExpression<N, V> type;
+};
+template <class N, class F>
+struct WrapBool {
+  typedef NeboBooleanExpression<N, F> type;
+};
+template <class N, class V>
+struct WrapBool<N, SpatialField<SingleValue, V>> {
+  typedef NeboBooleanSingleValueExpression<N, V> type;
+};
 
 template <class A, class B>
 struct BinaryTraits {
@@ -111,10 +176,11 @@ struct BoolBinary<A, B, true> {
 // ------------------------------------------------------------------ arithmetic
 #define NEBO_BINARY_OPERATOR(SYM, OP)                                                                          \
   template <class A, class B, class Bn = nebo_detail::Binary<A, B>>                                            \
-  NeboExpression<nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>, typename Bn::field_type> \
+  typename nebo_detail::Wrap<nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>,          \
+                             typename Bn::field_type>::type                                                    \
   operator SYM(const A& a, const B& b) {                                                                       \
     typedef nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB> N;                         \
-    return NeboExpression<N, typename Bn::field_type>(N(Bn::na(a), Bn::nb(b)));                                \
+    return typename nebo_detail::Wrap<N, typename Bn::field_type>::type(N(Bn::na(a), Bn::nb(b)));              \
   }
 NEBO_BINARY_OPERATOR(+, OpAdd)
 NEBO_BINARY_OPERATOR(-, OpSub)
@@ -124,10 +190,11 @@ NEBO_BINARY_OPERATOR(/, OpDiv)
 
 #define NEBO_BINARY_FUNCTION(NAME, OP)                                                                         \
   template <class A, class B, class Bn = nebo_detail::Binary<A, B>>                                            \
-  NeboExpression<nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>, typename Bn::field_type> \
+  typename nebo_detail::Wrap<nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>,          \
+                             typename Bn::field_type>::type                                                    \
   NAME(const A& a, const B& b) {                                                                               \
     typedef nebo_detail::BinNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB> N;                         \
-    return NeboExpression<N, typename Bn::field_type>(N(Bn::na(a), Bn::nb(b)));                                \
+    return typename nebo_detail::Wrap<N, typename Bn::field_type>::type(N(Bn::na(a), Bn::nb(b)));              \
   }
 NEBO_BINARY_FUNCTION(max, OpMax)
 NEBO_BINARY_FUNCTION(min, OpMin)
@@ -136,22 +203,25 @@ NEBO_BINARY_FUNCTION(min, OpMin)
 // pow(x, y): an int exponent selects PowIntFcn (NeboOperators.h:14598), anything else PowFcn.
 template <class A, class B, class Bn = nebo_detail::Binary<A, B>,
           class = typename std::enable_if<!std::is_integral<B>::value>::type>
-NeboExpression<nebo_detail::BinNode<nebo_detail::OpPow, typename Bn::NA, typename Bn::NB>, typename Bn::field_type> pow(
-    const A& a, const B& b) {
+typename nebo_detail::Wrap<nebo_detail::BinNode<nebo_detail::OpPow, typename Bn::NA, typename Bn::NB>,
+                           typename Bn::field_type>::type
+pow(const A& a, const B& b) {
   typedef nebo_detail::BinNode<nebo_detail::OpPow, typename Bn::NA, typename Bn::NB> N;
-  return NeboExpression<N, typename Bn::field_type>(N(Bn::na(a), Bn::nb(b)));
+  return typename nebo_detail::Wrap<N, typename Bn::field_type>::type(N(Bn::na(a), Bn::nb(b)));
 }
 template <class A, class U = nebo_detail::Unary<A>>
-NeboExpression<nebo_detail::PowIntNode<typename U::NA>, typename U::field_type> pow(const A& a, int e) {
+typename nebo_detail::Wrap<nebo_detail::PowIntNode<typename U::NA>, typename U::field_type>::type pow(const A& a,
+                                                                                                     int e) {
   typedef nebo_detail::PowIntNode<typename U::NA> N;
-  return NeboExpression<N, typename U::field_type>(N(U::na(a), e));
+  return typename nebo_detail::Wrap<N, typename U::field_type>::type(N(U::na(a), e));
 }
 
 #define NEBO_UNARY_FUNCTION(NAME, FN)                                                                          \
   template <class A, class U = nebo_detail::Unary<A>>                                                          \
-  NeboExpression<nebo_detail::UnNode<nebo_detail::FN, typename U::NA>, typename U::field_type> NAME(const A& a) { \
+  typename nebo_detail::Wrap<nebo_detail::UnNode<nebo_detail::FN, typename U::NA>, typename U::field_type>::type \
+  NAME(const A& a) {                                                                                           \
     typedef nebo_detail::UnNode<nebo_detail::FN, typename U::NA> N;                                            \
-    return NeboExpression<N, typename U::field_type>(N(U::na(a)));                                             \
+    return typename nebo_detail::Wrap<N, typename U::field_type>::type(N(U::na(a)));                           \
   }
 NEBO_UNARY_FUNCTION(operator-, FnNeg)
 NEBO_UNARY_FUNCTION(sin, FnSin)
@@ -174,10 +244,11 @@ NEBO_UNARY_FUNCTION(cube, FnCube)
 // ------------------------------------------------------------------ comparisons -> booleans
 #define NEBO_COMPARISON(SYM, OP)                                                                                \
   template <class A, class B, class Bn = nebo_detail::Binary<A, B>>                                             \
-  NeboBooleanExpression<nebo_detail::CmpNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>, typename Bn::field_type> \
+  typename nebo_detail::WrapBool<nebo_detail::CmpNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB>,       \
+                                 typename Bn::field_type>::type                                                 \
   operator SYM(const A& a, const B& b) {                                                                        \
     typedef nebo_detail::CmpNode<nebo_detail::OP, typename Bn::NA, typename Bn::NB> N;                          \
-    return NeboBooleanExpression<N, typename Bn::field_type>(N(Bn::na(a), Bn::nb(b)));                          \
+    return typename nebo_detail::WrapBool<N, typename Bn::field_type>::type(N(Bn::na(a), Bn::nb(b)));           \
   }
 NEBO_COMPARISON(==, CmpEq)
 NEBO_COMPARISON(!=, CmpNe)
@@ -189,25 +260,32 @@ NEBO_COMPARISON(>=, CmpGe)
 
 #define NEBO_LOGIC(SYM, OP)                                                                                     \
   template <class A, class B, class Bb = nebo_detail::BoolBinary<A, B>>                                         \
-  NeboBooleanExpression<nebo_detail::LogicNode<nebo_detail::OP, typename Bb::NA, typename Bb::NB>, typename Bb::field_type> \
+  typename nebo_detail::WrapBool<nebo_detail::LogicNode<nebo_detail::OP, typename Bb::NA, typename Bb::NB>,     \
+                                 typename Bb::field_type>::type                                                 \
   operator SYM(const A& a, const B& b) {                                                                        \
     typedef nebo_detail::LogicNode<nebo_detail::OP, typename Bb::NA, typename Bb::NB> N;                        \
-    return NeboBooleanExpression<N, typename Bb::field_type>(                                                   \
+    return typename nebo_detail::WrapBool<N, typename Bb::field_type>::type(                                    \
         N(nebo_detail::BoolOperand<A>::node(a), nebo_detail::BoolOperand<B>::node(b)));                         \
   }
 NEBO_LOGIC(&&, LogAnd)
 NEBO_LOGIC(||, LogOr)
 #undef NEBO_LOGIC
 
-template <class A, class = typename std::enable_if<nebo_detail::BoolOperand<A>::ok>::type>
-NeboBooleanExpression<nebo_detail::NotNode<decltype(nebo_detail::BoolOperand<A>::node(std::declval<A>()))>,
-                      typename nebo_detail::BoolOperand<A>::field_type>
+template <class A, class = typename std::enable_if<nebo_detail::BoolOperand<A>::ok && !std::is_same<A, bool>::value>::type>
+typename nebo_detail::WrapBool<nebo_detail::NotNode<decltype(nebo_detail::BoolOperand<A>::node(std::declval<A>()))>,
+                               typename nebo_detail::BoolOperand<A>::field_type>::type
 operator!(const A& a) {
   typedef nebo_detail::NotNode<decltype(nebo_detail::BoolOperand<A>::node(std::declval<A>()))> N;
-  return NeboBooleanExpression<N, typename nebo_detail::BoolOperand<A>::field_type>(N(nebo_detail::BoolOperand<A>::node(a)));
+  return typename nebo_detail::WrapBool<N, typename nebo_detail::BoolOperand<A>::field_type>::type(
+      N(nebo_detail::BoolOperand<A>::node(a)));
 }
 
 // ------------------------------------------------------------------ cond(...)(...)...(default)
+// cond(test, value)(test, value)...(default): the first clause whose test holds gives the value
+// (NeboCond.h:408-413).  Tests are boolean expressions, masks or plain bools; values are scalars,
+// fields, SingleValue fields or expressions.  cond(value) alone is the value.  A cond made of
+// scalars and bools only is evaluated on the host and is a plain number (NeboCond.h's simple
+// conds: `double d = cond(false, 1.0)(2.0);`).
 namespace nebo_detail {
 struct ClauseEnd {};
 template <class Prev, class TN, class VN>
@@ -215,6 +293,15 @@ struct ClauseLink {
   Prev prev;
   TN t;
   VN v;
+};
+
+template <class F>
+struct ValueTypeOf {
+  typedef typename F::value_type type;
+};
+template <>
+struct ValueTypeOf<void> {
+  typedef double type;
 };
 
 template <typename T, class Tail>
@@ -226,14 +313,24 @@ auto fold_cond(const ClauseLink<Prev, TN, VN>& c, const Tail& tail) {
   return fold_cond<T>(c.prev, CondNode<T, TN, VN, Tail>(c.t, c.v, tail));
 }
 
+// all-scalar chains: evaluated here, first clause first
+template <typename T>
+T host_cond(const ClauseEnd&, T tail) {
+  return tail;
+}
+template <typename T, class Prev, class TN, class VN>
+T host_cond(const ClauseLink<Prev, TN, VN>& c, T tail) {
+  return host_cond<T>(c.prev, c.t.b ? (T)c.v.v : tail);
+}
+
 template <class F, class Chain>
 struct CondBuilder {
-  typedef typename F::value_type T;
+  typedef typename ValueTypeOf<F>::type T;
   Chain chain;
 
   template <class Tst, class V>
   auto operator()(const Tst& t, const V& v) const {
-    static_assert(BoolOperand<Tst>::ok, "Nebo cond: a clause test must be a boolean expression or a mask");
+    static_assert(BoolOperand<Tst>::ok, "Nebo cond: a clause test must be a boolean expression, a mask or a bool");
     typedef typename MergeField<typename MergeField<F, typename BoolOperand<Tst>::field_type>::type,
                                 typename Operand<V>::field_type>::type F2;
     auto tn = BoolOperand<Tst>::node(t);
@@ -244,23 +341,47 @@ struct CondBuilder {
   template <class V>
   auto operator()(const V& v) const {
     typedef typename MergeField<F, typename Operand<V>::field_type>::type F2;
+    return finish<F2>(v);
+  }
+
+ private:
+  template <class F2, class V>
+  typename std::enable_if<std::is_void<F2>::value, T>::type finish(const V& v) const {
+    return host_cond<T>(chain, (T)v);
+  }
+  template <class F2, class V>
+  auto finish(const V& v, typename std::enable_if<!std::is_void<F2>::value, int>::type = 0) const {
     auto tail = Operand<V>::template node<T>(v);
     auto node = fold_cond<T>(chain, tail);
-    return NeboExpression<decltype(node), F2>(node);
+    return typename Wrap<decltype(node), F2>::type(node);
   }
 };
 }  // namespace nebo_detail
 
 template <class Tst, class V>
 auto cond(const Tst& t, const V& v) {
-  static_assert(nebo_detail::BoolOperand<Tst>::ok, "Nebo cond: a clause test must be a boolean expression or a mask");
+  static_assert(nebo_detail::BoolOperand<Tst>::ok, "Nebo cond: a clause test must be a boolean expression, a mask or a bool");
   typedef typename nebo_detail::MergeField<typename nebo_detail::BoolOperand<Tst>::field_type,
                                            typename nebo_detail::Operand<V>::field_type>::type F;
-  typedef typename F::value_type T;
+  typedef typename nebo_detail::ValueTypeOf<F>::type T;
   auto tn = nebo_detail::BoolOperand<Tst>::node(t);
   auto vn = nebo_detail::Operand<V>::template node<T>(v);
   typedef nebo_detail::ClauseLink<nebo_detail::ClauseEnd, decltype(tn), decltype(vn)> Link;
   return nebo_detail::CondBuilder<F, Link>{Link{nebo_detail::ClauseEnd(), tn, vn}};
+}
+
+// cond(value): the value itself (a number for a scalar, else the same expression)
+template <class V, class = typename std::enable_if<std::is_arithmetic<V>::value>::type>
+double cond(const V& v) {
+  return (double)v;
+}
+template <class V, class = typename std::enable_if<nebo_detail::Operand<V>::ok && !nebo_detail::Operand<V>::scalar>::type,
+          class = void>
+auto cond(const V& v) {
+  typedef typename nebo_detail::Operand<V>::field_type F;
+  typedef typename F::value_type T;
+  auto node = nebo_detail::Operand<V>::template node<T>(v);
+  return typename nebo_detail::Wrap<decltype(node), F>::type(node);
 }
 
 }  // namespace SpatialOps

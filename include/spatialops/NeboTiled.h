@@ -145,6 +145,8 @@ template <typename T>
 struct IsLeaf<DField<T>> : std::true_type {};
 template <typename T>
 struct IsLeaf<DScalar<T>> : std::true_type {};
+template <typename T>
+struct IsLeaf<DSingleValue<T>> : std::true_type {};
 
 template <class D, class R, int Off, class Enable = void>
 struct Tile {  // leaves, masks and anything without children that matter

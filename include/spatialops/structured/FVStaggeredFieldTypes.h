@@ -24,6 +24,8 @@ typedef SpatialField<ZVol> ZVolField;
 typedef SpatialField<ZSurfX> ZSurfXField;
 typedef SpatialField<ZSurfY> ZSurfYField;
 typedef SpatialField<ZSurfZ> ZSurfZField;
+// one value held in a field (a 1x1x1 window without ghosts); broadcast where it meets a field
+typedef SpatialField<SingleValue> SingleValueField;
 
 template <typename VolT> struct FaceTypes;
 template <> struct FaceTypes<SVolField> { typedef SSurfXField XFace; typedef SSurfYField YFace; typedef SSurfZField ZFace; };

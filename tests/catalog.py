@@ -196,6 +196,35 @@ def run_catalog(domain):
     simple("chain_heat_rhs", "SVol", heat_rhs)
     simple("chain_filter_cond", "SVol", lambda: db.filter()(cond(a > 0.0, a, b * 0.5)))
 
+    # SingleValue fields (catalog_ctx.h: 2u + 0.25 in a 1x1x1 window): in an expression the value
+    # with no ghost limit, which the oracle's scalar leaf is; SingleValue results are 1x1x1 records
+    def sv(k):
+        return 2.0 * float(nebo_io.uniform_pm1(nebo_io.field_stream(17, k, C.domain), 1)[0]) + 0.25
+    s1, s2 = sv(0), sv(1)
+    S1, S2 = O.Scalar(s1), O.Scalar(s2)
+
+    def sv_rec(name, v):
+        C.records[name] = ("field", nebo_io.TYPE_CODES["SingleValue"], np.full((1, 1, 1), v, dtype=np.float64))
+
+    simple("sv_broadcast", "SVol", lambda: S1)
+    simple("sv_times_int", "SVol", lambda: S1 * 4.0)
+    simple("sv_minus_field", "SVol", lambda: S1 - a)
+    simple("sv_div_sv", "SVol", lambda: S1 / S2)
+    simple("sv_mixed", "XVol", lambda: xa * (S1 + S2) - S2 * 0.5)
+    sv_rec("sv_to_sv", s1 * s2 + 1.5)
+    sv_rec("sv_copy", s2)
+    sv_rec("sv_scalar", 2.75)
+    simple("sv_interior", "SVol", lambda: S1 + 0.25, use_ghost=False)
+    simple("sv_stencil", "XVol", lambda: is2x(a) * S1 + S2)
+    simple("cond_final_sv", "SVol", lambda: S1 + S2)
+    simple("cond_final_field", "SVol", lambda: a + b)
+    simple("cond_bool_sv", "SVol", lambda: O.Scalar(2.0))  # cond(false, sv1)(2.0)
+    simple("cond_bool_field", "SVol", lambda: a + b)       # cond(true, a + b)(2.0)
+    simple("cond_sv_test", "SVol", lambda: cond(S1 < 0.0, a, S2 * 2.0))
+    sv_rec("cond_sv_to_sv", s1 + s2 if s1 > s2 else s2)
+    simple("cond_field_sv_value", "SVol", lambda: cond(a > 0.0, S1, b))
+    C.val("cond_simple", 1.0 + 10.0 * 2.0 + 100.0 * 4.5)
+
     # reductions
     def red_field():
         for op in ("sum", "max", "min", "norm"):

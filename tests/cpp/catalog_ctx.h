@@ -78,6 +78,7 @@ TYPE_CODE(SSurfXField, 5) TYPE_CODE(SSurfYField, 6) TYPE_CODE(SSurfZField, 7)
 TYPE_CODE(XSurfXField, 8) TYPE_CODE(XSurfYField, 9) TYPE_CODE(XSurfZField, 10)
 TYPE_CODE(YSurfXField, 11) TYPE_CODE(YSurfYField, 12) TYPE_CODE(YSurfZField, 13)
 TYPE_CODE(ZSurfXField, 14) TYPE_CODE(ZSurfYField, 15) TYPE_CODE(ZSurfZField, 16)
+TYPE_CODE(SingleValueField, 17)
 
 template <typename F>
 static void dump(Out& o, const std::string& name, const F& f) {
@@ -124,6 +125,29 @@ struct CatalogCtx {
       inputs[key] = f;
     }
     return *static_cast<F*>(inputs[key].get());
+  }
+
+  // SingleValue fields: a 1x1x1 window without ghosts (test/NeboTest.cpp's SVwindow); the value
+  // 2u + 0.25 rounds once however the compiler contracts it
+  SingleValueField make_sv() {
+    const GhostData g(0);
+    const BoundaryCellInfo bc = BoundaryCellInfo::build<SingleValueField>(false, false, false);
+    const MemoryWindow w = get_window_with_ghost(IntVec(1, 1, 1), g, bc);
+    return SingleValueField(w, bc, g, NULL);
+  }
+  SingleValueField& sv(int k) {
+    std::pair<int, int> key(TypeCode<SingleValueField>::value, k);
+    if (!inputs.count(key)) {
+      std::shared_ptr<SingleValueField> f(new SingleValueField(make_sv()));
+      f->field_values(CPU_INDEX)[0] = 2.0 * catalog::uniform_pm1(catalog::field_stream(17, k, domain_id), 0) + 0.25;
+      inputs[key] = f;
+    }
+    return *static_cast<SingleValueField*>(inputs[key].get());
+  }
+  SingleValueField fresh_sv() {
+    SingleValueField f = make_sv();
+    f.field_values(CPU_INDEX)[0] = catalog::CATALOG_SENTINEL_VALUE;
+    return f;
   }
 
   template <typename F> F fresh() {

@@ -12,13 +12,14 @@ import numpy as np
 
 SENTINEL = -7777.25
 
-# location type codes shared with tests/cpp (SVol=1 ... ZSurfZ=16)
+# location type codes shared with tests/cpp (SVol=1 ... ZSurfZ=16, SingleValue=17)
 TYPE_CODES = {
     "SVol": 1, "XVol": 2, "YVol": 3, "ZVol": 4,
     "SSurfX": 5, "SSurfY": 6, "SSurfZ": 7,
     "XSurfX": 8, "XSurfY": 9, "XSurfZ": 10,
     "YSurfX": 11, "YSurfY": 12, "YSurfZ": 13,
     "ZSurfX": 14, "ZSurfY": 15, "ZSurfZ": 16,
+    "SingleValue": 17,
 }
 
 
