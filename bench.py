@@ -82,19 +82,21 @@ def ncu_traffic(kernel, workload):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every interval_ms while running."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, bus_id=None):
+    def __init__(self, bus_id=None, interval_ms=200):
         self.rows = []
         self.proc = None
         self.bus_id = bus_id
+        self.interval_ms = interval_ms
 
     def start(self):
-        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms",
+               str(self.interval_ms)]
         if self.bus_id:
             cmd += ["-i", self.bus_id]
         try:
@@ -511,6 +513,165 @@ def make_workload(N, name, n):
     raise SystemExit(f"unknown workload {name}")
 
 
+# ----------------------------------------------------------------------------- metric parts
+# The metric names several comparisons ("Gcell-upd/s & %HBM peak: batched/FP32 vs plain FP64;
+# adjoint/fwd cost ratio").  The headline line carries each of them, timed in the same run with
+# CUDA events on the launching stream, each with its own clock record:
+#   heat_fp64     the plain FP64 heat RHS + Euler update at 256^3: Gcell-upd/s and %HBM peak
+#   patches       512 batched patches x 200 steps: FP32 / FP64 cell-update ratio and the
+#                 largest per-patch relative error of the FP32 state against the FP64 one
+#   transport     512^3 + 2 ghosts, 50 RK2 steps: FP32-storage / FP64 ratio and relative error
+#   adjoint       192^3 x 500 steps: gradient / forward device-time ratios
+#   dropin        `<<=` itself (tests/cpp/assign_timing): the deep chain, the box filter and the
+#                 heat update written as the reference's users write them, against the hand kernels
+def _timed(fn, steps, bus):
+    """(ms per step, clocks) of `steps` calls of fn (or one fn(steps) call when fn takes k)."""
+    import torch
+
+    sampler = ClockSampler(bus, interval_ms=100)
+    sampler.start()
+    time.sleep(0.25)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    fn(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    return e0.elapsed_time(e1) / steps, clocks
+
+
+def _steps_for(fn, target_s=0.6, cap=4000):
+    """How many steps fill about target_s of device time (one warm call of fn(1) measured)."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    fn(1)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = max(e0.elapsed_time(e1), 1e-3)
+    return int(max(3, min(cap, target_s * 1e3 / ms)))
+
+
+def part_heat(N, bus, peak):
+    W = Heat(N, 256, "f64")
+    run = lambda k: [W.step() for _ in range(k)]
+    run(3)
+    k = _steps_for(run)
+    ms, clocks = _timed(run, k, bus)
+    cells = W.cells
+    gbs = BYTES_PER_CELL["heat"] * cells / (ms * 1e-3) / 1e9
+    return {"workload": heat_label(256, "f64"), "gcell_upd_s": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
+            "steps": k, "alg_gbs": gbs, "hbm_frac": gbs / peak, "hbm_peak_gbs": peak, "clocks": clocks}
+
+
+def part_patches(N, bus):
+    import torch
+
+    out = {}
+    states = {}
+    for dtype in ("f64", "f32"):
+        W = Patches(N, dtype)
+        W.run(3)
+        k = _steps_for(W.run)
+        ms, clocks = _timed(W.run, k, bus)
+        out[dtype] = {"gcell_upd_s": W.cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "steps": k, "clocks": clocks}
+        # 200 steps from the initial state for the error
+        W.ps.arena(0).copy_(W.host)
+        W.ps.fill_ghosts(0)
+        fin = W.ps.run(200, start=0)
+        W.ps.sync(fin)
+        states[dtype] = [W.ps.window(fin, p).clone() for p in range(W.ps.npatch)]
+        cells = W.cells
+        del W
+        torch.cuda.empty_cache()
+    errs = [float((a - b).abs().max() / b.abs().max()) for a, b in zip(states["f32"], states["f64"])]
+    return {"workload": patches_label(512, cells, "f64/f32"), "fp64": out["f64"], "fp32": out["f32"],
+            "fp32_over_fp64": out["f32"]["gcell_upd_s"] / out["f64"]["gcell_upd_s"],
+            "fp32_max_patch_rel_err_200_steps": max(errs), "fp32_median_patch_rel_err_200_steps": float(np.median(errs)),
+            "error_reference": "the FP64 patch set (bit-identical to the oracle's serial walk per patch)"}
+
+
+def part_transport(N, bus):
+    import torch
+
+    out, phis = {}, {}
+    for dtype in ("f64", "f32"):
+        W = TransportWL(N, 512, dtype)
+        phi0 = W.t.phi.clone()
+        W.run(1)
+        k = 10 if dtype == "f64" else 40
+        ms, clocks = _timed(W.run, k, bus)
+        out[dtype] = {"gcell_upd_s": W.cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "steps": k, "clocks": clocks}
+        W.t.phi.copy_(phi0)
+        W.run(50)
+        g = 2
+        phis[dtype] = W.t.phi[g:-g, g:-g, g:-g].clone()
+        del W, phi0
+        torch.cuda.empty_cache()
+    err = float((phis["f32"] - phis["f64"]).abs().max() / phis["f64"].abs().max())
+    return {"workload": transport_label(512, "f64/f32"), "fp64": out["f64"], "fp32": out["f32"],
+            "fp32_over_fp64": out["f32"]["gcell_upd_s"] / out["f64"]["gcell_upd_s"],
+            "fp32_rel_err_50_steps": err, "error_reference": "the FP64 transport (1e-13 of the oracle on small cases)"}
+
+
+def part_adjoint(N, bus):
+    import torch
+
+    W = AdjointWL(N, 192)
+    sampler = ClockSampler(bus, interval_ms=100)
+    sampler.start()
+    fwd = W.forward_ms()
+    W.gradient_ms("f64")  # warm
+    g64 = W.gradient_ms("f64")
+    g32 = W.gradient_ms("f32")
+    W.gradient_ms("f32", N.CHECKPOINT_AUTO)  # warm: the pool grows to hold every state
+    gall = W.gradient_ms("f32", N.CHECKPOINT_AUTO)
+    clocks = sampler.stop()
+    del W
+    torch.cuda.empty_cache()
+    return {"workload": adjoint_label(192, 500), "forward_ms": fwd, "gradient_ms_fp64": g64,
+            "gradient_ms_f32_products": g32, "gradient_ms_every_state_kept": gall,
+            "adjoint_over_forward_fp64": g64 / fwd, "adjoint_over_forward_f32_products": g32 / fwd,
+            "adjoint_over_forward_every_state_kept": gall / fwd, "checkpoints": "ceil(sqrt(500)) = 23",
+            "clocks": clocks}
+
+
+def part_dropin(bus):
+    """`<<=` through the drop-in headers (C++ program built by build.py), parsed from its JSON."""
+    exe = os.path.join(REPO, "tests", "cpp", "_build", "assign_timing")
+    if not os.path.exists(exe):
+        return {"unavailable": "tests/cpp/_build/assign_timing not built"}
+    sampler = ClockSampler(bus, interval_ms=100)
+    sampler.start()
+    r = subprocess.run([exe, "256", "10"], capture_output=True, text=True, timeout=600)
+    clocks = sampler.stop()
+    if r.returncode != 0:
+        return {"unavailable": f"assign_timing exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    d["clocks"] = clocks
+    d["deep_assign_over_hand_chain"] = d["deep_assign"]["ms"] / d["deep_hand_chain"]["ms"]
+    d["heat_assign_over_hand"] = d["heat_assign"]["ms"] / d["heat_hand"]["ms"]
+    return d
+
+
+def metric_parts(N, bus, peak):
+    parts = {}
+    for name, fn in (("heat_fp64", lambda: part_heat(N, bus, peak)), ("patches", lambda: part_patches(N, bus)),
+                     ("transport", lambda: part_transport(N, bus)), ("adjoint", lambda: part_adjoint(N, bus)),
+                     ("dropin", lambda: part_dropin(bus))):
+        t0 = time.perf_counter()
+        try:
+            parts[name] = fn()
+        except Exception as e:  # a part that fails is reported, the headline stands
+            parts[name] = {"error": f"{type(e).__name__}: {e}"}
+        parts[name]["wall_s"] = time.perf_counter() - t0
+    return parts
+
+
 # ----------------------------------------------------------------------------- CPU legs
 def _oracle():
     sys.path.insert(0, os.path.join(REPO, "tests"))
@@ -521,20 +682,52 @@ def _oracle():
 
 def cpu_run(workload, n_xy, nz, threads):
     """One step of the workload on the CPU oracle over an n_xy x n_xy x nz block; returns seconds."""
+    return cpu_stepper(workload, (n_xy, n_xy, nz))(threads)
+
+
+def cpu_stepper(workload, shape):
+    """A sampler: one deep-chain or heat step on the CPU oracle over `shape` (inputs made once);
+    sampler(threads) returns seconds."""
     O = _oracle()
     from spatialops_gb300 import workloads as W
 
-    shape = (n_xy, n_xy, nz)
     if workload == "deep":
         a, b, c, pts = W.deep_inputs(shape)
         bits = W.mask_bits_from_points(pts, shape)
-        t0 = time.perf_counter()
-        O.deep_run(a, b, c, bits, shape, 1.0, threads)
-        return time.perf_counter() - t0
+
+        def run(threads):
+            t0 = time.perf_counter()
+            O.deep_run(a, b, c, bits, shape, 1.0, threads)
+            return time.perf_counter() - t0
+
+        return run
     lam, T0, dt = W.heat_inputs(shape)
-    t0 = time.perf_counter()
-    O.heat_run(lam, T0, shape, 1, dt, threads)
-    return time.perf_counter() - t0
+
+    def run(threads):
+        t0 = time.perf_counter()
+        O.heat_run(lam, T0, shape, 1, dt, threads)
+        return time.perf_counter() - t0
+
+    return run
+
+
+def cpu_patches(count=512):
+    """A sampler: one step of every patch of the 512-patch set by the oracle (each patch's walk
+    over z-slabs with the given threads); sampler(threads) returns seconds."""
+    O = _oracle()
+    from spatialops_gb300 import workloads as W
+
+    shapes = W.patch_shapes(count)
+    ins = W.patch_inputs(shapes)
+    lams = [np.full_like(T0, lam) for lam, T0, _ in ins]
+
+    def run(threads):
+        t0 = time.perf_counter()
+        for p, (lam, T0, dt) in enumerate(ins):
+            O.heat_run(lams[p], T0, tuple(int(v) for v in shapes[p]), 1, dt, threads)
+        return time.perf_counter() - t0
+
+    return run, int(np.prod(shapes.astype(np.int64), axis=1).sum())
 
 
 def cpu_particles(n, npart):
@@ -585,19 +778,23 @@ def cpu_gradient(m, steps):
     return run
 
 
-# One bounded sample of each workload by the oracle: (function(threads) -> seconds, units, what).
-# Slab and cube sizes keep a sample well under a second of host time per thread.
+# One bounded sample of each workload by the oracle:
+# (function(threads) -> seconds, cell-updates per call, what, same size as the device arm).
+# The deep chain, the heat step and the patch set run at full size; the transport and the
+# gradient on smaller patches (their full sizes take minutes of host time per step).
 def cpu_sample(workload, n):
-    if workload in ("deep", "heat", "heat32", "patches", "patches32"):
+    if workload in ("deep", "heat", "heat32"):
         kind = "deep" if workload == "deep" else "heat"
-        what = f"{n}x{n}x16 slab of {kind} steps"
-        return (lambda th: cpu_run(kind, n, 16, th)), n * n * 16, what
+        return cpu_stepper(kind, (n, n, n)), n ** 3, f"one full {n}^3 {kind} step", True
+    if workload in ("patches", "patches32"):
+        fn, cells = cpu_patches()
+        return fn, cells, "one step of all 512 patches", True
     if workload in ("transport", "transport32"):
         m = 128
-        return cpu_transport(m), m ** 3, f"one FP64 RK2 step on a {m}^3 periodic patch"
+        return cpu_transport(m), m ** 3, f"one FP64 RK2 step on a {m}^3 periodic patch", False
     if workload == "adjoint":
         m, steps = 48, 20
-        return cpu_gradient(m, steps), m ** 3 * steps, f"gradient over {steps} steps of a {m}^3 patch"
+        return cpu_gradient(m, steps), m ** 3 * steps, f"gradient over {steps} steps of a {m}^3 patch", False
     raise ValueError(workload)
 
 
@@ -613,14 +810,15 @@ def cpu_baseline(workload, n, budget_s=10.0):
                 "sample": f"{reps} x (CellToParticle + ParticleToCell of {npart} particles on the {n}^3 field), "
                           f"serial oracle loops (the reference's operators are serial), {total:.1f} s"}
     if workload in ("deep", "heat", "heat32"):
+        step = cpu_stepper("deep" if workload == "deep" else "heat", (n, n, n))
         reps, total = 0, 0.0
         while total < budget_s and reps < 20:
-            total += cpu_run("deep" if workload == "deep" else "heat", n, n, 1)
+            total += step(1)
             reps += 1
         cells = reps * n ** 3
         return {"value": cells / total / 1e9, "unit": "Gcell-upd/s", "cores": 1, "kind": "port",
                 "sample": f"{reps} full {n}^3 step(s) of the {workload} workload, serial oracle walk, {total:.1f} s"}
-    fn, units, what = cpu_sample(workload, n)
+    fn, units, what, _ = cpu_sample(workload, n)
     reps, total = 0, 0.0
     while total < budget_s and reps < 50:
         total += fn(1)
@@ -656,7 +854,7 @@ def run_reference(args):
         }
         print(json.dumps(line), flush=True)
         return 0
-    fn, units, what = cpu_sample(args.workload, n)
+    fn, units, what, same = cpu_sample(args.workload, n)
     for _ in range(max(args.warmup, 0)):
         fn(threads)
     t = 0.0
@@ -681,7 +879,10 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": label, "cells_per_step": units, "sample": what + " per step"},
+        "config": {"workload": label, "cells_per_step": units, "sample": what + " per step", "same_config": same,
+                   "sample_dtype": "f64",
+                   "note": ("the reference's CPU path runs FP64 here; the device arm's FP32 storage has no CPU "
+                            "counterpart" if w.endswith("32") else "")},
         "cpu_baseline": {"value": value, "unit": "Gcell-upd/s", "cores": 1 if w == "adjoint" else threads,
                          "kind": "port",
                          "sample": f"{what} per step, oracle restatement of the reference's serial walk"
@@ -714,6 +915,8 @@ def main():
                                                              "transport32", "adjoint", "particles"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parts", action="store_true",
+                    help="skip the metric's other comparisons (heat FP64 %%HBM, FP32/FP64 ratios, adjoint ratio, <<=)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -854,6 +1057,11 @@ def main():
         "clocks": clocks,
     }
     line.update(extra)
+    if W.name == "deep" and world == 1 and not args.no_parts:
+        # the headline workload's buffers go first: the parts need the memory
+        del W
+        torch.cuda.empty_cache()
+        line["metric_parts"] = metric_parts(N, bus if isinstance(bus, str) else None, peak)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

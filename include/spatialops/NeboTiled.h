@@ -12,6 +12,9 @@
 // computed once per point.  Field leaves are read with coalesced read-only loads (a tile's
 // neighbours hit L1 and L2, so each input is read from HBM about once).
 //
+// In builds that allow reassociation, a 27-point box sum is first split into three 3-point line
+// sums (x, then y, then z), so the box filter's partial sums are shared too.
+//
 // Everything is decided at compile time from the expression's type: which nodes are
 // materialised, each buffer's box (per-axis reach of the point collections, summed through
 // nested stencils), its shared-memory offset, the fill round, and the tile depth TZ (8, 4, 2
@@ -216,6 +219,54 @@ struct Tile<DCond<T, Test, Val, Rest>, R, Off> {
   static type make(const DCond<T, Test, Val, Rest>& d) { return type{TT::make(d.t), TV::make(d.v), TR::make(d.r)}; }
 };
 
+// The 27-point box sum (the box filters, NeboStencilBuilder.h:454-465) as three 3-point sums,
+// one axis each, when the build allows reassociation (not NEBO_EXACT_ARITHMETIC): about 7 FP64
+// additions per cell instead of 26, the x and y partial sums shared through shared memory.  The
+// result differs from the reference's point-by-point order by rounding only.
+template <class Pts>
+struct BoxMask;
+template <class P>
+struct BoxMask<NeboStencilPointCollection<P, NeboNil>> {
+  static constexpr bool inside = P::X >= -1 && P::X <= 1 && P::Y >= -1 && P::Y <= 1 && P::Z >= -1 && P::Z <= 1;
+  static constexpr long long bits = inside ? (1LL << ((P::X + 1) + 3 * (P::Y + 1) + 9 * (P::Z + 1))) : 0;
+  static constexpr bool ok = inside;
+};
+template <class P, class R>
+struct BoxMask<NeboStencilPointCollection<P, R>> {
+  typedef BoxMask<NeboStencilPointCollection<P, NeboNil>> H;
+  static constexpr long long bits = H::bits | BoxMask<R>::bits;
+  static constexpr bool ok = H::ok && BoxMask<R>::ok;
+};
+template <class Pts>
+struct IsBox27 {
+  static constexpr bool value = Pts::length == 27 && BoxMask<Pts>::ok && BoxMask<Pts>::bits == (1LL << 27) - 1;
+};
+#ifdef NEBO_EXACT_ARITHMETIC
+constexpr bool kReassociate = false;
+#else
+constexpr bool kReassociate = true;
+#endif
+template <class Pts>
+struct SplitBox {
+  static constexpr bool value = kReassociate && IsBox27<Pts>::value;
+};
+typedef NEBO_FIRST_IJK(-1, 0, 0)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(1, 0, 0) Line3X;
+typedef NEBO_FIRST_IJK(0, -1, 0)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(0, 1, 0) Line3Y;
+typedef NEBO_FIRST_IJK(0, 0, -1)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(0, 0, 1) Line3Z;
+
+template <typename T, class Pts, class A, class R, int Off>
+struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<SplitBox<Pts>::value>::type> {
+  typedef DSumStencil<T, Line3Z, DSumStencil<T, Line3Y, DSumStencil<T, Line3X, A>>> Split;
+  typedef Tile<Split, R, Off> TS;
+  typedef typename TS::type type;
+  enum { end = TS::end, rounds = TS::rounds };
+  static type make(const DSumStencil<T, Pts, A>& d) {
+    Split s;
+    s.a.a.a = d.a;
+    return TS::make(s);
+  }
+};
+
 // a stencil of a leaf: reads its neighbours directly
 template <typename T, class Pts, class A, class R, int Off>
 struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<IsLeaf<A>::value>::type> {
@@ -224,7 +275,8 @@ struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<IsLeaf<A>::valu
   static type make(const type& d) { return d; }
 };
 template <typename T, class Pts, class A, class R, int Off>
-struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<IsLeaf<A>::value>::type> {
+struct Tile<DSumStencil<T, Pts, A>, R, Off,
+            typename std::enable_if<IsLeaf<A>::value && !SplitBox<Pts>::value>::type> {
   typedef DSumStencil<T, Pts, A> type;
   enum { end = Off, rounds = 0 };
   static type make(const type& d) { return d; }
@@ -252,7 +304,8 @@ struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::val
   }
 };
 template <typename T, class Pts, class A, class R, int Off>
-struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::value>::type>
+struct Tile<DSumStencil<T, Pts, A>, R, Off,
+            typename std::enable_if<!IsLeaf<A>::value && !SplitBox<Pts>::value>::type>
     : TileSmemStencil<T, Pts, A, R, Off, true> {
   typedef TileSmemStencil<T, Pts, A, R, Off, true> B;
   static typename B::type make(const DSumStencil<T, Pts, A>& d) {
