@@ -264,6 +264,12 @@ enum { NEBO_CHECKPOINT_AUTO = -1 };
  *                      the adjoint state, dJ/dT_0 and J stay FP64.  Six FP64 operations per cell
  *                      and reverse step fewer. */
 enum { NEBO_PRODUCTS_F64 = 0, NEBO_PRODUCTS_F32 = 1 };
+/* OR'ed into `products`: the forward sweep in FP32 (storage and arithmetic of the states, their
+ * checkpoints and the recomputed segments: half the checkpoint memory and HBM traffic of the
+ * forward work), the adjoint state and every accumulation in FP64 on the widened FP32 states.
+ * The gradient is that of the FP64 model evaluated along the FP32 trajectory; J comes from the
+ * FP32 final state. */
+enum { NEBO_FORWARD_F32 = 2 };
 int nebo_heat_gradient_ex(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget,
                           int steps, double dt, int checkpoint_every, int products,
                           const nebo_field* gT0, const nebo_field* glam, double* J,
@@ -274,6 +280,20 @@ int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ain, const ne
 int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget,
                        int steps, double dt, int checkpoint_every, const nebo_field* gT0,
                        const nebo_field* glam, double* J, nebo_stream_t stream);
+
+/* Transposed stencil operator (reverse mode of a stencil assignment; no counterpart in the
+ * reference).  For the forward assignment dst(i) = sum_k coefs[k] * src(i + p_k) over the write
+ * region `limits` of dst ({xlo,xhi,ylo,yhi,zlo,zhi}, interior-relative, as nebo_write_limits
+ * gives it) -- Interpolant, Gradient, Divergence, FD and box-filter stencils alike, their points
+ * p_k (3 ints each, listed order) and coefficients as the operator defines them
+ * (spatialops/NeboStencilBuilder.h:154-232, structured/stencil/StencilBuilder.cpp:52-220) --
+ * every cell j of src_bar's window receives
+ *     sum over the k with j - p_k in limits of coefs[k] * dst_bar(j - p_k)
+ * (accumulate != 0: added to its value; else written, 0 where no point contributes).  FP64, up
+ * to 32 points, deterministic (a gather in listed point order, no atomics). */
+int nebo_stencil_transpose(const nebo_field* dst_bar, const int32_t limits[6], const nebo_field* src_bar,
+                           int32_t npoints, const int32_t* points, const double* coefs, int accumulate,
+                           nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ particle <-> cell operators
  * Replace Particle::CellToParticle<CellField>::apply_to_field and

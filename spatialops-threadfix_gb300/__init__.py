@@ -103,6 +103,7 @@ SIGNATURES = [
     ("nebo_box_filter", _I, [_FP, _FP, _I, _P, _P]),
     ("nebo_cell_to_particle", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _FP, _P, _P]),
     ("nebo_particle_to_cell", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _P, _FP, _P]),
+    ("nebo_stencil_transpose", _I, [_FP, ctypes.POINTER(ctypes.c_int32), _FP, ctypes.c_int32, _P, _P, _I, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
     ("nebo_profile_report", _I, [ctypes.c_char_p, ctypes.c_size_t, _I]),
@@ -421,24 +422,44 @@ class Transport:
 CHECKPOINT_AUTO = -1  # NEBO_CHECKPOINT_AUTO: keep every state when they fit in device memory
 
 
-def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None, products="f64"):
+FORWARD_F32 = 2  # NEBO_FORWARD_F32
+
+
+def heat_gradient(T0, lam, Ttarget, steps, dt, checkpoint_every=0, stream=None, products="f64", forward="f64"):
     """(J, dJ/dT0, dJ/dlambda) for J = 1/2 sum (T_N - T_target)^2 (fields: SVol, 1 ghost, FP64).
 
     checkpoint_every: 0 = ceil(sqrt(steps)); CHECKPOINT_AUTO = every state when they fit.
-    products="f32": the lambda gradient's face products in FP32 (nebo_heat_gradient_ex)."""
+    products="f32": the lambda gradient's face products in FP32 (nebo_heat_gradient_ex).
+    forward="f32": the forward states (and checkpoints) in FP32, the adjoint in FP64."""
     gT = Field(T0.loc, T0.n, T0.ghost)
     gl = Field(T0.loc, T0.n, T0.ghost)
     J = ctypes.c_double()
     a, b, c, d, e = T0.desc(), lam.desc(), Ttarget.desc(), gT.desc(), gl.desc()
-    if products == "f64":
+    if products == "f64" and forward == "f64":
         _check(lib().nebo_heat_gradient(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt),
                                         int(checkpoint_every), ctypes.byref(d), ctypes.byref(e), ctypes.byref(J),
                                         _stream(stream)))
     else:
         _check(lib().nebo_heat_gradient_ex(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps),
-                                           float(dt), int(checkpoint_every), {"f32": 1}[products], ctypes.byref(d),
+                                           float(dt), int(checkpoint_every),
+                                           {"f64": 0, "f32": 1}[products] | (FORWARD_F32 if forward == "f32" else 0),
+                                           ctypes.byref(d),
                                            ctypes.byref(e), ctypes.byref(J), _stream(stream)))
     return J.value, gT, gl
+
+
+def stencil_transpose(dst_bar, limits, src_bar, points, coefs, accumulate=False, stream=None):
+    """src_bar(j) (+)= sum_k coefs[k] * dst_bar(j - points[k]) over j - points[k] in limits: the
+    transpose of dst(i) = sum_k coefs[k] * src(i + points[k]) on the write region `limits`."""
+    pts = np.ascontiguousarray(points, dtype=np.int32).reshape(-1, 3)
+    cf = np.ascontiguousarray(coefs, dtype=np.float64).reshape(-1)
+    if len(pts) != len(cf):
+        raise RuntimeError("Nebo error in stencil_transpose: one coefficient per point")
+    lim = (ctypes.c_int32 * 6)(*[int(v) for v in limits])
+    a, b = dst_bar.desc(), src_bar.desc()
+    _check(lib().nebo_stencil_transpose(ctypes.byref(a), lim, ctypes.byref(b), len(pts),
+                                        ctypes.c_void_p(pts.ctypes.data), ctypes.c_void_p(cf.ctypes.data),
+                                        int(bool(accumulate)), _stream(stream)))
 
 
 def heat_adjoint_step(Tk, Ain, Aout, lam, glam, dt, stream=None):

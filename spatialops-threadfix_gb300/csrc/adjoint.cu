@@ -31,6 +31,10 @@ namespace {
 constexpr int BX = 32;
 constexpr int BY = 8;
 
+// A forward state as a double (FP32 states widen exactly).
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float v) { return (double)v; }
+
 __device__ __forceinline__ void store_images1(double* base, int sy, long sz, int x, int y, int z, int nx, int ny, int nz,
                                               double v) {
   base[(long)x + (long)sy * y + sz * z] = v;
@@ -56,8 +60,8 @@ __device__ __forceinline__ void store_images1(double* base, int sy, long sz, int
 // differences themselves are exact FP64, so no cancellation is amplified), their sum is FP32 and
 // only the fold into glam is FP64: 6 FP64 operations per cell fewer, and the adjoint state A,
 // hence dJ/dT0, is unaffected.
-template <bool EXACT, bool LF>
-__global__ void __launch_bounds__(BX* BY, 4) heat_adjoint_kernel(const double* __restrict__ T, const double* __restrict__ Ain,
+template <bool EXACT, bool LF, typename S = double>
+__global__ void __launch_bounds__(BX* BY, 4) heat_adjoint_kernel(const S* __restrict__ T, const double* __restrict__ Ain,
                                                               double* __restrict__ Aout, const double* __restrict__ L,
                                                               const double* __restrict__ lfx,
                                                               const double* __restrict__ lfy,
@@ -79,7 +83,7 @@ __global__ void __launch_bounds__(BX* BY, 4) heat_adjoint_kernel(const double* _
   // (dA, dT) of face (a, b); dT as the product operand type
   auto face = [&](long a, long b, double& da, P& dt) {
     da = __ldg(Ain + b) - __ldg(Ain + a);
-    const double d = __ldg(T + b) - __ldg(T + a);
+    const double d = to_f64(__ldg(T + b)) - to_f64(__ldg(T + a));  // exact for FP32 states too
     if constexpr (EXACT) dt = d; else dt = fixmath::f32_trunc(d);
   };
   auto coef = [&](const double* lf, long a, long b) { return LF ? __ldg(lf + b) : __ldg(L + a) + __ldg(L + b); };
@@ -157,15 +161,22 @@ __global__ void face_coef_kernel(const double* __restrict__ L, double* __restric
   }
 }
 
+// dst = src rounded to FP32 (whole windows of the same layout).
+__global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = fixmath::f64_to_f32_rn(src[i]);
+}
+
 // abar_N = T_N - T_target on the interior (+ images); per-block partial sums of (T_N - T_target)^2.
-__global__ void loss_seed_kernel(const double* __restrict__ T, const double* __restrict__ Tt, double* __restrict__ A,
+template <typename S>
+__global__ void loss_seed_kernel(const S* __restrict__ T, const double* __restrict__ Tt, double* __restrict__ A,
                                  int sy, long sz, int nx, int ny, int nz, double* __restrict__ partial) {
   double acc = 0.0;
   const long total = (long)nx * ny * nz;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
     const long c = (long)x + (long)sy * y + sz * z;
-    const double d = T[c] - Tt[c];
+    const double d = to_f64(T[c]) - Tt[c];
     acc = fma(d, d, acc);
     store_images1(A, sy, sz, x, y, z, nx, ny, nz, d);
   }
@@ -223,25 +234,26 @@ extern "C" int nebo_heat_adjoint_step(const nebo_field* Tk, const nebo_field* Ai
 namespace {
 // One reverse step of the gradient driver: precomputed face coefficients (View bases of the
 // three face arrays, same layout as T), exact or FP32 face products.
+template <typename S>
 int adjoint_step_lf(const nebo_field* Tk, const nebo_field* Ain, const nebo_field* Aout, const double* lfx,
                     const double* lfy, const double* lfz, const nebo_field* glam, double dt, bool exact,
                     cudaStream_t s) {
   int n[3];
   interior_extent(*Tk, n);
-  const View<double> vt = make_view<double>(*Tk), va = make_view<double>(*Ain), vo = make_view<double>(*Aout),
-                     vg = make_view<double>(*glam);
+  const View<S> vt = make_view<S>(*Tk);
+  const View<double> va = make_view<double>(*Ain), vo = make_view<double>(*Aout), vg = make_view<double>(*glam);
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
   static std::atomic<int> per_sm[2];  // z chunks in whole waves of resident blocks (zero: not queried)
-  const int bps = exact ? blocks_per_sm(heat_adjoint_kernel<true, true>, BX * BY, per_sm[1])
-                        : blocks_per_sm(heat_adjoint_kernel<false, true>, BX * BY, per_sm[0]);
+  const int bps = exact ? blocks_per_sm(heat_adjoint_kernel<true, true, S>, BX * BY, per_sm[1])
+                        : blocks_per_sm(heat_adjoint_kernel<false, true, S>, BX * BY, per_sm[0]);
   const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);
   const int chunks = (n[2] + zchunk - 1) / zchunk;
   LaunchScope ls("heat_adjoint_step", s);
   if (exact)
-    heat_adjoint_kernel<true, true><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
+    heat_adjoint_kernel<true, true, S><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
         vt.base, va.base, vo.base, nullptr, lfx, lfy, lfz, vg.base, vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
   else
-    heat_adjoint_kernel<false, true><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
+    heat_adjoint_kernel<false, true, S><<<dim3(gxb, gyb, chunks), dim3(BX, BY), 0, s>>>(
         vt.base, va.base, vo.base, nullptr, lfx, lfy, lfz, vg.base, vt.sy, vt.sz, n[0], n[1], n[2], zchunk, 0.5 * dt);
   NEBO_LAUNCH_CHECK("nebo_heat_gradient (reverse step)");
   return NEBO_OK;
@@ -249,16 +261,26 @@ int adjoint_step_lf(const nebo_field* Tk, const nebo_field* Ain, const nebo_fiel
 }  // namespace
 
 namespace {
-// Buffers of the pool (each one field): [0, nck) checkpoints T_0, T_L, ...; [nck, nck+L) segment
-// states; two adjoint states; one forward temporary; three face-coefficient arrays; then 256
+// The state buffers (element type S, `stride` elements apart): [0, nck) checkpoints T_0, T_L, ...;
+// [nck, nck+L) segment states; two forward temporaries; for FP32 states one more for the FP32
+// copy of lambda.  The FP64 buffers: two adjoint states, three face-coefficient arrays, then 256
 // doubles of loss partials.
-int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const nebo_field* T0, const nebo_field* lam,
-                  const nebo_field* Ttarget, int steps, double dt, bool exact, const nebo_field* gT0,
-                  const nebo_field* glam, double* J, nebo_stream_t stream) {
+template <typename S>
+int gradient_impl(S* spool, size_t stride, double* dpool, size_t cells, int nck, int L, const nebo_field* T0,
+                  const nebo_field* lam, const nebo_field* Ttarget, int steps, double dt, bool exact,
+                  const nebo_field* gT0, const nebo_field* glam, double* J, nebo_stream_t stream) {
+  constexpr bool f64 = std::is_same<S, double>::value;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = cells * sizeof(double);
-  auto buf = [&](size_t i) { return pool + i * cells; };
-  double* partial = pool + (size_t)nbuf * cells;
+  auto sbuf = [&](size_t i) { return spool + i * stride; };
+  auto dbuf = [&](size_t i) { return dpool + i * cells; };
+  double* partial = dpool + 5 * cells;
+  auto state_at = [&](S* p) {
+    nebo_field f = *T0;
+    f.data = p;
+    f.dtype = f64 ? NEBO_F64 : NEBO_F32;
+    return f;
+  };
   auto field_at = [&](double* p) {
     nebo_field f = *T0;
     f.data = p;
@@ -271,49 +293,60 @@ int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const ne
   interior_extent(*T0, n);
   // lambda's ghosts must be periodic images (they are read at boundary faces); face coefficients
   if ((rc = fill_periodic_any(&lamf, s))) return rc;
-  double* A0 = buf(nck + L);
-  double* A1 = buf(nck + L + 1);
-  double* tmp = buf(nck + L + 2);
+  double* A0 = dbuf(0);
+  double* A1 = dbuf(1);
+  S* tmp0 = sbuf(nck + L);
+  S* tmp1 = sbuf(nck + L + 1);
   const View<double> vl = make_view<double>(lamf);
   const long origin = vl.base - (const double*)lamf.data;  // interior origin within a window
-  double* lf[3] = {buf(nck + L + 3) + origin, buf(nck + L + 4) + origin, buf(nck + L + 5) + origin};
+  double* lf[3] = {dbuf(2) + origin, dbuf(3) + origin, dbuf(4) + origin};
   {
     LaunchScope ls("face_coef", s);
     face_coef_kernel<<<num_sms() * 4, 256, 0, s>>>(vl.base, lf[0], lf[1], lf[2], vl.sy, vl.sz, n[0], n[1], n[2]);
     NEBO_LAUNCH_CHECK("nebo_heat_gradient (face coefficients)");
   }
+  // the forward sweep's lambda and T_0 in the state type
+  nebo_field lamS = lamf;
+  if constexpr (!f64) {
+    lamS = state_at(sbuf(nck + L + 2));
+    LaunchScope ls("to_f32", s);
+    to_f32_kernel<<<num_sms() * 4, 256, 0, s>>>((const double*)lamf.data, (float*)lamS.data, (long)cells);
+    to_f32_kernel<<<num_sms() * 4, 256, 0, s>>>((const double*)T0->data, (float*)sbuf(0), (long)cells);
+    NEBO_LAUNCH_CHECK("nebo_heat_gradient (FP32 forward copies)");
+  } else {
+    NEBO_CUDA_TRY(cudaMemcpyAsync(sbuf(0), T0->data, bytes, cudaMemcpyDeviceToDevice, s));
+  }
   // forward sweep: checkpoints every L steps; the last segment's states go straight to the
   // segment buffers (they need no recomputation)
   const int klast = (nck - 1) * L;
-  NEBO_CUDA_TRY(cudaMemcpyAsync(buf(0), T0->data, bytes, cudaMemcpyDeviceToDevice, s));
   {
-    nebo_field c0 = field_at(buf(0));
+    nebo_field c0 = state_at(sbuf(0));
     if ((rc = fill_periodic_any(&c0, s))) return rc;
   }
-  double* cur = buf(0);
+  S* cur = sbuf(0);
   for (int k = 0; k < steps && !rc; ++k) {
     const int j = k + 1;  // state being written
-    double* nxt;
+    S* nxt;
     if (j == steps)
-      nxt = cur == tmp ? A1 : tmp;
+      nxt = cur == tmp0 ? tmp1 : tmp0;
     else if (j % L == 0)
-      nxt = buf(j / L);
+      nxt = sbuf(j / L);
     else if (j > klast)
-      nxt = buf(nck + (j - klast - 1));
+      nxt = sbuf(nck + (j - klast - 1));
     else
-      nxt = cur == tmp ? A1 : tmp;
-    nebo_field a = field_at(cur), b = field_at(nxt);
-    rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
+      nxt = cur == tmp0 ? tmp1 : tmp0;
+    nebo_field a = state_at(cur), b = state_at(nxt);
+    rc = heat_step_dispatch(&a, &b, &lamS, dt, unit, s);
     cur = nxt;
   }
   if (rc) return rc;
-  // seed: abar_N = T_N - T_target, J (the final state is in tmp or A1; the seed goes to A0)
-  const View<double> vt = make_view<double>(field_at(cur));
+  // seed: abar_N = T_N - T_target, J
+  const View<S> vt = make_view<S>(state_at(cur));
   const View<double> vtt = make_view<double>(*Ttarget);
   const View<double> va = make_view<double>(field_at(A0));
   {
     LaunchScope ls("loss_seed", s);
-    loss_seed_kernel<<<256, 256, 0, s>>>(vt.base, vtt.base, va.base, vt.sy, vt.sz, n[0], n[1], n[2], partial);
+    loss_seed_kernel<S><<<256, 256, 0, s>>>(vt.base, vtt.base, va.base, vt.sy, vt.sz, n[0], n[1], n[2], partial);
   }
   NEBO_CUDA_TRY(cudaGetLastError());
   double hp[256];
@@ -326,14 +359,14 @@ int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const ne
     const int k0 = seg * L, k1 = (k0 + L < steps) ? k0 + L : steps;  // states k0 .. k1-1
     // recompute states k0+1 .. k1-1 into the segment buffers (state k0 is the checkpoint)
     for (int k = k0; seg != nck - 1 && k + 1 < k1 && !rc; ++k) {
-      nebo_field a = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
-      nebo_field b = field_at(buf(nck + (k - k0)));
-      rc = heat_step_dispatch(&a, &b, &lamf, dt, unit, s);
+      nebo_field a = state_at(k == k0 ? sbuf(seg) : sbuf(nck + (k - k0 - 1)));
+      nebo_field b = state_at(sbuf(nck + (k - k0)));
+      rc = heat_step_dispatch(&a, &b, &lamS, dt, unit, s);
     }
     for (int k = k1 - 1; k >= k0 && !rc; --k) {
-      nebo_field tk = field_at(k == k0 ? buf(seg) : buf(nck + (k - k0 - 1)));
+      nebo_field tk = state_at(k == k0 ? sbuf(seg) : sbuf(nck + (k - k0 - 1)));
       nebo_field ai = field_at(Ain), ao = field_at(Aout);
-      rc = adjoint_step_lf(&tk, &ai, &ao, lf[0], lf[1], lf[2], glam, dt, exact, s);
+      rc = adjoint_step_lf<S>(&tk, &ai, &ao, lf[0], lf[1], lf[2], glam, dt, exact, s);
       double* t = Ain;
       Ain = Aout;
       Aout = t;
@@ -351,8 +384,8 @@ int gradient_impl(double* pool, size_t cells, int nck, int L, int nbuf, const ne
 }
 
 int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps, double dt,
-                   int checkpoint_every, bool exact, const nebo_field* gT0, const nebo_field* glam, double* J,
-                   nebo_stream_t stream, const char* what) {
+                   int checkpoint_every, bool exact, bool forward_f32, const nebo_field* gT0, const nebo_field* glam,
+                   double* J, nebo_stream_t stream, const char* what) {
   const nebo_field* fs[5] = {T0, lam, Ttarget, gT0, glam};
   for (int i = 0; i < 5; ++i) {
     int rc = check_field(fs[i], what);
@@ -364,28 +397,40 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
   if (steps < 1) return fail(NEBO_ERR_INVALID, "Nebo error in %s: steps < 1", what);
   cudaStream_t s = (cudaStream_t)stream;
   const size_t cells = (size_t)T0->glob[0] * T0->glob[1] * T0->glob[2];
-  const size_t bytes = cells * sizeof(double);
+  const size_t ssize = forward_f32 ? sizeof(float) : sizeof(double);
+  const size_t stride = (cells + 63) / 64 * 64;  // state buffers 256-byte aligned
+  const size_t dbytes = 5 * cells * sizeof(double) + 256 * sizeof(double);
   int L = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)steps));
   if (L > steps) L = steps;  // a segment never holds more than the run's states
   if (checkpoint_every == NEBO_CHECKPOINT_AUTO) {
-    // every state kept (no recomputation) when steps + 7 fields fit in 80 % of the free memory
+    // every state kept (no recomputation) when all of them fit in 80 % of the free memory
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-      if (((size_t)steps + 7) * bytes <= free_b / 10 * 8) L = 1;
+      if (((size_t)steps + 4) * stride * ssize + dbytes <= free_b / 10 * 8) L = 1;
     } else {
       cudaGetLastError();
     }
   }
   const int nck = (steps + L - 1) / L;  // checkpoints at steps 0, L, 2L, ...
-  // device memory: nck checkpoints + L segment states + 2 adjoint states + 1 forward temp +
-  // 3 face-coefficient arrays, ~ (2 sqrt(N) + 6) fields
-  const size_t nbuf = (size_t)nck + (size_t)L + 6;
-  double* pool = nullptr;
+  // state buffers: nck checkpoints + L segment states + 2 forward temporaries (+ FP32 lambda),
+  // ~ 2 sqrt(N) fields; FP64: 2 adjoint states + 3 face-coefficient arrays
+  const size_t nstate = (size_t)nck + (size_t)L + 2 + (forward_f32 ? 1 : 0);
+  void* spool = nullptr;
+  double* dpool = nullptr;
   pool_retain();
-  NEBO_CUDA_TRY(cudaMallocAsync((void**)&pool, nbuf * bytes + 256 * sizeof(double), s));
-  const int rc = gradient_impl(pool, cells, nck, L, (int)nbuf, T0, lam, Ttarget, steps, dt, exact, gT0, glam, J,
-                               stream);
-  cudaFreeAsync(pool, s);
+  NEBO_CUDA_TRY(cudaMallocAsync(&spool, nstate * stride * ssize, s));
+  cudaError_t e = cudaMallocAsync((void**)&dpool, dbytes, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(spool, s);
+    return cuda_fail(e, what);
+  }
+  const int rc = forward_f32
+                     ? gradient_impl<float>((float*)spool, stride, dpool, cells, nck, L, T0, lam, Ttarget, steps, dt,
+                                            exact, gT0, glam, J, stream)
+                     : gradient_impl<double>((double*)spool, stride, dpool, cells, nck, L, T0, lam, Ttarget, steps, dt,
+                                             exact, gT0, glam, J, stream);
+  cudaFreeAsync(spool, s);
+  cudaFreeAsync(dpool, s);
   return rc;
 }
 }  // namespace
@@ -397,15 +442,16 @@ int gradient_entry(const nebo_field* T0, const nebo_field* lam, const nebo_field
 extern "C" int nebo_heat_gradient(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
                                   double dt, int checkpoint_every, const nebo_field* gT0, const nebo_field* glam,
                                   double* J, nebo_stream_t stream) {
-  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, true, gT0, glam, J, stream,
+  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, true, false, gT0, glam, J, stream,
                         "nebo_heat_gradient");
 }
 
 extern "C" int nebo_heat_gradient_ex(const nebo_field* T0, const nebo_field* lam, const nebo_field* Ttarget, int steps,
                                      double dt, int checkpoint_every, int products, const nebo_field* gT0,
                                      const nebo_field* glam, double* J, nebo_stream_t stream) {
-  if (products != NEBO_PRODUCTS_F64 && products != NEBO_PRODUCTS_F32)
+  const int prod = products & ~NEBO_FORWARD_F32;
+  if (prod != NEBO_PRODUCTS_F64 && prod != NEBO_PRODUCTS_F32)
     return fail(NEBO_ERR_INVALID, "Nebo error in nebo_heat_gradient_ex: products %d", products);
-  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, products == NEBO_PRODUCTS_F64, gT0, glam, J,
-                        stream, "nebo_heat_gradient_ex");
+  return gradient_entry(T0, lam, Ttarget, steps, dt, checkpoint_every, prod == NEBO_PRODUCTS_F64,
+                        (products & NEBO_FORWARD_F32) != 0, gT0, glam, J, stream, "nebo_heat_gradient_ex");
 }

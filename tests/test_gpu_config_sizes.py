@@ -11,7 +11,8 @@ the patch work list).  Each test states the error it measures; tolerances are in
 * 512 patches x 200 steps: FP64 bit-exact against the oracle on the smallest, the largest and
   two random patches; FP32 and FP32x2 states: per-patch relative max error against FP64;
 * adjoint 192^3 x 500 steps (sqrt(N) checkpoints): dJ/d(T0, lambda) against central finite
-  differences along 16 random joint directions (eps = 1e-6), to 1e-6 relative.
+  differences along 16 random joint directions (eps = 1e-6), to 1e-6 relative; the FP32-forward
+  gradient against the FP64 one (1e-4 relative max-norm).
 """
 import os
 
@@ -205,3 +206,10 @@ def test_adjoint_192_cubed_500_steps_vs_finite_differences():
         worst = max(worst, abs(fd - g) / abs(g))
         assert abs(fd - g) <= 1e-6 * abs(g), (fd, g)
     print(f"adjoint 192^3 x {steps}: J {J:.6e}, worst FD relative difference over 16 directions {worst:.2e}")
+    # the FP32-forward gradient (FP32 states and checkpoints, FP64 adjoint) against the FP64 one
+    J32, gT32, gl32 = N.heat_gradient(F(T0), F(lam), Tt, steps, dt, forward="f32")
+    e_T = float(np.abs(gT32.numpy()[I] - gT[I]).max() / np.abs(gT[I]).max())
+    e_l = float(np.abs(gl32.numpy()[I] - gl[I]).max() / np.abs(gl[I]).max())
+    print(f"adjoint 192^3 x {steps} FP32 forward: dJ/dT0 rel err {e_T:.2e}, dJ/dlambda rel err {e_l:.2e}, "
+          f"J rel diff {abs(J32 - J) / J:.2e}")
+    assert e_T <= 1e-4 and e_l <= 1e-4 and abs(J32 - J) <= 1e-4 * J
