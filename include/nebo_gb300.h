@@ -75,6 +75,9 @@ int nebo_memcpy_h2d(void* dst, const void* src, size_t bytes, nebo_stream_t stre
 int nebo_memcpy_d2h(void* dst, const void* src, size_t bytes, nebo_stream_t stream);
 int nebo_memcpy_d2d(void* dst, const void* src, size_t bytes, nebo_stream_t stream);
 int nebo_memset(void* dst, int byte, size_t bytes, nebo_stream_t stream);
+/* nebo_stream_sync also reports NEBO_ERR_TIMEOUT when a bounded device-side wait of a kernel
+ * (the FP32 heat step's bulk-copy barriers give up after about a second) gave up since the last
+ * report; the kernel's results are then not valid. */
 int nebo_stream_sync(nebo_stream_t stream);
 
 /* ------------------------------------------------------------------ ghost bookkeeping (host)

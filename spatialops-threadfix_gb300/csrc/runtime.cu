@@ -164,6 +164,11 @@ int nebo_memset(void* dst, int byte, size_t bytes, nebo_stream_t stream) {
 
 int nebo_stream_sync(nebo_stream_t stream) {
   NEBO_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  unsigned int timeouts = 0;
+  int rc = nebo::bulk_wait_timeouts(&timeouts);
+  if (rc) return rc;
+  if (timeouts)
+    return nebo::fail(NEBO_ERR_TIMEOUT, "Nebo error in nebo_stream_sync: %u bounded device wait(s) gave up", timeouts);
   return NEBO_OK;
 }
 

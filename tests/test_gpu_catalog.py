@@ -8,7 +8,9 @@ same C++ expression evaluated by the reference's serial Nebo and by one fused sm
 * error records (the reference's ghost-check exceptions) are identical;
 * with NEBO_EXACT_ARITHMETIC (no contraction), arithmetic and stencil results are bit-identical;
   libm functions (sin, exp, pow, ...) differ from the host's by a few ulp;
-* in the default build (FMA contraction allowed) every field is within 1e-13 relative max-norm.
+* in the default build (FMA contraction allowed; the 27-point box sums of the tiled lowering
+  split into line sums) every field is within 1e-13 relative max-norm, and max/min values of
+  such fields within that field's tolerance.
 """
 import os
 import subprocess
@@ -64,7 +66,11 @@ def _check(gold, got, exact):
         if g[0] == "value":
             ref, val = g[1], m[1]
             if "max" in name or "min" in name:
-                tol = 4 * EPS * abs(ref) if name == "red_expr_max" else 0.0
+                # exact: the same doubles; default build: the max/min of a field that may differ
+                # from the reference's by reassociation (the split box sum, FMA contraction)
+                tol = 4 * EPS * abs(ref) if (name == "red_expr_max" or not exact) else 0.0
+                if not exact and name.startswith("chain_deep"):
+                    tol = 1e-13 * float(np.abs(gold["chain_deep_filt"][2]).max())
             elif name.startswith("chain_deep"):
                 tol = 1e-13 * float(np.abs(gold["chain_deep_filt"][2]).sum())
             else:

@@ -43,16 +43,19 @@ def test_heat_fp64_bitexact_vs_oracle(n, steps):
     assert (_bits(T.numpy()) == _bits(ref)).all()
 
 
-@pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_heat_graph_equals_stream_launches(dtype):
-    # the graph runs first: the FP32 kernel's per-device set-up must happen outside the capture
-    lam, T0, dt = W.heat_inputs((40, 36, 20), cfl=0.15)
+# (40, 36, 20): the cp.async kernels; (48, 40, 20) in FP32: the bulk-copy kernel (rows in 8s)
+@pytest.mark.parametrize("dtype,n", [("f64", (40, 36, 20)), ("f32", (40, 36, 20)), ("f32", (48, 40, 20))])
+def test_heat_graph_equals_stream_launches(dtype, n):
+    # the graph runs first: the FP32 kernels' per-device set-up must work inside the capture
+    lam, T0, dt = W.heat_inputs(n, cfl=0.15)
     a = _run(lam, T0, 9, dt, use_graph=True, dtype=dtype).numpy()
     b = _run(lam, T0, 9, dt, use_graph=False, dtype=dtype).numpy()
     assert (a.view(np.uint8) == b.view(np.uint8)).all()
 
 
-@pytest.mark.parametrize("n", [(64, 48, 40), (37, 21, 19)])  # even pitch (8-byte copies), odd pitch
+# bulk-copied row slabs (rows in 8s, even pitch: full width 256, narrower with a ragged last z
+# chunk), 8-byte copies (odd row count), odd pitch
+@pytest.mark.parametrize("n", [(64, 48, 40), (256, 256, 24), (200, 96, 37), (64, 44, 40), (37, 21, 19)])
 def test_heat_fp32_error_vs_fp64_oracle(n):
     lam, T0, dt = W.heat_inputs(n, cfl=0.15)  # a stable step, so the error measure is meaningful
     ref = O.heat_run(lam, T0, n, 50, dt)
