@@ -147,13 +147,15 @@ def heat_label(n, dtype):
 
 
 def transport_label(n, dtype):
-    return (f"transport {n}^3 + 2 ghosts, Heun RK2 step, "
-            f"{'FP64' if dtype == 'f64' else 'FP32 storage, FP64 state accumulation'}")
+    prec = {"f64": "FP64", "f32": "FP32 storage, FP64 state accumulation"}.get(
+        dtype, "FP64, and FP32 storage with FP64 state accumulation")
+    return f"transport {n}^3 + 2 ghosts, Heun RK2 step, {prec}"
 
 
 def patches_label(count, cells, dtype):
+    prec = {"f64": "FP64", "f32": "FP32"}.get(dtype, "FP64 and FP32")
     return (f"{count} heat patches, edges ~ U{{16..96}}, 1 ghost, {cells / 1e6:.1f} M cells, "
-            f"{'FP64' if dtype == 'f64' else 'FP32'}; one persistent launch per step")
+            f"{prec}; one persistent launch per step")
 
 
 def adjoint_label(n, steps):
