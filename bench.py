@@ -566,8 +566,18 @@ def part_heat(N, bus, peak):
     ms, clocks = _timed(run, k, bus)
     cells = W.cells
     gbs = BYTES_PER_CELL["heat"] * cells / (ms * 1e-3) / 1e9
-    return {"workload": heat_label(256, "f64"), "gcell_upd_s": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
-            "steps": k, "alg_gbs": gbs, "hbm_frac": gbs / peak, "hbm_peak_gbs": peak, "clocks": clocks}
+    out = {"workload": heat_label(256, "f64"), "gcell_upd_s": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
+           "steps": k, "alg_gbs": gbs, "hbm_frac": gbs / peak, "hbm_peak_gbs": peak, "clocks": clocks}
+    # the same step with the flux arithmetic on the integer pipe (NEBO_HEAT_FIXED_POINT): k steps in
+    # one nebo_heat_run_ex call (two exponent reductions per call, a 4-byte reset per step)
+    runfix = lambda kk: N.heat_run_ex(W.T, W.Tt, W.L, kk, W.dt, mode="fixed")
+    runfix(3)
+    msf, clocksf = _timed(runfix, k, bus)
+    gbsf = BYTES_PER_CELL["heat"] * cells / (msf * 1e-3) / 1e9
+    out["fixed_point"] = {"gcell_upd_s": cells / (msf * 1e-3) / 1e9, "ms_per_step": msf, "steps": k,
+                          "alg_gbs": gbsf, "hbm_frac": gbsf / peak, "clocks": clocksf,
+                          "accuracy": "within 1e-13 relative max-norm of the bit-exact form (tests)"}
+    return out
 
 
 def part_patches(N, bus):

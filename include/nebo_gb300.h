@@ -149,6 +149,18 @@ int nebo_heat_step(const nebo_field* T, const nebo_field* Tout, const nebo_field
 int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
                   double dt, const double spacing[3], int use_graph, nebo_stream_t stream);
 
+/* nebo_heat_run with a choice of arithmetic (no graph):
+ *   NEBO_HEAT_EXACT        the bit-exact FP64 form of nebo_heat_step;
+ *   NEBO_HEAT_FIXED_POINT  FP64 storage; each face flux (lam_a + lam_b)(T_b - T_a) and the
+ *                          divergence exact in 64/128-bit integers at a per-field scale (the
+ *                          largest exponent of T, carried from step to step), then
+ *                          T' = fma(dt/2, RN(divergence), T): one FP64 operation per cell, the
+ *                          rest on the integer pipe.  Within a few 2^-60 of max|T| per step of
+ *                          the exact form (not bit-identical).  FP64, unit spacing. */
+enum { NEBO_HEAT_EXACT = 0, NEBO_HEAT_FIXED_POINT = 1 };
+int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
+                     double dt, const double spacing[3], int mode, nebo_stream_t stream);
+
 /* ------------------------------------------------------------------ deep fused chain
  *   out <<= cond(mask, 0.0)( Interp_{S->X}(Grad_{X->S}(Interp_{S->X}(a))) * exp(b) + sin(c) )
  *   filt <<= Filter_{X->X}(out)                       (27-point box, 1/27)

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("nebo_box_filter", _I, [_FP, _FP, _I, _P, _P]),
     ("nebo_cell_to_particle", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _FP, _P, _P]),
     ("nebo_particle_to_cell", _I, [ctypes.POINTER(ParticleMesh), _P, _P, _P, _P, ctypes.c_int64, _P, _FP, _P]),
+    ("nebo_heat_run_ex", _I, [_FP, _FP, _FP, _I, _D, ctypes.POINTER(_D), _I, _P]),
     ("nebo_stencil_transpose", _I, [_FP, ctypes.POINTER(ctypes.c_int32), _FP, ctypes.c_int32, _P, _P, _I, _P]),
     ("nebo_kernel_launch_count", ctypes.c_ulonglong, []),
     ("nebo_profile_enable", _I, [_I]),
@@ -278,6 +279,18 @@ def heat_run(T, Ttmp, lam, steps, dt, spacing=(1.0, 1.0, 1.0), use_graph=True, s
     sp = (ctypes.c_double * 3)(*spacing)
     _check(lib().nebo_heat_run(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt), sp,
                                int(use_graph), _stream(stream)))
+
+
+HEAT_MODES = {"exact": 0, "fixed": 1}  # NEBO_HEAT_EXACT, NEBO_HEAT_FIXED_POINT
+
+
+def heat_run_ex(T, Ttmp, lam, steps, dt, mode="fixed", spacing=(1.0, 1.0, 1.0), stream=None):
+    """nebo_heat_run_ex: `steps` FP64 Euler steps, the result in T; mode "fixed" computes the fluxes
+    on the integer pipe (within a few 2^-60 of max|T| per step of the exact form)."""
+    a, b, c = T.desc(), Ttmp.desc(), lam.desc()
+    sp = (ctypes.c_double * 3)(*spacing)
+    _check(lib().nebo_heat_run_ex(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt), sp,
+                                  HEAT_MODES[mode], _stream(stream)))
 
 
 def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None, reductions=None, interior=False):

@@ -25,6 +25,7 @@
 #include <tuple>
 
 #include "common.cuh"
+#include "fp64_int.cuh"
 
 namespace nebo {
 namespace {
@@ -479,6 +480,126 @@ __global__ void __launch_bounds__(QX* QY, 3) heat_step_f32x2_kernel(const float*
   cp_async_wait<0>();
 }
 
+// ------------------------------------------------------------------ FP64 step in fixed point
+// An FP64 heat step (FP64 storage, unit spacing) whose flux arithmetic runs on the integer pipe.
+// With |T| < 2^ET and |lambda| < 2^EL over the windows, every value becomes a signed 64-bit
+// integer in units of 2^(ET-61) (2^(EL-61)), truncated toward zero.  Per face the sum of the two
+// lambdas and the difference of the two T are exact in 64 bits, their product exact in 128 bits,
+// and the divergence S = (Fx+ - Fx-) + (Fy+ - Fy-) + (Fz+ - Fz-) exact in 128 bits; then
+//   T' = fma(dt/2, RN(S 2^(ET+EL-122)), T)
+// rounds twice.  The FP64 pipe runs one FMA per cell instead of the reference form's 16
+// operations.  Error: each truncation moves a value by less than 2^(ET-61), so a step's error is
+// within a few 2^-60 of max|T| (the reference's FP64 form: a few 2^-53 of each value), i.e. the
+// result agrees with the reference to well within 1e-13 relative max-norm, but not bit for bit.
+// ET comes from the previous step (each launch folds the largest biased exponent of what it
+// writes into an integer in device memory; the first from a reduction pass).  A field with an
+// infinity or a NaN, or too small for the scaled divergence to stay a normal double, runs the
+// same kernel in plain FP64.
+__device__ __forceinline__ long long to_fix61(double v, int E) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  const int sh = (e ? e : 1) - 1014 - E;  // v 2^(61-E) = m 2^sh; sh <= 8 when |v| < 2^E
+  const unsigned long long f = sh >= 0 ? m << sh : (sh > -64 ? m >> -sh : 0ull);
+  return (b >> 63) ? -(long long)f : (long long)f;
+}
+
+// largest biased exponent of n doubles -> atomicMax(*out)
+__global__ void max_biased_exp_kernel(const double* __restrict__ f, long n, int* __restrict__ out) {
+  int m = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    m = max(m, (int)(((unsigned long long)__double_as_longlong(f[i]) >> 52) & 0x7ff));
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+typedef __int128 i128;
+
+__global__ void __launch_bounds__(BX* BY) heat_step_fix_kernel(const double* __restrict__ tin, double* __restrict__ tout,
+                                                              const double* __restrict__ lam, int sy, long sz, int nx,
+                                                              int ny, int nz, int zchunk, const int* __restrict__ eT,
+                                                              const int* __restrict__ eL, int* __restrict__ eOut,
+                                                              double hdt) {
+  __shared__ i128 sfx[2][BY][BX + 1];
+  __shared__ i128 sfy[2][BY + 1][BX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk;
+  const int z1 = min(z0 + zchunk, nz);
+  const bool active = x < nx && y < ny;
+  const int xc = min(x, nx), yc = min(y, ny);
+  auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
+  const int bT = *eT, bL = *eL;  // largest biased exponents of T's and lambda's windows
+  const int ET = bT - 1022, EL = bL - 1022;
+  const int su = ET + EL - 122;  // S counts units of 2^su
+  // plain FP64 (the unit form of heat_step_kernel) for non-finite values or a scale whose
+  // results could leave the normal range
+  const bool plain = bT >= 2047 || bL >= 2047 || su < -900 || su > 900;
+  int emax = 0;
+  auto flux = [&](long a, long b) -> i128 {
+    const long long ls = to_fix61(__ldg(lam + a), EL) + to_fix61(__ldg(lam + b), EL);
+    const long long dt = to_fix61(__ldg(tin + b), ET) - to_fix61(__ldg(tin + a), ET);
+    return (i128)ls * (i128)dt;
+  };
+  auto fluxd = [&](long a, long b) -> double {
+    return __dmul_rn(__dadd_rn(__ldg(lam + a), __ldg(lam + b)), __dsub_rn(__ldg(tin + b), __ldg(tin + a)));
+  };
+  // the plain path keeps its doubles in the low word's bits of the same shared arrays
+  auto pack = [](double d) -> i128 { return (i128)(long long)__double_as_longlong(d); };
+  auto unpack = [](i128 v) -> double { return __longlong_as_double((long long)v); };
+  const long c0 = at(xc, yc, z0);
+  i128 fzlo = plain ? pack(fluxd(c0 - sz, c0)) : flux(c0 - sz, c0);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = z & 1;
+    const long c = at(xc, yc, z);
+    i128 fzhi, fx, fy;
+    if (plain) {
+      fzhi = pack(fluxd(c, c + sz));
+      fx = pack(fluxd(c - 1, c));
+      fy = pack(fluxd(c - sy, c));
+    } else {
+      fzhi = flux(c, c + sz);
+      fx = flux(c - 1, c);
+      fy = flux(c - sy, c);
+    }
+    sfx[buf][ty][tx] = fx;
+    sfy[buf][ty][tx] = fy;
+    if (ty == 0) {
+      const int yh = y0 + BY;  // +y halo face of column x
+      if (yh <= ny && x <= nx) {
+        const long a = at(xc, yh - 1, z), b = at(xc, yh, z);
+        sfy[buf][BY][tx] = plain ? pack(fluxd(a, b)) : flux(a, b);
+      }
+    } else if (ty == 1 && tx < BY) {
+      const int xh = x0 + BX, yr = y0 + tx;  // +x halo face of row yr
+      if (xh <= nx && yr < ny) {
+        const long a = at(xh - 1, yr, z), b = at(xh, yr, z);
+        sfx[buf][tx][BX] = plain ? pack(fluxd(a, b)) : flux(a, b);
+      }
+    }
+    __syncthreads();
+    if (active) {
+      const i128 fxhi = sfx[buf][ty][tx + 1], fyhi = sfy[buf][ty + 1][tx];
+      const double tc = __ldg(tin + c);
+      double v;
+      if (plain) {
+        const double sum = __dadd_rn(__dadd_rn(__dsub_rn(unpack(fxhi), unpack(fx)), __dsub_rn(unpack(fyhi), unpack(fy))),
+                                     __dsub_rn(unpack(fzhi), unpack(fzlo)));
+        v = __dadd_rn(tc, __dmul_rn(hdt, sum));
+      } else {
+        const i128 S = ((fxhi - fx) + (fyhi - fy)) + (fzhi - fzlo);
+        v = fma(hdt, fixmath::units_to_double0(S, su), tc);
+      }
+      store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
+      emax = max(emax, (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff));
+    }
+    fzlo = fzhi;
+  }
+  emax = __reduce_max_sync(0xffffffffu, emax);
+  if ((tx & 31) == 0) atomicMax(eOut, emax);
+}
+
 // ------------------------------------------------------------------ FP32 step on bulk-copied slabs
 // The FP32 fields' rows are full-width slabs in HBM: rows y0-1 .. y0+8 of a plane (10 x gx floats)
 // are one contiguous run that starts on an even row, so with an even row pitch it is 16-byte
@@ -762,6 +883,57 @@ extern "C" int nebo_heat_step(const nebo_field* T, const nebo_field* Tout, const
   int rc = check_heat(T, Tout, lam, "nebo_heat_step");
   if (rc) return rc;
   return heat_step_any(T, Tout, lam, dt, spacing ? spacing : unit, (cudaStream_t)stream);
+}
+
+extern "C" int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
+                                double dt, const double spacing[3], int mode, nebo_stream_t stream) {
+  const char* what = "nebo_heat_run_ex";
+  if (mode == NEBO_HEAT_EXACT) return nebo_heat_run(T, Ttmp, lam, steps, dt, spacing, 0, stream);
+  if (mode != NEBO_HEAT_FIXED_POINT) return fail(NEBO_ERR_INVALID, "Nebo error in %s: mode %d", what, mode);
+  int rc = check_heat(T, Ttmp, lam, what);
+  if (rc) return rc;
+  if (T->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: fixed point is FP64 only", what);
+  if (spacing && (spacing[0] != 1.0 || spacing[1] != 1.0 || spacing[2] != 1.0))
+    return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: fixed point takes unit spacing", what);
+  if (steps < 0) return fail(NEBO_ERR_INVALID, "Nebo error in %s: negative step count", what);
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((rc = fill_periodic_any(T, s))) return rc;
+  if (steps == 0) return NEBO_OK;
+  int n[3];
+  interior_extent(*T, n);
+  const size_t cells = (size_t)T->glob[0] * T->glob[1] * T->glob[2];
+  int* e = nullptr;  // [0], [1]: T's exponents, ping-pong; [2]: lambda's
+  pool_retain();
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&e, 3 * sizeof(int), s));
+  cudaError_t err = cudaMemsetAsync(e, 0, 3 * sizeof(int), s);
+  const int rblocks = num_sms() * 4;
+  {
+    LaunchScope ls("max_exponent", s);
+    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)T->data, (long)cells, e);
+    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)lam->data, (long)cells, e + 2);
+  }
+  if (err == cudaSuccess) err = cudaGetLastError();
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  static std::atomic<int> per_sm{0};
+  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * blocks_per_sm(heat_step_fix_kernel, BX * BY, per_sm),
+                                 n[2], 1, 8, 1);
+  const dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
+  for (int k = 0; k < steps && err == cudaSuccess; ++k) {
+    const nebo_field* a = (k & 1) ? Ttmp : T;
+    const nebo_field* b = (k & 1) ? T : Ttmp;
+    const View<double> va = make_view<double>(*a), vb = make_view<double>(*b), vl = make_view<double>(*lam);
+    err = cudaMemsetAsync(e + ((k + 1) & 1), 0, sizeof(int), s);
+    if (err != cudaSuccess) break;
+    LaunchScope ls("heat_step_fix", s);
+    heat_step_fix_kernel<<<grid, block, 0, s>>>(va.base, vb.base, vl.base, va.sy, va.sz, n[0], n[1], n[2], zchunk,
+                                                e + (k & 1), e + 2, e + ((k + 1) & 1), 0.5 * dt);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess && (steps & 1))
+    err = cudaMemcpyAsync(T->data, Ttmp->data, cells * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  cudaFreeAsync(e, s);
+  if (err != cudaSuccess) return cuda_fail(err, what);
+  return NEBO_OK;
 }
 
 extern "C" int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps, double dt,

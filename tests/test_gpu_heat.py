@@ -99,3 +99,46 @@ def test_heat_rejects_in_place_and_bad_ghosts():
     T2 = N.Field("SVol", (8, 8, 8), 2)
     with pytest.raises(RuntimeError, match="ghost"):
         N.heat_step(T2, N.Field("SVol", (8, 8, 8), 2), N.Field("SVol", (8, 8, 8), 2), 0.1)
+
+
+# ---------------------------------------------------------------------------- fixed-point FP64 mode
+def _run_ex(lam, T0, steps, dt, mode):
+    T = N.Field.from_numpy("SVol", T0, 1)
+    Tt = N.Field.from_numpy("SVol", np.zeros_like(T0), 1)
+    L = N.Field.from_numpy("SVol", lam, 1)
+    N.heat_run_ex(T, Tt, L, steps, dt, mode=mode)
+    return T.numpy()
+
+
+@pytest.mark.parametrize("n,steps", [((64, 64, 64), 100), ((37, 21, 19), 10), ((24, 20, 16), 50)])
+def test_heat_fixed_point_vs_oracle(n, steps):
+    """NEBO_HEAT_FIXED_POINT against the oracle's serial walk at the heat workload's own step
+    (dt = 0.2 / max lambda, above the stability limit: the values grow, the scale follows them):
+    within 1e-13 relative max-norm (test bound), ghost images included."""
+    lam, T0, dt = W.heat_inputs(n, sigma=min(n) / 4.0)
+    ref = O.heat_run(lam, T0, n, steps, dt)
+    got = _run_ex(lam, T0, steps, dt, "fixed")
+    err = float(np.abs(got - ref).max() / np.abs(ref).max())
+    print(f"fixed-point heat {n} x {steps}: rel max-norm err {err:.2e}")
+    assert err <= 1e-13, err
+
+
+def test_heat_fixed_point_256_against_exact_kernel():
+    n, steps = (256, 256, 256), 20
+    lam, T0, dt = W.heat_inputs(n)
+    a = _run_ex(lam, T0, steps, dt, "fixed")
+    b = _run_ex(lam, T0, steps, dt, "exact")  # bit-identical to the oracle (tests above)
+    err = float(np.abs(a - b).max() / np.abs(b).max())
+    print(f"fixed-point heat 256^3 x {steps}: rel max-norm err vs the exact form {err:.2e}")
+    assert err <= 1e-13, err
+
+
+def test_heat_fixed_point_falls_back_to_fp64_on_non_finite_values():
+    """A NaN in T: the fixed-point mode runs the exact FP64 form, bit for bit."""
+    n, steps = (20, 16, 12), 4
+    lam, T0, dt = W.heat_inputs(n)
+    T0 = T0.copy()
+    T0[5, 6, 7] = np.nan
+    a = _run_ex(lam, T0, steps, dt, "fixed")
+    b = _run_ex(lam, T0, steps, dt, "exact")
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
