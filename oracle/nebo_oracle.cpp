@@ -503,16 +503,41 @@ void orc_mask_from_points(uint32_t* bits, const int32_t glob[3], const int32_t o
   }
 }
 
-void orc_fill_periodic(double* f, const int32_t n[3], int32_t g) {
-  const int gx = n[0] + 2 * g, gy = n[1] + 2 * g;
-  for (int z = -g; z < n[2] + g; ++z)
-    for (int y = -g; y < n[1] + g; ++y)
-      for (int x = -g; x < n[0] + g; ++x) {
-        if (x >= 0 && x < n[0] && y >= 0 && y < n[1] && z >= 0 && z < n[2]) continue;
-        f[(x + g) + gx * ((y + g) + gy * (z + g))] =
-            f[(wrap(x, n[0]) + g) + gx * ((wrap(y, n[1]) + g) + gy * (wrap(z, n[2]) + g))];
+// Every ghost cell takes its wrapped interior image.  Rows are visited once: a ghost row copies
+// from its source row, an interior row only its ghost columns.  Sources are interior cells,
+// which no iteration writes, so the rows may run on several threads in any order.
+static void fill_periodic_threads(double* f, const int32_t n[3], int32_t g, int threads) {
+  const int gx = n[0] + 2 * g, gy = n[1] + 2 * g, gz = n[2] + 2 * g;
+#pragma omp parallel for num_threads(threads > 1 ? threads : 1) schedule(static)
+  for (int zz = 0; zz < gz; ++zz) {
+    const int z = zz - g;
+    const bool zin = z >= 0 && z < n[2];
+    const long szz = wrap(z, n[2]) + g;
+    for (int yy = 0; yy < gy; ++yy) {
+      const int y = yy - g;
+      double* row = f + (long)gx * (yy + (long)gy * zz);
+      const double* src = f + (long)gx * ((wrap(y, n[1]) + g) + (long)gy * szz);
+      if (zin && y >= 0 && y < n[1]) {
+        for (int x = -g; x < 0; ++x) row[x + g] = src[wrap(x, n[0]) + g];
+        for (int x = n[0]; x < n[0] + g; ++x) row[x + g] = src[wrap(x, n[0]) + g];
+      } else {
+        for (int x = -g; x < n[0] + g; ++x) row[x + g] = src[wrap(x, n[0]) + g];
       }
+    }
+  }
 }
+
+static void copy_threads(double* dst, const double* src, size_t n, int threads) {
+  const long chunk = 1 << 16;
+  const long nchunks = (long)((n + chunk - 1) / chunk);
+#pragma omp parallel for num_threads(threads > 1 ? threads : 1) schedule(static)
+  for (long c = 0; c < nchunks; ++c) {
+    const size_t lo = (size_t)c * chunk, hi = lo + chunk < n ? lo + chunk : n;
+    std::memcpy(dst + lo, src + lo, (hi - lo) * sizeof(double));
+  }
+}
+
+void orc_fill_periodic(double* f, const int32_t n[3], int32_t g) { fill_periodic_threads(f, n, g, 1); }
 
 double orc_reduce_field(const double* f, const int32_t glob[3], int32_t g, int op, int interior) {
   const int lo = interior ? g : 0;
@@ -546,12 +571,14 @@ void orc_heat_run(double* T, double* Ttmp, const double* lam, const int32_t n[3]
   const double c0 = -1.0 / 1.0, c1 = 1.0 / 1.0, h0 = 0.5, h1 = 0.5;
   double* cur = T;
   double* nxt = Ttmp;
-  std::vector<double> lamf((size_t)gx * gy * (n[2] + 2));
-  std::memcpy(lamf.data(), lam, lamf.size() * sizeof(double));
-  orc_fill_periodic(lamf.data(), n, 1);
-  const double* L = lamf.data();
+  // uninitialised: the threads' copy touches the pages first
+  const size_t npts = (size_t)gx * gy * (n[2] + 2);
+  std::unique_ptr<double[]> lamf(new double[npts]);
+  copy_threads(lamf.get(), lam, npts, threads);
+  fill_periodic_threads(lamf.get(), n, 1, threads);
+  const double* L = lamf.get();
   for (int s = 0; s < steps; ++s) {
-    orc_fill_periodic(cur, n, 1);
+    fill_periodic_threads(cur, n, 1, threads);
 #pragma omp parallel for num_threads(threads > 1 ? threads : 1) schedule(static)
     for (int z = 0; z < n[2]; ++z)
       for (int y = 0; y < n[1]; ++y)
@@ -568,8 +595,8 @@ void orc_heat_run(double* T, double* Ttmp, const double* lam, const int32_t n[3]
         }
     std::swap(cur, nxt);
   }
-  orc_fill_periodic(cur, n, 1);
-  if (cur != T) std::memcpy(T, cur, sizeof(double) * (size_t)gx * gy * (n[2] + 2));
+  fill_periodic_threads(cur, n, 1, threads);
+  if (cur != T) copy_threads(T, cur, (size_t)gx * gy * (n[2] + 2), threads);
 }
 
 // Deep fused chain (one ghost layer, no BC):
@@ -584,6 +611,7 @@ void orc_deep_run(const double* a, const double* b, const double* c, const uint3
   const long N = (long)gx * gy * gz;
   const long sy = gx, sz = (long)gx * gy;
   const double g0 = -1.0 / dx, g1 = 1.0 / dx;
+#pragma omp parallel for num_threads(threads > 1 ? threads : 1) schedule(static)
   for (long i = 0; i < N; ++i) { out[i] = 0.0; filt[i] = 0.0; }
 #pragma omp parallel for num_threads(threads > 1 ? threads : 1) schedule(static)
   for (int z = -1; z < n[2] + 1; ++z)

@@ -33,6 +33,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <typeinfo>
 #include <vector>
 
@@ -71,6 +72,14 @@ static void load(F& f, const std::vector<double>& v) {
 }
 
 // ----------------------------------------------------------------------------- heat
+// With NEBO_REF_TIMING set, the wall time of a driver's `<<=` evaluations goes to stderr (it is
+// not a record: the golden vectors do not change).
+static void report_seconds(const char* what, std::chrono::steady_clock::time_point t0) {
+  if (!std::getenv("NEBO_REF_TIMING")) return;
+  const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::fprintf(stderr, "seconds %s %.6f\n", what, s);
+}
+
 static int run_heat(int argc, char** argv) {
   if (argc < 10) return 1;
   int n[3] = {std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4])};
@@ -99,11 +108,13 @@ static int run_heat(int argc, char** argv) {
   SVolField* cur = &T0;
   SVolField* nxt = &T1;
   Out o(argv[9]);
+  const auto t0 = std::chrono::steady_clock::now();
   for (int s = 0; s < steps; ++s) {
     fill_periodic(*cur, n, 1);
     *nxt <<= *cur + dt * (dx(ix(lam) * gx(*cur)) + dy(iy(lam) * gy(*cur)) + dz(iz(lam) * gz(*cur)));
     std::swap(cur, nxt);
   }
+  report_seconds("heat", t0);
   fill_periodic(*cur, n, 1);
   dump(o, "T", *cur);
   o.value("sum", nebo_sum(*cur));
@@ -139,10 +150,12 @@ static int run_deep(int argc, char** argv) {
   const GX2S& gx2s = *opdb.retrieve_operator<GX2S>();
   const Box& box = *opdb.retrieve_operator<Box>();
   Out o(argv[9]);
+  const auto t0 = std::chrono::steady_clock::now();
   out <<= 0.0;
   out <<= cond(mask, 0.0)(is2x(gx2s(is2x(a))) * exp(b) + sin(c));
   filt <<= 0.0;
   filt <<= box(out);
+  report_seconds("deep", t0);
   dump(o, "out", out);
   dump(o, "filt", filt);
   o.value("sum", nebo_sum(filt));
@@ -243,6 +256,15 @@ int main(int argc, char** argv) {
   }
   const std::string cmd = argv[1];
   int rc = 1;
+#ifdef ENABLE_THREADS
+  // the Threading build's pool (spatialops/Threading.h:17-19): NEBO_THREADS threads, else one per
+  // host core
+  {
+    const char* nt = std::getenv("NEBO_THREADS");
+    const int n = nt ? std::atoi(nt) : (int)std::thread::hardware_concurrency();
+    Threading::setup(n > 0 ? n : 1);
+  }
+#endif
   if (cmd == "catalog" && argc >= 4) {
     const int id = std::atoi(argv[2]);
     Out o(argv[3]);

@@ -606,18 +606,15 @@ __global__ void __launch_bounds__(BX* BY) heat_step_fix_kernel(const double* __r
 // aligned and a multiple of 16 bytes long: one cp.async.bulk per plane and field moves it into
 // shared memory, issued by one thread and tracked by an mbarrier (no per-thread copy
 // instructions, no per-thread waits on copy groups).  A block of 256 threads owns 8 full rows
-// and marches a chunk of z planes through a ring of BK_NS stages: at
+// (one x column per thread) and marches a chunk of z planes through a ring of BK_NS stages: at
 // plane z it computes from the stages of planes z and z+1 (the z face below is carried in a
-// register) while the copies of planes z+2 .. z+3 are in flight.  512 threads: two groups of 256
-// columns, four rows each (32 warps per SM at two blocks).  Same per-cell arithmetic as the
+// register) while the copies of planes z+2 .. z+4 are in flight.  Same per-cell arithmetic as the
 // other FP32 kernels.  Every wait is bounded (about a second of clock cycles); a wait that gives
 // up is counted in g_bulk_timeouts, which nebo_stream_sync reports as NEBO_ERR_TIMEOUT.
 constexpr int BK_RY = 8;              // interior rows per block
 constexpr int BK_ROWS = BK_RY + 2;    // rows per stage (one halo row on each side)
-constexpr int BK_NS = 4;              // stages
-constexpr int BK_COLS = 256;          // x columns per block: nx <= 256
-constexpr int BK_RPT = 4;             // rows per thread: two groups of 256 threads
-constexpr int BK_THREADS = BK_COLS * (BK_RY / BK_RPT);
+constexpr int BK_NS = 5;              // stages
+constexpr int BK_THREADS = 256;       // one x column per thread: nx <= 256
 
 __device__ unsigned int g_bulk_timeouts;
 
@@ -683,24 +680,23 @@ __global__ void __launch_bounds__(BK_THREADS, 2) heat_step_f32_bulk_kernel(const
   };
   if (tid == 0)
     for (int q = 0; q < BK_NS; ++q) issue(q);
-  const int x = tid % BK_COLS, col = x + 1;
-  const int rg = (tid / BK_COLS) * BK_RPT;  // the thread's first row in the block
+  const int x = tid, col = tid + 1;
   const bool active = x < nx;
   const bool xedge = x == 0 || x == nx - 1;
   bool ok = mbar_wait(bar0, 0) & mbar_wait(bar0 + 8, 0);
-  float fz[BK_RPT];
+  float fz[BK_RY];
   {
     const float* Tm = sb;       // stage 0: plane z0 - 1
     const float* Lm = sb + sf;
     const float* Tc = sb + 2 * sf;  // stage 1: plane z0
     const float* Lc = sb + 3 * sf;
 #pragma unroll
-    for (int r = 0; r < BK_RPT; ++r) {
-      const int i = (rg + r + 1) * gx + col;
+    for (int r = 0; r < BK_RY; ++r) {
+      const int i = (r + 1) * gx + col;
       fz[r] = active ? (Lm[i] + Lc[i]) * (Tc[i] - Tm[i]) : 0.0f;
     }
   }
-  float* out = tout + (long)x + (long)gx * (y0 + rg) + sz * z0;
+  float* out = tout + (long)x + (long)gx * y0 + sz * z0;
 #pragma unroll 1
   for (int z = z0; z < z1; ++z) {
     const int q = z - z0 + 1;  // centre plane
@@ -717,12 +713,11 @@ __global__ void __launch_bounds__(BK_THREADS, 2) heat_step_f32_bulk_kernel(const
     const float* Ln = Tn + sf;
     if (active) {
       const bool xzedge = xedge || z == 0 || z == nz - 1;
-      const int i0 = (rg + 1) * gx + col;
-      float t = Tc[i0], l = Lc[i0];
-      float fyl = (Lc[i0 - gx] + l) * (t - Tc[i0 - gx]);
+      float t = Tc[gx + col], l = Lc[gx + col];
+      float fyl = (Lc[col] + l) * (t - Tc[col]);
 #pragma unroll
-      for (int r = 0; r < BK_RPT; ++r) {
-        const int i = i0 + r * gx;
+      for (int r = 0; r < BK_RY; ++r) {
+        const int i = (r + 1) * gx + col;
         const float tu = Tc[i + gx], lu = Lc[i + gx];
         const float fxl = (Lc[i - 1] + l) * (t - Tc[i - 1]);
         const float fxh = (l + Lc[i + 1]) * (Tc[i + 1] - t);
@@ -730,8 +725,9 @@ __global__ void __launch_bounds__(BK_THREADS, 2) heat_step_f32_bulk_kernel(const
         const float fzh = (l + Ln[i]) * (Tn[i] - t);
         const float v = t + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fz[r]);
         out[(long)gx * r] = v;
-        const int y = y0 + rg + r;
-        if (xzedge || y == 0 || y == ny - 1) store_images_only(tout, gx, sz, x, y, z, nx, ny, nz, v);
+        const int y = y0 + r;
+        if (xzedge || (r == 0 && y == 0) || (r == BK_RY - 1 && y == ny - 1))
+          store_images_only(tout, gx, sz, x, y, z, nx, ny, nz, v);
         fz[r] = fzh;
         fyl = fyh;
         t = tu;
@@ -786,9 +782,8 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     // bulk-copied slabs: rows of 16-byte aligned windows with an even pitch, 8 rows per block
     const int gx = Tf->glob[0], gy = Tf->glob[1];
     const size_t bk_smem = (size_t)BK_NS * 2 * BK_ROWS * gx * sizeof(float) + BK_NS * sizeof(uint64_t);
-    const bool bulk = n[0] <= BK_COLS && n[1] % BK_RY == 0 && gx % 2 == 0 && gy % 2 == 0 &&
+    const bool bulk = n[0] <= BK_THREADS && n[1] % BK_RY == 0 && gx % 2 == 0 && gy % 2 == 0 &&
                       (uintptr_t)Tf->data % 16 == 0 && (uintptr_t)Lf->data % 16 == 0 && bk_smem <= 113 * 1024;
-    static_assert(BK_RY % BK_RPT == 0, "rows split evenly between the thread groups");
     if (bulk) {
       // (per device and cheap: set on every launch)
       NEBO_CUDA_TRY(cudaFuncSetAttribute(heat_step_f32_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
