@@ -739,6 +739,123 @@ __global__ void __launch_bounds__(BK_THREADS, 2) heat_step_f32_bulk_kernel(const
   if (!ok) atomicAdd(&g_bulk_timeouts, 1u);
 }
 
+// The same slabs and ring with packed pairs: a thread owns the x-adjacent cells (x, x+1), x even,
+// in four rows (two groups of 128 pair columns cover the block's 8 rows).  The aligned 8-byte
+// pairs (x-1, x) and (x+1, x+2) of a stage row bring both cells and their x neighbours; every
+// face flux and the update run as packed FP32x2 operations (the arithmetic of
+// heat_step_f32x2_kernel).  Even nx.
+constexpr int BP_PAIRS = 128;  // pair columns per block: nx <= 256
+constexpr int BP_RPT = 4;      // rows per thread
+constexpr int BP_THREADS = BP_PAIRS * (BK_RY / BP_RPT);
+static_assert(BK_RY % BP_RPT == 0, "the block's rows split evenly between the groups");
+
+__global__ void __launch_bounds__(BP_THREADS, 2) heat_step_f32_bulk2_kernel(const float* __restrict__ tin,
+                                                                           float* __restrict__ tout,
+                                                                           const float* __restrict__ lam, int gx,
+                                                                           long sz, int nx, int ny, int nz, int zchunk,
+                                                                           float w0, float w1, float w2) {
+  extern __shared__ __align__(128) unsigned char bk_smem[];
+  const int sf = BK_ROWS * gx;  // floats per stage and field
+  const uint32_t bytes = (uint32_t)sf * 4u;
+  const float* sb = reinterpret_cast<const float*>(bk_smem);
+  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(bk_smem);
+  const uint32_t bar0 = s0 + (uint32_t)(BK_NS * 2) * bytes;
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * BK_RY;
+  const int z0 = blockIdx.y * zchunk, z1 = min(z0 + zchunk, nz);
+  if (tid == 0) {
+    for (int st = 0; st < BK_NS; ++st) mbar_init(bar0 + 8 * st, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // plane q of the chunk is interior plane z0 - 1 + q, in stage q % BK_NS, phase (q / BK_NS) & 1
+  auto issue = [&](int q) {
+    if (z0 - 1 + q > z1) return;
+    const int st = q % BK_NS;
+    const uint32_t bar = bar0 + 8 * st;
+    const long off = (long)(z0 + q) * sz + (long)y0 * gx;
+    mbar_expect_tx(bar, 2 * bytes);
+    bulk_g2s(s0 + (uint32_t)(2 * st) * bytes, tin + off, bytes, bar);
+    bulk_g2s(s0 + (uint32_t)(2 * st + 1) * bytes, lam + off, bytes, bar);
+  };
+  if (tid == 0)
+    for (int q = 0; q < BK_NS; ++q) issue(q);
+  const int x = 2 * (tid % BP_PAIRS), g = x + 1;  // cells x, x+1 at glob columns g, g+1
+  const int rg = (tid / BP_PAIRS) * BP_RPT;       // the group's first row
+  const bool active = x < nx;
+  const bool xedge0 = x == 0, xedge1 = x + 1 == nx - 1;
+  auto pair = [](const float* row, int i) { return *reinterpret_cast<const float2*>(row + i); };
+  auto centre = [](float2 a, float2 b) { return make_float2(a.y, b.x); };
+  bool ok = mbar_wait(bar0, 0) & mbar_wait(bar0 + 8, 0);
+  float2 fz[BP_RPT];
+  {
+    const float* Tm = sb;  // stage 0: plane z0 - 1
+    const float* Lm = sb + sf;
+    const float* Tc = sb + 2 * sf;  // stage 1: plane z0
+    const float* Lc = sb + 3 * sf;
+#pragma unroll
+    for (int r = 0; r < BP_RPT; ++r) {
+      const int i = (rg + r + 1) * gx + g;
+      fz[r] = active ? pflux(centre(pair(Lm, i - 1), pair(Lm, i + 1)), centre(pair(Lc, i - 1), pair(Lc, i + 1)),
+                             centre(pair(Tm, i - 1), pair(Tm, i + 1)), centre(pair(Tc, i - 1), pair(Tc, i + 1)))
+                     : make_float2(0.f, 0.f);
+    }
+  }
+  const float2 W0 = make_float2(w0, w0), W1 = make_float2(w1, w1), W2 = make_float2(w2, w2);
+  float* out = tout + (long)x + (long)gx * (y0 + rg) + sz * z0;
+#pragma unroll 1
+  for (int z = z0; z < z1; ++z) {
+    const int q = z - z0 + 1;  // centre plane
+    __syncthreads();           // plane q-1's stage is no longer read
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(q - 1 + BK_NS);
+    }
+    ok &= mbar_wait(bar0 + 8 * ((q + 1) % BK_NS), ((q + 1) / BK_NS) & 1);
+    const float* Tc = sb + 2 * (q % BK_NS) * sf;
+    const float* Lc = Tc + sf;
+    const float* Tn = sb + 2 * ((q + 1) % BK_NS) * sf;
+    const float* Ln = Tn + sf;
+    if (active) {
+      const bool zedge = z == 0 || z == nz - 1;
+      const int i0 = (rg + 1) * gx + g;
+      float2 aT = pair(Tc, i0 - 1), bT = pair(Tc, i0 + 1), aL = pair(Lc, i0 - 1), bL = pair(Lc, i0 + 1);
+      float2 fyl = pflux(centre(pair(Lc, i0 - gx - 1), pair(Lc, i0 - gx + 1)), centre(aL, bL),
+                         centre(pair(Tc, i0 - gx - 1), pair(Tc, i0 - gx + 1)), centre(aT, bT));
+#pragma unroll
+      for (int r = 0; r < BP_RPT; ++r) {
+        const int i = i0 + r * gx;
+        const float2 uaT = pair(Tc, i + gx - 1), ubT = pair(Tc, i + gx + 1);
+        const float2 uaL = pair(Lc, i + gx - 1), ubL = pair(Lc, i + gx + 1);
+        const float2 tc = centre(aT, bT), lc = centre(aL, bL);
+        const float2 fxl = pflux(aL, lc, aT, tc);  // faces x-1/2 of both cells
+        const float2 fxh = pflux(lc, bL, tc, bT);  // faces x+1/2
+        const float2 fyh = pflux(lc, centre(uaL, ubL), tc, centre(uaT, ubT));
+        const float2 fzh = pflux(lc, centre(pair(Ln, i - 1), pair(Ln, i + 1)), tc,
+                                 centre(pair(Tn, i - 1), pair(Tn, i + 1)));
+        float2 v = __ffma2_rn(W0, psub(fxh, fxl), tc);
+        v = __ffma2_rn(W1, psub(fyh, fyl), v);
+        v = __ffma2_rn(W2, psub(fzh, fz[r]), v);
+        float* o = out + (long)gx * r;
+        o[0] = v.x;
+        o[1] = v.y;
+        const int y = y0 + rg + r;
+        const bool yzedge = zedge || y == 0 || y == ny - 1;
+        if (xedge0 || yzedge) store_images_only(tout, gx, sz, x, y, z, nx, ny, nz, v.x);
+        if (xedge1 || yzedge) store_images_only(tout, gx, sz, x + 1, y, z, nx, ny, nz, v.y);
+        fz[r] = fzh;
+        fyl = fyh;
+        aT = uaT;
+        bT = ubT;
+        aL = uaL;
+        bL = ubL;
+      }
+    }
+    out += sz;
+  }
+  if (!ok) atomicAdd(&g_bulk_timeouts, 1u);
+}
+
 int check_heat(const nebo_field* T, const nebo_field* To, const nebo_field* L, const char* what) {
   int rc;
   if ((rc = check_field(T, what)) || (rc = check_field(To, what)) || (rc = check_field(L, what))) return rc;
@@ -785,13 +902,14 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     const bool bulk = n[0] <= BK_THREADS && n[1] % BK_RY == 0 && gx % 2 == 0 && gy % 2 == 0 &&
                       (uintptr_t)Tf->data % 16 == 0 && (uintptr_t)Lf->data % 16 == 0 && bk_smem <= 113 * 1024;
     if (bulk) {
-      // (per device and cheap: set on every launch)
-      NEBO_CUDA_TRY(cudaFuncSetAttribute(heat_step_f32_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         113 * 1024));
+      // packed pairs for even nx (same threads per block); (per device and cheap: the attribute
+      // is set on every launch)
+      const bool pairs = n[0] % 2 == 0;
+      auto kern = pairs ? heat_step_f32_bulk2_kernel : heat_step_f32_bulk_kernel;
+      static_assert(BP_THREADS == BK_THREADS, "both slab kernels take the same launch");
+      NEBO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 113 * 1024));
       int bps = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, heat_step_f32_bulk_kernel, BK_THREADS, bk_smem) !=
-              cudaSuccess ||
-          bps < 1) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, BK_THREADS, bk_smem) != cudaSuccess || bps < 1) {
         cudaGetLastError();
         bps = 1;
       }
@@ -800,7 +918,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
       const int ch = max(1, min(num_sms() * bps / yb, n[2]));
       const int zc = (n[2] + ch - 1) / ch;
       LaunchScope ls("heat_step_f32", s);
-      heat_step_f32_bulk_kernel<<<dim3(yb, (n[2] + zc - 1) / zc), BK_THREADS, bk_smem, s>>>(
+      kern<<<dim3(yb, (n[2] + zc - 1) / zc), BK_THREADS, bk_smem, s>>>(
           (const float*)Tf->data, vout.base, (const float*)Lf->data, gx, vin.sz, n[0], n[1], n[2], zc, p.w[0], p.w[1],
           p.w[2]);
       NEBO_LAUNCH_CHECK("nebo_heat_step");
