@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "fp64_int.cuh"
+#include "bulk.cuh"
 
 namespace nebo {
 namespace {
@@ -606,150 +607,28 @@ __global__ void __launch_bounds__(BX* BY) heat_step_fix_kernel(const double* __r
 // aligned and a multiple of 16 bytes long: one cp.async.bulk per plane and field moves it into
 // shared memory, issued by one thread and tracked by an mbarrier (no per-thread copy
 // instructions, no per-thread waits on copy groups).  A block of 256 threads owns 8 full rows
-// (one x column per thread) and marches a chunk of z planes through a ring of BK_NS stages: at
-// plane z it computes from the stages of planes z and z+1 (the z face below is carried in a
-// register) while the copies of planes z+2 .. z+4 are in flight.  Same per-cell arithmetic as the
-// other FP32 kernels.  Every wait is bounded (about a second of clock cycles); a wait that gives
+// and marches a chunk of z planes through a ring of BK_NS stages: at plane z it computes from the
+// stages of planes z and z+1 (the z face below is carried in a register) while the copy of plane
+// z+2 is in flight.  Every wait is bounded (about a second of clock cycles); a wait that gives
 // up is counted in g_bulk_timeouts, which nebo_stream_sync reports as NEBO_ERR_TIMEOUT.
 constexpr int BK_RY = 8;              // interior rows per block
 constexpr int BK_ROWS = BK_RY + 2;    // rows per stage (one halo row on each side)
-constexpr int BK_NS = 5;              // stages
-constexpr int BK_THREADS = 256;       // one x column per thread: nx <= 256
+constexpr int BK_NS = 3;              // stages (three blocks per SM)
 
 __device__ unsigned int g_bulk_timeouts;
 
-__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// false when the phase has not completed within 2^31 clock cycles (about a second)
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1LL << 31)) return false;
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
-// tin, lam: glob element (0,0,0) of the windows (16-byte aligned); tout: the interior origin.
-__global__ void __launch_bounds__(BK_THREADS, 2) heat_step_f32_bulk_kernel(const float* __restrict__ tin,
-                                                                          float* __restrict__ tout,
-                                                                          const float* __restrict__ lam, int gx,
-                                                                          long sz, int nx, int ny, int nz, int zchunk,
-                                                                          float w0, float w1, float w2) {
-  extern __shared__ __align__(128) unsigned char bk_smem[];
-  const int sf = BK_ROWS * gx;  // floats per stage and field
-  const uint32_t bytes = (uint32_t)sf * 4u;
-  const float* sb = reinterpret_cast<const float*>(bk_smem);
-  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(bk_smem);
-  const uint32_t bar0 = s0 + (uint32_t)(BK_NS * 2) * bytes;
-  const int tid = threadIdx.x;
-  const int y0 = blockIdx.x * BK_RY;                 // interior row of the block's first row
-  const int z0 = blockIdx.y * zchunk, z1 = min(z0 + zchunk, nz);
-  if (tid == 0) {
-    for (int st = 0; st < BK_NS; ++st) mbar_init(bar0 + 8 * st, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  // plane q of the chunk is interior plane z0 - 1 + q, in stage q % BK_NS, phase (q / BK_NS) & 1;
-  // its rows y0-1 .. y0+8 start at glob row y0 of glob plane z0 + q
-  auto issue = [&](int q) {
-    if (z0 - 1 + q > z1) return;  // the +z neighbour of the chunk's last plane is the last one read
-    const int st = q % BK_NS;
-    const uint32_t bar = bar0 + 8 * st;
-    const long off = (long)(z0 + q) * sz + (long)y0 * gx;
-    mbar_expect_tx(bar, 2 * bytes);
-    bulk_g2s(s0 + (uint32_t)(2 * st) * bytes, tin + off, bytes, bar);
-    bulk_g2s(s0 + (uint32_t)(2 * st + 1) * bytes, lam + off, bytes, bar);
-  };
-  if (tid == 0)
-    for (int q = 0; q < BK_NS; ++q) issue(q);
-  const int x = tid, col = tid + 1;
-  const bool active = x < nx;
-  const bool xedge = x == 0 || x == nx - 1;
-  bool ok = mbar_wait(bar0, 0) & mbar_wait(bar0 + 8, 0);
-  float fz[BK_RY];
-  {
-    const float* Tm = sb;       // stage 0: plane z0 - 1
-    const float* Lm = sb + sf;
-    const float* Tc = sb + 2 * sf;  // stage 1: plane z0
-    const float* Lc = sb + 3 * sf;
-#pragma unroll
-    for (int r = 0; r < BK_RY; ++r) {
-      const int i = (r + 1) * gx + col;
-      fz[r] = active ? (Lm[i] + Lc[i]) * (Tc[i] - Tm[i]) : 0.0f;
-    }
-  }
-  float* out = tout + (long)x + (long)gx * y0 + sz * z0;
-#pragma unroll 1
-  for (int z = z0; z < z1; ++z) {
-    const int q = z - z0 + 1;  // centre plane
-    __syncthreads();           // plane q-1's stage is no longer read
-    if (tid == 0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(q - 1 + BK_NS);
-    }
-    ok &= mbar_wait(bar0 + 8 * ((q + 1) % BK_NS), ((q + 1) / BK_NS) & 1);
-    const int sc = q % BK_NS, sn = (q + 1) % BK_NS;
-    const float* Tc = sb + 2 * sc * sf;
-    const float* Lc = Tc + sf;
-    const float* Tn = sb + 2 * sn * sf;
-    const float* Ln = Tn + sf;
-    if (active) {
-      const bool xzedge = xedge || z == 0 || z == nz - 1;
-      float t = Tc[gx + col], l = Lc[gx + col];
-      float fyl = (Lc[col] + l) * (t - Tc[col]);
-#pragma unroll
-      for (int r = 0; r < BK_RY; ++r) {
-        const int i = (r + 1) * gx + col;
-        const float tu = Tc[i + gx], lu = Lc[i + gx];
-        const float fxl = (Lc[i - 1] + l) * (t - Tc[i - 1]);
-        const float fxh = (l + Lc[i + 1]) * (Tc[i + 1] - t);
-        const float fyh = (l + lu) * (tu - t);
-        const float fzh = (l + Ln[i]) * (Tn[i] - t);
-        const float v = t + w0 * (fxh - fxl) + w1 * (fyh - fyl) + w2 * (fzh - fz[r]);
-        out[(long)gx * r] = v;
-        const int y = y0 + r;
-        if (xzedge || (r == 0 && y == 0) || (r == BK_RY - 1 && y == ny - 1))
-          store_images_only(tout, gx, sz, x, y, z, nx, ny, nz, v);
-        fz[r] = fzh;
-        fyl = fyh;
-        t = tu;
-        l = lu;
-      }
-    }
-    out += sz;
-  }
-  if (!ok) atomicAdd(&g_bulk_timeouts, 1u);
-}
-
-// The same slabs and ring with packed pairs: a thread owns the x-adjacent cells (x, x+1), x even,
-// in four rows (two groups of 128 pair columns cover the block's 8 rows).  The aligned 8-byte
-// pairs (x-1, x) and (x+1, x+2) of a stage row bring both cells and their x neighbours; every
-// face flux and the update run as packed FP32x2 operations (the arithmetic of
-// heat_step_f32x2_kernel).  Even nx.
+// Packed pairs: a thread owns the x-adjacent cells (x, x+1), x even, in four rows (two groups of
+// 128 pair columns cover the block's 8 rows).  The aligned 8-byte pairs (x-1, x) and (x+1, x+2)
+// of a stage row bring both cells and their x neighbours; every face flux and the update run as
+// packed FP32x2 operations (the arithmetic of heat_step_f32x2_kernel).  The slab layout needs an
+// even row pitch, so nx is even.  Three stages (62 KB) and at most 80 registers let three blocks
+// (24 warps) share an SM.
 constexpr int BP_PAIRS = 128;  // pair columns per block: nx <= 256
 constexpr int BP_RPT = 4;      // rows per thread
 constexpr int BP_THREADS = BP_PAIRS * (BK_RY / BP_RPT);
 static_assert(BK_RY % BP_RPT == 0, "the block's rows split evenly between the groups");
 
-__global__ void __launch_bounds__(BP_THREADS, 2) heat_step_f32_bulk2_kernel(const float* __restrict__ tin,
+__global__ void __launch_bounds__(BP_THREADS, 3) heat_step_f32_bulk2_kernel(const float* __restrict__ tin,
                                                                            float* __restrict__ tout,
                                                                            const float* __restrict__ lam, int gx,
                                                                            long sz, int nx, int ny, int nz, int zchunk,
@@ -899,17 +778,14 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     // bulk-copied slabs: rows of 16-byte aligned windows with an even pitch, 8 rows per block
     const int gx = Tf->glob[0], gy = Tf->glob[1];
     const size_t bk_smem = (size_t)BK_NS * 2 * BK_ROWS * gx * sizeof(float) + BK_NS * sizeof(uint64_t);
-    const bool bulk = n[0] <= BK_THREADS && n[1] % BK_RY == 0 && gx % 2 == 0 && gy % 2 == 0 &&
+    const bool bulk = n[0] <= 2 * BP_PAIRS && n[1] % BK_RY == 0 && gx % 2 == 0 && gy % 2 == 0 &&
                       (uintptr_t)Tf->data % 16 == 0 && (uintptr_t)Lf->data % 16 == 0 && bk_smem <= 113 * 1024;
     if (bulk) {
-      // packed pairs for even nx (same threads per block); (per device and cheap: the attribute
-      // is set on every launch)
-      const bool pairs = n[0] % 2 == 0;
-      auto kern = pairs ? heat_step_f32_bulk2_kernel : heat_step_f32_bulk_kernel;
-      static_assert(BP_THREADS == BK_THREADS, "both slab kernels take the same launch");
+      // (per device and cheap: the attribute is set on every launch)
+      auto kern = heat_step_f32_bulk2_kernel;
       NEBO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 113 * 1024));
       int bps = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, BK_THREADS, bk_smem) != cudaSuccess || bps < 1) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, BP_THREADS, bk_smem) != cudaSuccess || bps < 1) {
         cudaGetLastError();
         bps = 1;
       }
@@ -918,7 +794,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
       const int ch = max(1, min(num_sms() * bps / yb, n[2]));
       const int zc = (n[2] + ch - 1) / ch;
       LaunchScope ls("heat_step_f32", s);
-      kern<<<dim3(yb, (n[2] + zc - 1) / zc), BK_THREADS, bk_smem, s>>>(
+      kern<<<dim3(yb, (n[2] + zc - 1) / zc), BP_THREADS, bk_smem, s>>>(
           (const float*)Tf->data, vout.base, (const float*)Lf->data, gx, vin.sz, n[0], n[1], n[2], zc, p.w[0], p.w[1],
           p.w[2]);
       NEBO_LAUNCH_CHECK("nebo_heat_step");

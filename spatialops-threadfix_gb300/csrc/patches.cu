@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "bulk.cuh"
 
 struct nebo_patchset;  // opaque handle of the C ABI
 
@@ -36,8 +37,10 @@ constexpr int PT_MAX_TX = 64;   // TY = 4
 
 struct PatchDev {
   long long offset;  // element offset of the patch window in the arena
+  long long off32;   // FP32 slab layout: element offset of the patch's interior (0,0,0)
   int nx, ny, nz;
   int log2tx;        // tile x extent = 1 << log2tx
+  int pitch32;       // FP32 slab layout: row pitch in floats (nx rounded up to a multiple of 4)
   double lam2;       // 2*lambda
   double hdt;        // dt/2
 };
@@ -352,7 +355,169 @@ __global__ void __launch_bounds__(PT_THREADS, 2) patches_f32_strip_kernel(const 
   }
 }
 
+// FP32 mode on bulk-copied slabs (every patch with nx <= PB_CELLS).  The FP32 working state
+// holds each patch's interior only, rows padded to a multiple of 4 floats (16 bytes) and each
+// patch 256-byte aligned, so every row starts on a 16-byte boundary.  An item is a strip of R
+// full rows of one patch over a z range (R nx <= 1024, the rows split evenly between the strips).
+// Per plane three cp.async.bulk copies fill a stage of the ring: the row below the strip, its R
+// rows (one contiguous run) and the row above, the two halo rows and the halo planes taken from
+// their periodic sources (rows ny-1 / 0, planes nz-1 / 0); the x halo is the row's own other end.
+// One thread arms the stage's mbarrier and issues the copies; the 256 threads own the strip's
+// cells linearly (4 each) and compute what patches_f32_strip_kernel computes, with the same
+// operations.  No ghost cells exist in this layout: nebo_patchset_sync writes whole FP64 windows.
+constexpr int PB_CELLS = 1024;                 // cells per strip plane
+constexpr int PB_CPT = PB_CELLS / PT_THREADS;  // cells per thread
+constexpr int PB_NS = 5;                       // stages
+
+__host__ __device__ __forceinline__ int strip_rows_bulk(int nx, int ny) {
+  const int rmax = PB_CELLS / nx > 0 ? PB_CELLS / nx : 1;
+  const int nstrips = (ny + rmax - 1) / rmax;
+  return (ny + nstrips - 1) / nstrips;
+}
+
+__device__ unsigned int g_patch_bulk_timeouts;
+
+// stage_floats: floats per stage (a multiple of 4, at least (R + 2) pitch32 for every item)
+__global__ void __launch_bounds__(PT_THREADS) patches_f32_bulk_kernel(const PatchDev* __restrict__ patches,
+                                                                      const WorkItem* __restrict__ items, int nitems,
+                                                                      const float* __restrict__ src,
+                                                                      float* __restrict__ dst, int stage_floats) {
+  extern __shared__ __align__(128) unsigned char pb_smem[];
+  const float* ring = reinterpret_cast<const float*>(pb_smem);
+  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(pb_smem);
+  const uint32_t bar0 = ring0 + (uint32_t)(PB_NS * stage_floats) * 4u;
+  const int tid = threadIdx.x;
+  bool ok = true;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const WorkItem it = items[w];
+    const PatchDev P = patches[it.patch];
+    const int nx = P.nx, ny = P.ny, nz = P.nz, pitch = P.pitch32;
+    const int R = min(strip_rows_bulk(nx, ny), ny - it.y0);
+    const long sz = (long)ny * pitch;
+    const float* base = src + P.off32;
+    float* obase = dst + P.off32;
+    const float l2 = (float)P.lam2, hdt = (float)P.hdt;
+    const int z0 = it.z0, z1 = it.z1;
+    const uint32_t rowb = (uint32_t)pitch * 4u;
+    const int ylo = it.y0 == 0 ? ny - 1 : it.y0 - 1;
+    const int yhi = it.y0 + R == ny ? 0 : it.y0 + R;
+    if (tid == 0) {
+      for (int st = 0; st < PB_NS; ++st) mbar_init(bar0 + 8 * st, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // plane q of the item is z0 - 1 + q (periodic), in stage q % PB_NS, phase (q / PB_NS) & 1
+    auto issue = [&](int q) {
+      const int p = z0 - 1 + q;
+      if (p > z1) return;  // the last plane read is z1 (the +z neighbour of the item's last plane)
+      const int pw = p < 0 ? p + nz : (p >= nz ? p - nz : p);
+      const int st = q % PB_NS;
+      const uint32_t bar = bar0 + 8 * st;
+      const uint32_t so = ring0 + (uint32_t)(st * stage_floats) * 4u;
+      const float* pl = base + (long)pw * sz;
+      mbar_expect_tx(bar, (uint32_t)(R + 2) * rowb);
+      bulk_g2s(so, pl + (long)ylo * pitch, rowb, bar);
+      bulk_g2s(so + rowb, pl + (long)it.y0 * pitch, (uint32_t)R * rowb, bar);
+      bulk_g2s(so + (uint32_t)(R + 1) * rowb, pl + (long)yhi * pitch, rowb, bar);
+    };
+    if (tid == 0)
+      for (int q = 0; q < PB_NS; ++q) issue(q);
+    // this thread's cells: strip cell tid + 256 j -> stage indices (centre, x-1, x+1, wrapped
+    // within the row) and the output offset in a plane; bit j of `live`: the cell exists
+    int si[PB_CPT], sl[PB_CPT], sr[PB_CPT], go[PB_CPT];
+    unsigned live = 0;
+#pragma unroll
+    for (int j = 0; j < PB_CPT; ++j) {
+      const int c = tid + j * PT_THREADS;
+      const bool in = c < R * nx;
+      const int r = in ? c / nx : 0, col = in ? c - r * nx : 0;
+      if (in) live |= 1u << j;
+      si[j] = (r + 1) * pitch + col;
+      sl[j] = (r + 1) * pitch + (col == 0 ? nx - 1 : col - 1);
+      sr[j] = (r + 1) * pitch + (col == nx - 1 ? 0 : col + 1);
+      go[j] = (it.y0 + r) * pitch + col;
+    }
+    ok &= mbar_wait(bar0, 0) & mbar_wait(bar0 + 8, 0);
+    float t[PB_CPT], fz[PB_CPT];
+#pragma unroll
+    for (int j = 0; j < PB_CPT; ++j) {
+      t[j] = ring[stage_floats + si[j]];
+      fz[j] = l2 * (t[j] - ring[si[j]]);
+    }
+    for (int z = z0; z < z1; ++z) {
+      const int q = z - z0 + 1;  // centre plane
+      __syncthreads();           // plane q-1's stage is no longer read
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(q - 1 + PB_NS);
+      }
+      ok &= mbar_wait(bar0 + 8 * ((q + 1) % PB_NS), ((q + 1) / PB_NS) & 1);
+      const float* T0 = ring + (q % PB_NS) * stage_floats;
+      const float* Tn = ring + ((q + 1) % PB_NS) * stage_floats;
+      float* op = obase + (long)z * sz;
+#pragma unroll
+      for (int j = 0; j < PB_CPT; ++j) {
+        const int c = si[j];
+        const float tc = t[j], tn = Tn[c];
+        const float fxl = l2 * (tc - T0[sl[j]]);
+        const float fxh = l2 * (T0[sr[j]] - tc);
+        const float fyl = l2 * (tc - T0[c - pitch]);
+        const float fyh = l2 * (T0[c + pitch] - tc);
+        const float fzh = l2 * (tn - tc);
+        const float sflux = ((fxh - fxl) + (fyh - fyl)) + (fzh - fz[j]);
+        if ((live >> j) & 1u) op[go[j]] = tc + hdt * sflux;
+        fz[j] = fzh;
+        t[j] = tn;
+      }
+    }
+    __syncthreads();  // every copy of the item has landed and been read: the barriers start over
+    if (tid == 0)
+      for (int st = 0; st < PB_NS; ++st) mbar_inval(bar0 + 8 * st);
+  }
+  if (!ok) atomicAdd(&g_patch_bulk_timeouts, 1u);
+}
+
+// FP64 windows -> FP32 slab layout (interiors only) and back (whole windows: each cell of a
+// window takes its periodic interior source, so the ghosts are filled in the same pass).
+__global__ void patches_pack_f32_kernel(const PatchDev* __restrict__ patches, int npatch,
+                                        const double* __restrict__ a64, float* __restrict__ a32) {
+  for (int p = blockIdx.y; p < npatch; p += gridDim.y) {
+    const PatchDev P = patches[p];
+    const int nx = P.nx, ny = P.ny, gx = nx + 2, gy = ny + 2;
+    const long n = (long)nx * ny * P.nz;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+      a32[P.off32 + ((long)z * ny + y) * P.pitch32 + x] =
+          (float)a64[P.offset + (x + 1) + (long)gx * ((y + 1) + (long)gy * (z + 1))];
+    }
+  }
+}
+__global__ void patches_unpack_f32_kernel(const PatchDev* __restrict__ patches, int npatch,
+                                          const float* __restrict__ a32, double* __restrict__ a64) {
+  for (int p = blockIdx.y; p < npatch; p += gridDim.y) {
+    const PatchDev P = patches[p];
+    const int nx = P.nx, ny = P.ny, nz = P.nz, gx = nx + 2, gy = ny + 2;
+    const long n = (long)gx * gy * (nz + 2);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      int x = (int)(i % gx) - 1, y = (int)((i / gx) % gy) - 1, z = (int)(i / ((long)gx * gy)) - 1;
+      x = x < 0 ? nx - 1 : (x == nx ? 0 : x);
+      y = y < 0 ? ny - 1 : (y == ny ? 0 : y);
+      z = z < 0 ? nz - 1 : (z == nz ? 0 : z);
+      a64[P.offset + i] = (double)a32[P.off32 + ((long)z * ny + y) * P.pitch32 + x];
+    }
+  }
+}
+
 }  // namespace
+
+// Bounded waits of the patch kernels that gave up since the last call (cleared by the read).
+int patch_wait_timeouts(unsigned int* count) {
+  unsigned int v = 0, zero = 0;
+  NEBO_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_patch_bulk_timeouts, sizeof(v)));
+  if (v) NEBO_CUDA_TRY(cudaMemcpyToSymbol(g_patch_bulk_timeouts, &zero, sizeof(zero)));
+  *count = v;
+  return NEBO_OK;
+}
 
 struct PatchSet {
   int npatch = 0;
@@ -371,6 +536,11 @@ struct PatchSet {
   int zchunk = 16;
   int grid = 0;
   int grid32 = 0;  // resident blocks of the FP32 ring kernel (one full wave)
+  bool bulk32 = false;            // FP32 mode on the slab layout (every nx <= PB_CELLS)
+  std::vector<long long> off32;   // slab layout: interior offsets
+  std::vector<int> pitch32;       // slab layout: row pitches
+  long long total32 = 0;          // slab layout: floats per arena
+  int stage32 = 0;                // slab layout: floats per ring stage
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, parity) -> graph
   ~PatchSet() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -393,7 +563,14 @@ std::vector<WorkItem> build_items(const PatchSet& ps, const std::vector<int>& wh
     const int nx = ps.shape[3 * p], ny = ps.shape[3 * p + 1], nz = ps.shape[3 * p + 2];
     // FP32: row strips (strip_shape); otherwise tiles, one row per thread row
     int TX = 1 << ps.log2tx[p], TY = PT_THREADS / TX;
-    if (ps.dtype == NEBO_F32) strip_shape(nx, ny, TX, TY);
+    if (ps.dtype == NEBO_F32) {
+      if (ps.bulk32) {
+        TX = nx;
+        TY = strip_rows_bulk(nx, ny);
+      } else {
+        strip_shape(nx, ny, TX, TY);
+      }
+    }
     for (int z0 = 0; z0 < nz; z0 += zchunk)
       for (int y0 = 0; y0 < ny; y0 += TY)
         for (int x0 = 0; x0 < nx; x0 += TX) items.push_back(WorkItem{p, x0, y0, z0, std::min(z0 + zchunk, nz)});
@@ -407,6 +584,8 @@ int upload_tables(PatchSet& ps, const std::vector<WorkItem>& items, cudaStream_t
   std::vector<PatchDev> pd(ps.npatch);
   for (int p = 0; p < ps.npatch; ++p) {
     pd[p].offset = ps.offset[p];
+    pd[p].off32 = ps.bulk32 ? ps.off32[p] : 0;
+    pd[p].pitch32 = ps.bulk32 ? ps.pitch32[p] : 0;
     pd[p].nx = ps.shape[3 * p];
     pd[p].ny = ps.shape[3 * p + 1];
     pd[p].nz = ps.shape[3 * p + 2];
@@ -435,6 +614,10 @@ int launch_step(const PatchSet& ps, const WorkItem* items, int nitems, int parit
     patches_step_kernel<PMODE_F64><<<grid, PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
                                                                (const double*)ps.arena[parity],
                                                                (double*)ps.arena[parity ^ 1]);
+  else if (ps.dtype == NEBO_F32 && ps.bulk32)
+    patches_f32_bulk_kernel<<<std::min(nitems, ps.grid32), PT_THREADS,
+                              (size_t)PB_NS * ps.stage32 * sizeof(float) + PB_NS * sizeof(uint64_t), s>>>(
+        ps.d_patches, items, nitems, ps.arena32[parity], ps.arena32[parity ^ 1], ps.stage32);
   else if (ps.dtype == NEBO_F32)
     patches_f32_strip_kernel<<<std::min(nitems, ps.grid32), PT_THREADS, 0, s>>>(ps.d_patches, items, nitems,
                                                                                ps.arena32[parity],
@@ -515,7 +698,29 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
     if (e == cudaSuccess) e = cudaMemset(ps->arena2[1], 0, b2);
   }
   if (dtype == NEBO_F32) {
-    const size_t b32 = (size_t)off * sizeof(float);
+    // the slab layout when every row fits a strip: interiors only, rows padded to 16 bytes
+    ps->bulk32 = true;
+    for (int p = 0; p < npatch; ++p) ps->bulk32 = ps->bulk32 && shapes[3 * p] <= PB_CELLS;
+    if (ps->bulk32) {
+      ps->off32.resize(npatch);
+      ps->pitch32.resize(npatch);
+      long long o32 = 0;
+      int stage = 0;
+      for (int p = 0; p < npatch; ++p) {
+        const int nx = shapes[3 * p], ny = shapes[3 * p + 1], nz = shapes[3 * p + 2];
+        const int pitch = (nx + 3) / 4 * 4;
+        ps->off32[p] = o32;
+        ps->pitch32[p] = pitch;
+        o32 += (long long)pitch * ny * nz;
+        o32 = (o32 + 63) & ~63LL;  // 256-byte aligned patches
+        stage = std::max(stage, (strip_rows_bulk(nx, ny) + 2) * pitch);
+      }
+      ps->total32 = o32;
+      ps->stage32 = stage;
+    }
+  }
+  if (dtype == NEBO_F32) {
+    const size_t b32 = (size_t)(ps->bulk32 ? ps->total32 : off) * sizeof(float);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena32[0], b32);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ps->arena32[1], b32);
     if (e == cudaSuccess) e = cudaMemset(ps->arena32[0], 0, b32);
@@ -529,9 +734,28 @@ extern "C" int nebo_patchset_create(nebo_patchset** out, int npatch, const int32
   if (dtype == NEBO_F32) {
     ps->zchunk = 1 << 30;  // FP32 items cover the patch's whole z extent
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, patches_f32_strip_kernel, PT_THREADS, 0) != cudaSuccess ||
-        per_sm < 1)
+    if (ps->bulk32) {
+      const size_t smem = (size_t)PB_NS * ps->stage32 * sizeof(float) + PB_NS * sizeof(uint64_t);
+      if (smem > 48 * 1024 &&
+          cudaFuncSetAttribute(patches_f32_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        delete ps;
+        return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in nebo_patchset_create: FP32 strips need %zu bytes of "
+                                          "shared memory", smem);
+      }
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, patches_f32_bulk_kernel, PT_THREADS, smem) !=
+              cudaSuccess ||
+          per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+      }
+    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, patches_f32_strip_kernel, PT_THREADS, 0) !=
+                   cudaSuccess ||
+               per_sm < 1) {
+      cudaGetLastError();
       per_sm = 1;
+    }
     ps->grid32 = num_sms() * per_sm;
   }
   std::vector<int> all(npatch);
@@ -582,7 +806,12 @@ extern "C" int nebo_patchset_fill_ghosts(const nebo_patchset* ps, int which, neb
     int rc = nebo::fill_periodic_any(&f, (cudaStream_t)stream);
     if (rc) return rc;
   }
-  if (ps->dtype == NEBO_F32) {  // the FP32 working state
+  if (ps->dtype == NEBO_F32 && ps->bulk32) {  // the FP32 working state, slab layout
+    LaunchScope ls("patches_pack_f32", (cudaStream_t)stream);
+    patches_pack_f32_kernel<<<dim3(8, std::min(ps->npatch, 4096)), 256, 0, (cudaStream_t)stream>>>(
+        ps->d_patches, ps->npatch, (const double*)ps->arena[which], ps->arena32[which]);
+    NEBO_LAUNCH_CHECK("nebo_patchset_fill_ghosts");
+  } else if (ps->dtype == NEBO_F32) {  // the FP32 working state
     LaunchScope ls("patches_cast_f32", (cudaStream_t)stream);
     patches_cast_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>((const double*)ps->arena[which],
                                                                          ps->arena32[which], (size_t)ps->total);
@@ -605,6 +834,9 @@ extern "C" int nebo_patchset_sync(const nebo_patchset* ps, int which, nebo_strea
   if (ps->dtype == NEBO_F32X2)
     patches_join_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena2[which], (double*)ps->arena[which],
                                                                          (size_t)ps->total);
+  else if (ps->bulk32)
+    patches_unpack_f32_kernel<<<dim3(8, std::min(ps->npatch, 4096)), 256, 0, (cudaStream_t)stream>>>(
+        ps->d_patches, ps->npatch, ps->arena32[which], (double*)ps->arena[which]);
   else
     patches_widen_kernel<<<num_sms() * 8, 256, 0, (cudaStream_t)stream>>>(ps->arena32[which],
                                                                           (double*)ps->arena[which], (size_t)ps->total);
@@ -713,7 +945,7 @@ extern "C" int nebo_patchset_autotune(nebo_patchset* ps, nebo_stream_t stream, i
 // After the steps of a run: the FP32 strip kernel writes no ghost cells, so the arena that holds
 // the result gets them here (one launch).
 int finish_run(const PatchSet& ps, int which, cudaStream_t s) {
-  if (ps.dtype != NEBO_F32) return NEBO_OK;
+  if (ps.dtype != NEBO_F32 || ps.bulk32) return NEBO_OK;  // the slab layout has no ghost cells
   LaunchScope ls("patches_ghosts_f32", s);
   patches_ghosts_f32_kernel<<<std::min(ps.npatch, num_sms() * 8), 256, 0, s>>>(ps.d_patches, ps.npatch,
                                                                                ps.arena32[which]);

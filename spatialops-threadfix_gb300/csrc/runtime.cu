@@ -164,9 +164,11 @@ int nebo_memset(void* dst, int byte, size_t bytes, nebo_stream_t stream) {
 
 int nebo_stream_sync(nebo_stream_t stream) {
   NEBO_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-  unsigned int timeouts = 0;
+  unsigned int timeouts = 0, more = 0;
   int rc = nebo::bulk_wait_timeouts(&timeouts);
   if (rc) return rc;
+  if ((rc = nebo::patch_wait_timeouts(&more))) return rc;
+  timeouts += more;
   if (timeouts)
     return nebo::fail(NEBO_ERR_TIMEOUT, "Nebo error in nebo_stream_sync: %u bounded device wait(s) gave up", timeouts);
   return NEBO_OK;

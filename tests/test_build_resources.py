@@ -14,8 +14,7 @@ HOT = {
     "deep_out_kernel": 48,           # 5 blocks of 256 threads per SM
     "box_filter_kernel": 64,         # 4 blocks of 256
     "heat_step_f32x2_kernel": 80,    # 3 blocks of 256
-    "heat_step_f32_bulk_kernel": 128,  # 2 blocks of 256 (shared memory allows two)
-    "heat_step_f32_bulk2_kernel": 128,
+    "heat_step_f32_bulk2_kernel": 80,  # 3 blocks of 256
     "transport_stage_f32_pair_kernel": 96,
     "patches_f32_strip_kernel": 128,  # 2 blocks of 256
 }
