@@ -516,86 +516,118 @@ __global__ void max_biased_exp_kernel(const double* __restrict__ f, long n, int*
 
 typedef __int128 i128;
 
+// 64 x 64 -> 128-bit signed product (two 64-bit multiplies on the integer pipe)
+__device__ __forceinline__ i128 mul_wide(long long a, long long b) {
+  const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+  const long long hi = __mul64hi(a, b);
+  return (i128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
+// One plane of a 32 x 8 tile at a time: every value of the tile and of its one-cell x / y halo
+// is converted once and staged in shared memory (two buffers, one barrier per plane); each thread
+// then forms its cell's six face fluxes from the staged values (an in-plane face is formed by both
+// of its cells with the same exact integer operations, so both see the same value), carrying the
+// z faces and the next plane's converted values in registers.  In the plain FP64 fallback the
+// same slots hold the doubles' bits and the fluxes are the exact form's.
 __global__ void __launch_bounds__(BX* BY) heat_step_fix_kernel(const double* __restrict__ tin, double* __restrict__ tout,
                                                               const double* __restrict__ lam, int sy, long sz, int nx,
                                                               int ny, int nz, int zchunk, const int* __restrict__ eT,
                                                               const int* __restrict__ eL, int* __restrict__ eOut,
                                                               double hdt) {
-  __shared__ i128 sfx[2][BY][BX + 1];
-  __shared__ i128 sfy[2][BY + 1][BX];
+  __shared__ long long cT[2][BY + 2][BX + 2];
+  __shared__ long long cL[2][BY + 2][BX + 2];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
   const int x = x0 + tx, y = y0 + ty;
   const int z0 = blockIdx.z * zchunk;
   const int z1 = min(z0 + zchunk, nz);
   const bool active = x < nx && y < ny;
+  // inactive threads convert the +ghost column/row, which exists, and write nothing
   const int xc = min(x, nx), yc = min(y, ny);
   auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
   const int bT = *eT, bL = *eL;  // largest biased exponents of T's and lambda's windows
   const int ET = bT - 1022, EL = bL - 1022;
   const int su = ET + EL - 122;  // S counts units of 2^su
-  // plain FP64 (the unit form of heat_step_kernel) for non-finite values or a scale whose
-  // results could leave the normal range
+  // plain FP64 (the exact unit form) for non-finite values or a scale whose results could leave
+  // the normal range
   const bool plain = bT >= 2047 || bL >= 2047 || su < -900 || su > 900;
-  int emax = 0;
-  auto flux = [&](long a, long b) -> i128 {
-    const long long ls = to_fix61(__ldg(lam + a), EL) + to_fix61(__ldg(lam + b), EL);
-    const long long dt = to_fix61(__ldg(tin + b), ET) - to_fix61(__ldg(tin + a), ET);
-    return (i128)ls * (i128)dt;
+  auto cvt = [&](double v, int E) -> long long { return plain ? (long long)__double_as_longlong(v) : to_fix61(v, E); };
+  auto asd = [](long long b) { return __longlong_as_double(b); };
+  // the tile's one-cell halo, staged by three warps per plane: warp 0 the row below (y0 - 1),
+  // warp 1 the row above (y0 + 8), lanes 0..15 of warp 2 the columns x0 - 1 and x0 + 32 of the
+  // 8 rows; coordinates clamped into the window (a clamped cell is never read by an active cell)
+  bool has_halo = false;
+  int hx = 0, hy = 0, hsx = 0, hsy = 0;
+  if (ty == 0) {
+    has_halo = true;
+    hx = xc;
+    hy = y0 - 1;
+    hsx = tx + 1;
+    hsy = 0;
+  } else if (ty == 1) {
+    has_halo = true;
+    hx = xc;
+    hy = min(y0 + BY, ny);
+    hsx = tx + 1;
+    hsy = BY + 1;
+  } else if (ty == 2 && tx < 2 * BY) {
+    has_halo = true;
+    const int r = tx % BY;
+    hx = tx < BY ? x0 - 1 : min(x0 + BX, nx);
+    hy = min(y0 + r, ny);
+    hsx = tx < BY ? 0 : BX + 1;
+    hsy = r + 1;
+  }
+  // face flux between staged/registered values (a low, b high)
+  auto flux = [&](long long la, long long lb, long long ta, long long tb) -> i128 {
+    if (plain) {
+      const double f = __dmul_rn(__dadd_rn(asd(la), asd(lb)), __dsub_rn(asd(tb), asd(ta)));
+      return (i128)(long long)__double_as_longlong(f);
+    }
+    return mul_wide(la + lb, tb - ta);
   };
-  auto fluxd = [&](long a, long b) -> double {
-    return __dmul_rn(__dadd_rn(__ldg(lam + a), __ldg(lam + b)), __dsub_rn(__ldg(tin + b), __ldg(tin + a)));
-  };
-  // the plain path keeps its doubles in the low word's bits of the same shared arrays
-  auto pack = [](double d) -> i128 { return (i128)(long long)__double_as_longlong(d); };
-  auto unpack = [](i128 v) -> double { return __longlong_as_double((long long)v); };
   const long c0 = at(xc, yc, z0);
-  i128 fzlo = plain ? pack(fluxd(c0 - sz, c0)) : flux(c0 - sz, c0);
+  long long tc = cvt(__ldg(tin + c0), ET), lc = cvt(__ldg(lam + c0), EL);
+  i128 fzlo = flux(cvt(__ldg(lam + c0 - sz), EL), lc, cvt(__ldg(tin + c0 - sz), ET), tc);
+  int emax = 0;
   for (int z = z0; z < z1; ++z) {
     const int buf = z & 1;
     const long c = at(xc, yc, z);
-    i128 fzhi, fx, fy;
-    if (plain) {
-      fzhi = pack(fluxd(c, c + sz));
-      fx = pack(fluxd(c - 1, c));
-      fy = pack(fluxd(c - sy, c));
-    } else {
-      fzhi = flux(c, c + sz);
-      fx = flux(c - 1, c);
-      fy = flux(c - sy, c);
+    cT[buf][ty + 1][tx + 1] = tc;
+    cL[buf][ty + 1][tx + 1] = lc;
+    if (has_halo) {
+      const long h = at(hx, hy, z);
+      cT[buf][hsy][hsx] = cvt(__ldg(tin + h), ET);
+      cL[buf][hsy][hsx] = cvt(__ldg(lam + h), EL);
     }
-    sfx[buf][ty][tx] = fx;
-    sfy[buf][ty][tx] = fy;
-    if (ty == 0) {
-      const int yh = y0 + BY;  // +y halo face of column x
-      if (yh <= ny && x <= nx) {
-        const long a = at(xc, yh - 1, z), b = at(xc, yh, z);
-        sfy[buf][BY][tx] = plain ? pack(fluxd(a, b)) : flux(a, b);
-      }
-    } else if (ty == 1 && tx < BY) {
-      const int xh = x0 + BX, yr = y0 + tx;  // +x halo face of row yr
-      if (xh <= nx && yr < ny) {
-        const long a = at(xh - 1, yr, z), b = at(xh, yr, z);
-        sfx[buf][tx][BX] = plain ? pack(fluxd(a, b)) : flux(a, b);
-      }
-    }
+    // the next plane of this cell (its z+1 face and next iteration's centre)
+    const long long tn = cvt(__ldg(tin + c + sz), ET), ln = cvt(__ldg(lam + c + sz), EL);
     __syncthreads();
+    const i128 fzhi = flux(lc, ln, tc, tn);
     if (active) {
-      const i128 fxhi = sfx[buf][ty][tx + 1], fyhi = sfy[buf][ty + 1][tx];
-      const double tc = __ldg(tin + c);
+      const long long tw = cT[buf][ty + 1][tx], te = cT[buf][ty + 1][tx + 2];
+      const long long ts = cT[buf][ty][tx + 1], tnn = cT[buf][ty + 2][tx + 1];
+      const long long lw = cL[buf][ty + 1][tx], le = cL[buf][ty + 1][tx + 2];
+      const long long ls = cL[buf][ty][tx + 1], lnn = cL[buf][ty + 2][tx + 1];
+      const i128 fx = flux(lw, lc, tw, tc), fxhi = flux(lc, le, tc, te);
+      const i128 fy = flux(ls, lc, ts, tc), fyhi = flux(lc, lnn, tc, tnn);
+      const double tcd = __ldg(tin + c);
       double v;
       if (plain) {
-        const double sum = __dadd_rn(__dadd_rn(__dsub_rn(unpack(fxhi), unpack(fx)), __dsub_rn(unpack(fyhi), unpack(fy))),
-                                     __dsub_rn(unpack(fzhi), unpack(fzlo)));
-        v = __dadd_rn(tc, __dmul_rn(hdt, sum));
+        auto d = [&](i128 f) { return __longlong_as_double((long long)f); };
+        const double sum = __dadd_rn(__dadd_rn(__dsub_rn(d(fxhi), d(fx)), __dsub_rn(d(fyhi), d(fy))),
+                                     __dsub_rn(d(fzhi), d(fzlo)));
+        v = __dadd_rn(tcd, __dmul_rn(hdt, sum));
       } else {
         const i128 S = ((fxhi - fx) + (fyhi - fy)) + (fzhi - fzlo);
-        v = fma(hdt, fixmath::units_to_double0(S, su), tc);
+        v = fma(hdt, fixmath::units_to_double0(S, su), tcd);
       }
       store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
       emax = max(emax, (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff));
     }
     fzlo = fzhi;
+    tc = tn;
+    lc = ln;
   }
   emax = __reduce_max_sync(0xffffffffu, emax);
   if ((tx & 31) == 0) atomicMax(eOut, emax);
