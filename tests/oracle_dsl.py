@@ -477,6 +477,23 @@ def deep_run(a, b, c, maskbits, n, dx=1.0, threads=1):
     return out, filt
 
 
+def deep_write_region(n, ghost=1):
+    """The write region of out <<= cond(mask, 0)(I(G(I(a))) * exp(b) + sin(c)) as write_limits
+    returns it, by the oracle's restatement of calculate_actual_ghost (host integer code; the
+    fields are zero-stride stand-ins, never read)."""
+    gs, gx = glob_dims("SVol", n, ghost, (0, 0, 0)), glob_dims("XVol", n, ghost, (0, 0, 0))
+    one = np.empty(1)
+    a = Field("SVol", np.lib.stride_tricks.as_strided(one, shape=gs[::-1], strides=(0, 0, 0)), ghost)
+    bx = np.lib.stride_tricks.as_strided(one, shape=gx[::-1], strides=(0, 0, 0))
+    b, c, out = Field("XVol", bx, ghost), Field("XVol", bx, ghost), Field("XVol", bx, ghost)
+    m = Mask("XVol", np.zeros(1, dtype=np.uint32), gx, ghost)
+    db = OpDB(n, n)
+    i_sx, g_xs = db.interp("SVol", "XVol"), db.grad("XVol", "SVol")
+    e = cond(m, 0.0, i_sx(g_xs(i_sx(a))) * exp(b) + sin(c))
+    lim, _ = write_limits(out, e, True)
+    return lim
+
+
 def transport_run(phi0, u, v, w, lam, n, steps, dt, nu, threads=1):
     phi = np.ascontiguousarray(phi0, dtype=np.float64).copy()
     p1 = np.zeros_like(phi)

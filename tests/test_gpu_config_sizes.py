@@ -33,23 +33,6 @@ def _rel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
-def _deep_write_region(n):
-    """The reference's write region of out <<= cond(mask, 0)(I(G(I(a))) * exp(b) + sin(c)),
-    computed by the oracle's restatement of calculate_actual_ghost (host integer code)."""
-    gs, gx = O.glob_dims("SVol", n, 1, (0, 0, 0)), O.glob_dims("XVol", n, 1, (0, 0, 0))
-    a = O.Field("SVol", np.empty((1, 1, 1)), 1)
-    a.data = np.lib.stride_tricks.as_strided(np.empty(1), shape=gs[::-1], strides=(0, 0, 0))
-    b = O.Field("XVol", np.lib.stride_tricks.as_strided(np.empty(1), shape=gx[::-1], strides=(0, 0, 0)), 1)
-    c = O.Field("XVol", b.data, 1)
-    out = O.Field("XVol", b.data, 1)
-    m = O.Mask("XVol", np.zeros(1, dtype=np.uint32), gx, 1)
-    db = O.OpDB(n, n)
-    i_sx, g_xs = db.interp("SVol", "XVol"), db.grad("XVol", "SVol")
-    e = O.cond(m, 0.0, i_sx(g_xs(i_sx(a))) * O.exp(b) + O.sin(c))
-    lim, _ = O.write_limits(out, e, True)
-    return lim
-
-
 def test_deep_chain_256_vs_oracle_with_written_cells():
     import torch
 
@@ -69,7 +52,7 @@ def test_deep_chain_256_vs_oracle_with_written_cells():
     words = N.mask_from_points(N.mask_words(out.glob), out.glob, 1, pts)
     N.deep_chain(A, B, C, words, out, filt)
     unwritten = out.numpy().view(np.uint64) == NAN_SENTINEL
-    lim = _deep_write_region(n)
+    lim = O.deep_write_region(n)
     want = np.ones(unwritten.shape, dtype=bool)
     want[lim[4] + 1:lim[5] + 1, lim[2] + 1:lim[3] + 1, lim[0] + 1:lim[1] + 1] = False
     assert np.array_equal(unwritten, want), f"written-cell set differs from the write region {lim}"

@@ -62,6 +62,40 @@ def test_deep_vs_oracle(n):
     assert _relerr(filt.numpy(), o_filt) <= TOL
 
 
+NAN_SENTINEL = np.uint64(0x7FF4DEAD00C0FFEE)  # a NaN payload no computed value carries
+
+
+@pytest.mark.parametrize("n", [(64, 64, 64), (45, 30, 17), (33, 5, 2), (130, 3, 9), (8, 70, 3)])
+def test_deep_written_cells_with_sentinel(n):
+    """out and filt pre-filled with a NaN payload: the cells still holding it are exactly those
+    outside the reference's write regions (calculate_actual_ghost through the oracle for out; the
+    interior for filt), so an extra or a missing write of any value fails."""
+    import torch
+
+    a, b, c, pts = W.deep_inputs(n)
+    A = N.Field.from_numpy("SVol", a, 1)
+    B = N.Field.from_numpy("XVol", b, 1)
+    C = N.Field.from_numpy("XVol", c, 1)
+    g = N.glob_dims("XVol", n, 1)
+
+    def sentinel_field():
+        t = torch.full((g[2], g[1], g[0]), int(NAN_SENTINEL.astype(np.int64)), dtype=torch.int64, device="cuda")
+        return N.Field("XVol", n, 1, tensor=t.view(torch.float64))
+
+    out, filt = sentinel_field(), sentinel_field()
+    words = N.mask_from_points(N.mask_words(out.glob), out.glob, 1, pts)
+    N.deep_chain(A, B, C, words, out, filt)
+    lim = O.deep_write_region(n)
+    want = np.ones((g[2], g[1], g[0]), dtype=bool)
+    want[lim[4] + 1:lim[5] + 1, lim[2] + 1:lim[3] + 1, lim[0] + 1:lim[1] + 1] = False
+    assert np.array_equal(out.numpy().view(np.uint64) == NAN_SENTINEL, want), (n, lim)
+    # the filter writes the interior only (cells next to out's unwritten planes read the payload
+    # and come out as quiet NaNs, never as the payload itself)
+    want_f = np.ones_like(want)
+    want_f[1:-1, 1:-1, 1:-1] = False
+    assert np.array_equal(filt.numpy().view(np.uint64) == NAN_SENTINEL, want_f), n
+
+
 @pytest.mark.parametrize("n,interior", [((64, 64, 64), False), ((45, 30, 17), False), ((45, 30, 17), True),
                                         ((33, 5, 2), False), ((130, 3, 9), True), ((8, 70, 3), False)])
 def test_fused_filter_reductions(n, interior):
