@@ -46,9 +46,10 @@ BYTES_PER_CELL = {  # algorithmic bytes per cell-update of the dominant kernel
     "heat32": 4 * 3,
     "patches": 8 * 2,    # T read, T' written (lambda is a scalar per patch)
     "patches32": 4 * 2,  # FP32 state read and written
-    # one RK stage: phi (stencil) + u,v,w,lambda read, state accumulation read/written
-    "transport": 8 * 5 + 8 + 8,            # FP64: phi, u, v, w, lam, acc read; out written
-    "transport32": 4 * 5 + 8 + 8 + 4,      # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
+    # one RK stage, averaged over the two: phi (stencil) + u,v,w,lambda read, state accumulation
+    # read/written; stage 2 also reads the step's start state (8 bytes, so 4 on average)
+    "transport": 8 * 5 + 8 + 8 + 4,        # FP64: phi, u, v, w, lam, acc read; out written
+    "transport32": 4 * 5 + 8 + 8 + 4 + 4,  # FP32 storage: 5 float reads, FP64 acc r/w, float copy written
     # one reverse step: T_k, A_{k+1}, lambda read, glam read and written, A_k written
     "adjoint": 8 * 6,
     # ParticleToCell fill, per particle: x, y, z, size and value read (its entries are not counted)

@@ -42,6 +42,8 @@ int check_field(const nebo_field* f, const char* what);
 int bulk_wait_timeouts(unsigned int* count);
 // The same for the patch kernels (patches.cu).
 int patch_wait_timeouts(unsigned int* count);
+// The same for the tensor-staged transport stage kernel (transport.cu).
+int transport_wait_timeouts(unsigned int* count);
 // Same shape, ghosts and dtype.
 int check_same_layout(const nebo_field* a, const nebo_field* b, const char* what);
 // Uniform periodic patch: equal ghosts g on all six faces, no BC cells, window == allocation.

@@ -169,6 +169,8 @@ int nebo_stream_sync(nebo_stream_t stream) {
   if (rc) return rc;
   if ((rc = nebo::patch_wait_timeouts(&more))) return rc;
   timeouts += more;
+  if ((rc = nebo::transport_wait_timeouts(&more))) return rc;
+  timeouts += more;
   if (timeouts)
     return nebo::fail(NEBO_ERR_TIMEOUT, "Nebo error in nebo_stream_sync: %u bounded device wait(s) gave up", timeouts);
   return NEBO_OK;

@@ -15,10 +15,18 @@
 // Each stage is ONE kernel: face fluxes computed once per face (low faces by each thread, high
 // faces through shared memory or carried in z), RK combination fused, periodic ghost images of
 // the stencil copy written in the same pass.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's driver entry point)
+
+#include "bulk.cuh"
 #include "common.cuh"
 #include "fp64_int.cuh"
 
 namespace nebo {
+
+// Bounded mbarrier waits of the tensor-staged FP32 stage kernel that gave up (read and cleared
+// by transport_wait_timeouts; nebo_stream_sync reports them).
+__device__ unsigned int g_transport_timeouts;
+
 namespace {
 
 constexpr int TX = 32;
@@ -305,7 +313,34 @@ __global__ void __launch_bounds__(TX* TY) transport_stage_f32_staged_kernel(TrAr
 // shared face x+1/2 is evaluated twice, identically); y and z faces take one packed flux each.
 // The RK combination, the FP64 state and the stencil copy with its images stay per cell.
 // Needs n even (even pitch) and 8-byte aligned field bases.
-constexpr int PTX = TX / 2;  // threads per tile row
+//
+// Two ways to stage the phi and lambda planes (template TMA):
+//   false: 8-byte cp.async copies by every thread, one commit group per plane;
+//   true:  one thread issues two 3-D tensor-tile loads per plane (cp.async.bulk.tensor, box
+//          36 x 12 x 1 floats at glob (x0, y0, z + G): the tile and its two-cell halo) into
+//          128-byte-aligned stages; each stage's mbarrier counts the 3456 bytes, and every
+//          thread waits on the phase of the newest plane it reads.  The tensor maps cover the
+//          whole windows, so the row pitch (n + 4) * 4 bytes must be a multiple of 16 (n a
+//          multiple of 4) and the window bases 16-byte aligned.  A tile reaching past the window
+//          (n not a multiple of 32 or 8) reads zeros there, which only idle lanes use.  Waits
+//          are bounded; one that gives up is counted in g_transport_timeouts.
+constexpr int PTX = TX / 2;   // threads per tile row
+constexpr int TSTRIDE = 448;  // floats per TMA stage: 36 x 12 = 432, padded to 128 bytes
+static_assert(SPW == 36 && SPH == 12 && TSTRIDE * 4 % 128 == 0 && TSTRIDE >= SPLANE, "TMA stage layout");
+constexpr uint32_t TMA_STAGE_BYTES = 2u * SPLANE * sizeof(float);  // phi and lambda boxes
+
+// The tensor maps of one stage launch: phi's stencil copy and lambda, each over its whole window.
+struct TrMaps {
+  CUtensorMap phi, lam;
+};
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
 
 __device__ __forceinline__ float2 tsub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 __device__ __forceinline__ float2 tld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
@@ -334,12 +369,15 @@ __device__ __forceinline__ void store_images2_pair(float* base, int sy, long sz,
   }
 }
 
-template <bool SECOND>
-__global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArgs<float> a, int zchunk) {
+template <bool SECOND, bool TMA>
+__global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArgs<float> a, int zchunk,
+                                                                           const __grid_constant__ TrMaps maps) {
   constexpr int NT = PTX * TY;
   constexpr int NCP = (2 * SUNITS + NT - 1) / NT;
-  __shared__ __align__(16) float sP[SNS * SPLANE];
-  __shared__ __align__(16) float sL[SNS * SPLANE];
+  constexpr int STRIDE = TMA ? TSTRIDE : SPLANE;  // floats per stage
+  __shared__ __align__(128) float sP[SNS * STRIDE];
+  __shared__ __align__(128) float sL[SNS * STRIDE];
+  __shared__ __align__(8) uint64_t sbar[TMA ? SNS : 1];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * PTX + tx;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int n = a.n, sy = a.sy;
@@ -362,22 +400,42 @@ __global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArg
     soff[j] = (lamf[j] ? sL0 : sP0) + (uint32_t)((r * SPW + c) * sizeof(float));
   }
   const bool last_slot = tid + (NCP - 1) * NT < 2 * SUNITS;
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(sbar);
+  // plane p (z0 <= p <= z1 + 1) into stage st; with TMA thread 0 alone calls this
   auto issue = [&](int p, int st) {
     if (p <= z1 + 1) {
-      const float* pp = a.phi + sz * p;
-      const float* lp = a.lam + sz * p;
-      const uint32_t so = (uint32_t)st * (SPLANE * sizeof(float));
+      const uint32_t so = (uint32_t)st * (STRIDE * sizeof(float));
+      if constexpr (TMA) {
+        const uint32_t bar = bar0 + 8u * (uint32_t)st;
+        mbar_expect_tx(bar, TMA_STAGE_BYTES);
+        tma_load_3d(sP0 + so, &maps.phi, x0, y0, p + G, bar);
+        tma_load_3d(sL0 + so, &maps.lam, x0, y0, p + G, bar);
+      } else {
+        const float* pp = a.phi + sz * p;
+        const float* lp = a.lam + sz * p;
 #pragma unroll
-      for (int j = 0; j < NCP; ++j) {
-        if (j == NCP - 1 && !last_slot) break;
-        tcp_async8(soff[j] + so, (lamf[j] ? lp : pp) + goff[j]);
+        for (int j = 0; j < NCP; ++j) {
+          if (j == NCP - 1 && !last_slot) break;
+          tcp_async8(soff[j] + so, (lamf[j] ? lp : pp) + goff[j]);
+        }
       }
     }
   };
+  bool ok = true;
+  if constexpr (TMA) {
+    if (tid == 0) {
+      for (int st = 0; st < SNS; ++st) mbar_init(bar0 + 8u * st, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int i = 0; i < SNS - 1; ++i) issue(z0 + i, i);
+  } else {
 #pragma unroll
-  for (int i = 0; i < SNS - 1; ++i) {
-    issue(z0 + i, i);
-    tcp_commit();
+    for (int i = 0; i < SNS - 1; ++i) {
+      issue(z0 + i, i);
+      tcp_commit();
+    }
   }
   auto at = [&](int i, int j, int k) { return (long)i + (long)sy * j + sz * k; };
   const long c0 = at(xc, yc, z0);
@@ -409,14 +467,26 @@ __global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArg
   for (int z = z0; z < z1; ++z) {
     const int i = z - z0;
     const Col nxt = load_col(min(z + 1, n));  // plane n is a ghost plane: valid memory
-    tcp_wait<1>();
-    __syncthreads();
-    issue(z + SNS - 1, (i + SNS - 1) % SNS);
-    tcp_commit();
-    const float* P0 = sP + (i % SNS) * SPLANE + ci;
-    const float* L0 = sL + (i % SNS) * SPLANE + ci;
-    const float* L1 = sL + ((i + 1) % SNS) * SPLANE + ci;
-    const float* P2 = sP + ((i + 2) % SNS) * SPLANE + ci;
+    if constexpr (TMA) {
+      // planes z and z+1 were waited for as the newest planes of the two previous iterations
+      if (i == 0) ok &= mbar_wait(bar0, 0) & mbar_wait(bar0 + 8u, 0);
+      const int q = i + 2;  // plane z+2: stage q % SNS, its (q / SNS)-th use
+      ok &= mbar_wait(bar0 + 8u * (uint32_t)(q % SNS), (uint32_t)(q / SNS) & 1u);
+      __syncthreads();  // the stage of plane z-1 is no longer read
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(z + SNS - 1, (i + SNS - 1) % SNS);
+      }
+    } else {
+      tcp_wait<1>();
+      __syncthreads();
+      issue(z + SNS - 1, (i + SNS - 1) % SNS);
+      tcp_commit();
+    }
+    const float* P0 = sP + (i % SNS) * STRIDE + ci;
+    const float* L0 = sL + (i % SNS) * STRIDE + ci;
+    const float* L1 = sL + ((i + 1) % SNS) * STRIDE + ci;
+    const float* P2 = sP + ((i + 2) % SNS) * STRIDE + ci;
     const float2 p2 = tsh2(P2), l0 = tsh2(L0), l1 = tsh2(L1);
     const float2 pxm = tsh2(P0 - 2), pxp = tsh2(P0 + 2), lxm = tsh2(L0 - 2), lxp = tsh2(L0 + 2);
     const float2 pym2 = tsh2(P0 - 2 * SPW), pym1 = tsh2(P0 - SPW), pyp1 = tsh2(P0 + SPW), pyp2 = tsh2(P0 + 2 * SPW);
@@ -450,7 +520,11 @@ __global__ void __launch_bounds__(PTX* TY) transport_stage_f32_pair_kernel(TrArg
     p1 = p2;
     cur = nxt;
   }
-  tcp_wait<0>();
+  if constexpr (TMA) {
+    if (!ok) atomicAdd(&g_transport_timeouts, 1u);
+  } else {
+    tcp_wait<0>();
+  }
 }
 
 __global__ void cast_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, size_t n) {
@@ -465,25 +539,63 @@ int cast_f64_to_f32(const double* a, float* b, size_t n, cudaStream_t s) {
   return NEBO_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static std::atomic<EncodeTiledFn> fn{nullptr};
+  EncodeTiledFn f = fn.load(std::memory_order_acquire);
+  if (!f) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    f = reinterpret_cast<EncodeTiledFn>(p);
+    fn.store(f, std::memory_order_release);
+  }
+  return f;
+}
+
+// The tensor map of a float window of gl^3 cells at `base` (16-byte aligned, gl a multiple of 4),
+// box 36 x 12 x 1 (the pair kernel's staged tile).  False when the encoder refuses it.
+bool window_map(CUtensorMap* m, const float* base, int gl) {
+  EncodeTiledFn f = encode_tiled();
+  if (!f || ((uintptr_t)base & 15u) || gl % 4) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)gl, (cuuint64_t)gl, (cuuint64_t)gl};
+  const cuuint64_t strides[2] = {(cuuint64_t)gl * 4, (cuuint64_t)gl * gl * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)SPW, (cuuint32_t)SPH, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return f(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// maps: the tensor maps of a.phi's and a.lam's windows, or nullptr (no tensor staging)
 template <typename T>
-int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
+int transport_launch(TrArgs<T> a, bool second, cudaStream_t s, const TrMaps* maps = nullptr) {
   const int n = a.n;
   const int gxb = (n + TX - 1) / TX, gyb = (n + TY - 1) / TY;
-  // FP32 kernels: 2 = cell pairs (even pitch, every float field 8-byte aligned), 1 = staged
-  // planes (even pitch, phi and lambda 8-byte aligned), 0 = the generic kernel
+  // FP32 kernels: 3 = cell pairs with tensor-tile staging (kind 2 and tensor maps), 2 = cell
+  // pairs (even pitch, every float field 8-byte aligned), 1 = staged planes (even pitch, phi and
+  // lambda 8-byte aligned), 0 = the generic kernel
   auto al8 = [](const void* p) { return ((uintptr_t)p & 7u) == 0; };
   int kind = 0;
   if (sizeof(T) == 4 && a.sy % 2 == 0 && al8(a.phi) && al8(a.lam)) {
     kind = 1;
-    if (al8(a.u) && al8(a.v) && al8(a.w) && al8(a.outS)) kind = 2;
+    if (al8(a.u) && al8(a.v) && al8(a.w) && al8(a.outS)) kind = maps ? 3 : 2;
   }
   // z chunks in whole waves of resident blocks (a chunk reads 2G halo planes beyond its own)
-  static std::atomic<int> per_sm[3][2];  // zero: not queried
+  static std::atomic<int> per_sm[4][2];  // zero: not queried
   std::atomic<int>& cache = per_sm[kind][second];
   int ps;
-  if (kind == 2)
-    ps = second ? blocks_per_sm(transport_stage_f32_pair_kernel<true>, PTX * TY, cache)
-                : blocks_per_sm(transport_stage_f32_pair_kernel<false>, PTX * TY, cache);
+  if (kind == 3)
+    ps = second ? blocks_per_sm(transport_stage_f32_pair_kernel<true, true>, PTX * TY, cache)
+                : blocks_per_sm(transport_stage_f32_pair_kernel<false, true>, PTX * TY, cache);
+  else if (kind == 2)
+    ps = second ? blocks_per_sm(transport_stage_f32_pair_kernel<true, false>, PTX * TY, cache)
+                : blocks_per_sm(transport_stage_f32_pair_kernel<false, false>, PTX * TY, cache);
   else if (kind == 1)
     ps = second ? blocks_per_sm(transport_stage_f32_staged_kernel<true>, TX * TY, cache)
                 : blocks_per_sm(transport_stage_f32_staged_kernel<false>, TX * TY, cache);
@@ -494,11 +606,20 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
   dim3 grid(gxb, gyb, (n + zchunk - 1) / zchunk), block(TX, TY);
   LaunchScope ls(sizeof(T) == 4 ? "transport_stage_f32" : "transport_stage_f64", s);
   if constexpr (sizeof(T) == 4) {
-    if (kind == 2) {
+    if (kind == 3) {
       if (second)
-        transport_stage_f32_pair_kernel<true><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk);
+        transport_stage_f32_pair_kernel<true, true><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk, *maps);
       else
-        transport_stage_f32_pair_kernel<false><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk);
+        transport_stage_f32_pair_kernel<false, true><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk, *maps);
+      NEBO_LAUNCH_CHECK("nebo_transport_run");
+      return NEBO_OK;
+    }
+    if (kind == 2) {
+      const TrMaps none{};
+      if (second)
+        transport_stage_f32_pair_kernel<true, false><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk, none);
+      else
+        transport_stage_f32_pair_kernel<false, false><<<grid, dim3(PTX, TY), 0, s>>>(a, zchunk, none);
       NEBO_LAUNCH_CHECK("nebo_transport_run");
       return NEBO_OK;
     }
@@ -520,6 +641,15 @@ int transport_launch(TrArgs<T> a, bool second, cudaStream_t s) {
 }
 
 }  // namespace
+
+int transport_wait_timeouts(unsigned int* count) {
+  unsigned int v = 0, zero = 0;
+  NEBO_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_transport_timeouts, sizeof(v)));
+  if (v) NEBO_CUDA_TRY(cudaMemcpyToSymbol(g_transport_timeouts, &zero, sizeof(zero)));
+  *count = v;
+  return NEBO_OK;
+}
+
 }  // namespace nebo
 
 using namespace nebo;
@@ -622,6 +752,12 @@ extern "C" int nebo_transport_run(double* phi, const void* u, const void* v, con
   a.q2 = 27.0f * h;
   a.q3 = -h;
   a.dt = dt;
+  // tensor-tile staging of the stencil copies and lambda where the windows allow it (n a multiple
+  // of 4, 16-byte aligned bases; the encoder available)
+  TrMaps m0, m1;  // stage 1 reads s0, stage 2 reads s1
+  const bool tma = n % 4 == 0 && window_map(&m0.phi, s0, gl) && window_map(&m1.phi, s1, gl) &&
+                   window_map(&m0.lam, (const float*)lam, gl);
+  m1.lam = m0.lam;
   double* cur = phi;
   for (int k = 0; k < steps; ++k) {
     a.phi = s0 + interior;
@@ -629,14 +765,14 @@ extern "C" int nebo_transport_run(double* phi, const void* u, const void* v, con
     a.out64 = phi1 + interior;
     a.outS = s1;
     a.outS += interior;
-    if ((rc = transport_launch(a, false, s))) return rc;
+    if ((rc = transport_launch(a, false, s, tma ? &m0 : nullptr))) return rc;
     a.phi = s1 + interior;
     a.acc = phi1 + interior;
     a.base = cur + interior;
     double* nxt = (cur == phi) ? phin : phi;
     a.out64 = nxt + interior;
     a.outS = s0 + interior;
-    if ((rc = transport_launch(a, true, s))) return rc;
+    if ((rc = transport_launch(a, true, s, tma ? &m1 : nullptr))) return rc;
     cur = nxt;
   }
   if (cur != phi) NEBO_CUDA_TRY(cudaMemcpyAsync(phi, cur, cells * sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -43,6 +43,32 @@ def test_transport_fp32_storage_error_vs_fp64_oracle(n, steps):
     assert _rel(t.phi.cpu().numpy(), ref) <= 1e-5
 
 
+@pytest.mark.parametrize("n,steps", [(32, 6), (24, 4)])
+def test_transport_fp32_tensor_staging_matches_cp_async_staging(n, steps):
+    """n a multiple of 4 and lambda 16-byte aligned: the stage kernel stages phi and lambda as
+    tensor tiles (24 also reads past the window's x end, where the tile is zero-filled); lambda
+    8 bytes past a 16-byte boundary takes the cp.async form of the same kernel.  Same arithmetic
+    on the same values, so the FP64 states are bit-identical."""
+    import torch
+
+    phi, u, v, w, lam, dt, nu = W.transport_inputs(n)
+    a = N.Transport(phi, u, v, w, lam, n, dt, nu, dtype="f32")
+    assert a.coef[3].data_ptr() % 16 == 0
+    a.run(steps)
+    b = N.Transport(phi, u, v, w, lam, n, dt, nu, dtype="f32")
+    m = b.coef[3].numel()
+    buf = torch.empty(m + 4, dtype=torch.float32, device="cuda")
+    off = next(k for k in range(4) if (buf.data_ptr() + 4 * k) % 16 == 8)
+    shifted = buf[off:off + m].view_as(b.coef[3])
+    shifted.copy_(b.coef[3])
+    b.coef[3] = shifted
+    assert shifted.data_ptr() % 16 == 8
+    b.run(steps)
+    torch.cuda.synchronize()
+    assert torch.equal(a.phi.view(torch.int64), b.phi.view(torch.int64))
+    assert N.lib().nebo_stream_sync(None) == 0
+
+
 def test_transport_velocity_is_divergence_free():
     n = 16
     _, u, v, w, _, _, _ = W.transport_inputs(n)
