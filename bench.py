@@ -578,6 +578,31 @@ def part_heat(N, bus, peak):
     out["fixed_point"] = {"gcell_upd_s": cells / (msf * 1e-3) / 1e9, "ms_per_step": msf, "steps": k,
                           "alg_gbs": gbsf, "hbm_frac": gbsf / peak, "clocks": clocksf,
                           "accuracy": "within 1e-13 relative max-norm of the bit-exact form (tests)"}
+    # FP32 storage and arithmetic (the bandwidth path), and its error against the FP64 step after
+    # 50 steps from the same state at the stable step 0.15 / max(lambda)
+    W32 = Heat(N, 256, "f32")
+    run32 = lambda kk: [W32.step() for _ in range(kk)]
+    run32(3)
+    k32 = _steps_for(run32)
+    ms32, clocks32 = _timed(run32, k32, bus)
+    gbs32 = BYTES_PER_CELL["heat32"] * cells / (ms32 * 1e-3) / 1e9
+    dt_stable = W.dt * 0.75
+
+    def state_after(w, steps):
+        w.T.tensor.copy_(w.host[0])
+        N.fill_periodic(w.T)
+        a, b = w.T, w.Tt
+        for _ in range(steps):
+            N.heat_step(a, b, w.L, dt_stable)
+            a, b = b, a
+        return a.tensor[1:-1, 1:-1, 1:-1].double()
+
+    s64, s32 = state_after(W, 50), state_after(W32, 50)
+    err = float((s32 - s64).abs().max() / s64.abs().max())
+    out["fp32"] = {"gcell_upd_s": cells / (ms32 * 1e-3) / 1e9, "ms_per_step": ms32, "steps": k32,
+                   "alg_gbs": gbs32, "hbm_frac": gbs32 / peak, "clocks": clocks32,
+                   "fp32_over_fp64": ms / ms32, "rel_err_50_steps_vs_fp64": err,
+                   "error_reference": "the bit-exact FP64 step (equal to the oracle bit for bit)"}
     return out
 
 
