@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cmath>
 
 #include <spatialops/NeboCore.h>
 #include <spatialops/NeboOperators.h>
@@ -104,14 +105,17 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
   const long sz = (long)lhs.window_with_ghost().glob_dim(0) * (long)lhs.window_with_ghost().glob_dim(1);
   const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
   cudaStream_t s = (cudaStream_t)lhs.get_stream();
-  typedef typename std::decay<decltype(dev)>::type D;
+  // linear stencils of linear stencils merged into one (reassociating builds; NeboTiled.h)
+  typedef Compose<typename std::decay<decltype(dev)>::type> CP;
+  typedef typename CP::type D;
+  const D devc = CP::make(dev);
 #ifndef NEBO_UNTILED
   if constexpr (TilePlan<D>::tz > 0) {
     // nested stencils: one block per 32 x 8 x TZ tile, inner levels materialised in shared memory
     constexpr int TZ = TilePlan<D>::tz;
     typedef typename TileAt<D, TZ>::type Plan;
     typedef typename Plan::type DT;
-    const DT dt = Plan::make(dev);
+    const DT dt = Plan::make(devc);
     constexpr int smem = Plan::end;
     auto kern = nebo_tiled_assign_kernel<T, DT, TZ, Plan::rounds>;
     if (smem > 48 * 1024)
@@ -121,23 +125,49 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
     kern<<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(out, sy, sz, lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], dt);
     throw_cuda(cudaGetLastError(), "Nebo Assignment (kernel launch)");
   } else {
-    assign_plain<T>(out, sy, sz, lim, dev, s);
+    assign_plain<T>(out, sy, sz, lim, devc, s);
   }
 #else
-  assign_plain<T>(out, sy, sz, lim, dev, s);
+  assign_plain<T>(out, sy, sz, lim, devc, s);
 #endif
 }
 
-// The one-pass form: one thread per (x, y) column of a z-chunk.
+// The one-pass form: one thread per (x, y) column of a z-chunk.  The z split: the whole number
+// of resident-block waves (at most 8) whose last wave is fullest (a split that leaves most of a
+// last wave idle costs a whole wave); NEBO_UNTILED keeps the plain rule of about 8 blocks per SM.
 template <typename T, class D>
 void assign_plain(T* out, int sy, long sz, const int32_t lim[6], const D& dev, cudaStream_t s) {
   const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
   dim3 block(32, 8, 1);
   dim3 grid((nx + 31) / 32, (ny + 7) / 8, 1);
   const long plane_blocks = (long)grid.x * grid.y;
+#ifndef NEBO_UNTILED
+  static std::atomic<int> per_sm{0};  // resident blocks of this instantiation (one architecture)
+  int bps = per_sm.load(std::memory_order_relaxed);
+  if (bps <= 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, nebo_assign_kernel<T, D>, 256, 0) != cudaSuccess ||
+        bps < 1) {
+      cudaGetLastError();
+      bps = 1;
+    }
+    per_sm.store(bps, std::memory_order_relaxed);
+  }
+  const long slots = (long)device_sm_count() * bps;
+  long chunks = 1;
+  double best = -1.0;
+  for (long k = 1; k <= nz && plane_blocks * k <= 8 * slots; ++k) {
+    const double waves = (double)(plane_blocks * k) / (double)slots;
+    const double fill = waves / std::ceil(waves);
+    if (fill > best + 1e-3) {
+      best = fill;
+      chunks = k;
+    }
+  }
+#else
   long chunks = (8L * device_sm_count() + plane_blocks - 1) / plane_blocks;
   if (chunks < 1) chunks = 1;
   if (chunks > nz) chunks = nz;
+#endif
   const int zchunk = (int)((nz + chunks - 1) / chunks);
   grid.z = (unsigned)((nz + zchunk - 1) / zchunk);
   nebo_assign_kernel<T, D><<<grid, block, 0, s>>>(
@@ -151,7 +181,8 @@ void masked(const SpatialMask<F>& mask, F& lhs, const Node& rhs) {
   const int np = mask.num_points();
   if (np == 0) return;
   LaunchStreamScope scope(lhs.get_stream());
-  auto dev = rhs.device();
+  typedef Compose<typename std::decay<decltype(rhs.device())>::type> CP;
+  const auto dev = CP::make(rhs.device());
   T* out = lhs.device_values_for_write() + lhs.interior_origin();
   const int sy = (int)lhs.window_with_ghost().glob_dim(0);
   const long sz = (long)lhs.window_with_ghost().glob_dim(0) * (long)lhs.window_with_ghost().glob_dim(1);

@@ -365,6 +365,185 @@ struct Tile<DApply<T, Fn, D...>, R, Off> {
 };
 #endif
 
+// ---------------------------------------------------------------------------- stencil composition
+// In builds that allow reassociation (and not NEBO_UNTILED), a weighted stencil whose argument
+// is a weighted stencil becomes ONE weighted stencil of the inner argument: its points are the
+// sums p + q of the outer and inner points (the Minkowski sum, each sum listed once), and a
+// point's coefficient is the sum of the products c_outer[i] * c_inner[j] of the pairs landing
+// on it, computed on the host once per launch.  Interp(Grad(Interp(a))) thus becomes the
+// 4-point stencil (g/4) * (-a[i-2] - a[i-1] + a[i] + a[i+1]) of the field a, read directly
+// instead of materialised level by level.  The composed stencil reads exactly the points the
+// nested sums read (the write region's guarantee holds); its values differ from the nested
+// evaluation by rounding only.  Compositions of more than kComposeMaxPoints points, box sums
+// and stencils of different value types are left as they are.
+constexpr int kComposeMaxPoints = 27;
+#if defined(NEBO_EXACT_ARITHMETIC) || defined(NEBO_UNTILED)
+constexpr bool kCompose = false;
+#else
+constexpr bool kCompose = true;
+#endif
+
+template <class L, class P>
+struct HasPt;
+template <class P>
+struct HasPt<NeboNil, P> : std::false_type {};
+template <class Q, class R, class P>
+struct HasPt<NeboStencilPointCollection<Q, R>, P>
+    : std::integral_constant<bool, (Q::X == P::X && Q::Y == P::Y && Q::Z == P::Z) || HasPt<R, P>::value> {};
+
+// L with P appended as its last-listed point, unless L holds P already (L may be NeboNil)
+template <class L, class P>
+struct PushPt {
+  typedef typename std::conditional<HasPt<L, P>::value, L, NeboStencilPointCollection<P, L>>::type type;
+};
+
+// Acc with every point of L (in listed order) shifted by Q appended
+template <class Acc, class L, class Q>
+struct AddShifted;
+template <class Acc, class Q>
+struct AddShifted<Acc, NeboNil, Q> {
+  typedef Acc type;
+};
+template <class Acc, class P, class R, class Q>
+struct AddShifted<Acc, NeboStencilPointCollection<P, R>, Q> {
+  typedef typename AddShifted<Acc, R, Q>::type A1;  // R holds the points listed before P
+  typedef typename PushPt<A1, IndexTriplet<P::X + Q::X, P::Y + Q::Y, P::Z + Q::Z>>::type type;
+};
+
+// Minkowski sum of two point collections: for each q of L2 in listed order, L1 shifted by q
+template <class Acc, class L1, class L2>
+struct MinkAcc;
+template <class Acc, class L1>
+struct MinkAcc<Acc, L1, NeboNil> {
+  typedef Acc type;
+};
+template <class Acc, class L1, class Q, class R>
+struct MinkAcc<Acc, L1, NeboStencilPointCollection<Q, R>> {
+  typedef typename MinkAcc<Acc, L1, R>::type A1;
+  typedef typename AddShifted<A1, L1, Q>::type type;
+};
+template <class L1, class L2>
+struct MinkSum {
+  typedef typename MinkAcc<NeboNil, L1, L2>::type type;
+};
+
+// The points of a collection by listed index (the index of a point's coefficient), host side.
+template <class L>
+struct PtsAt;
+template <>
+struct PtsAt<NeboNil> {
+  static int x(int) { return 0; }
+  static int y(int) { return 0; }
+  static int z(int) { return 0; }
+  static int index_of(int, int, int) { return -1; }
+};
+template <class P, class R>
+struct PtsAt<NeboStencilPointCollection<P, R>> {
+  static int x(int i) { return i == R::length ? P::X : PtsAt<R>::x(i); }
+  static int y(int i) { return i == R::length ? P::Y : PtsAt<R>::y(i); }
+  static int z(int i) { return i == R::length ? P::Z : PtsAt<R>::z(i); }
+  static int index_of(int px, int py, int pz) {
+    return (P::X == px && P::Y == py && P::Z == pz) ? R::length : PtsAt<R>::index_of(px, py, pz);
+  }
+};
+
+// An outer stencil (points P1, coefficients c1) over an already composed argument AC.
+template <typename T, class P1, class AC, class Enable = void>
+struct StencilMerge {  // kept nested
+  typedef DStencil<T, P1, AC> type;
+  static type make(const double* c1, const AC& a) {
+    type o;
+    o.a = a;
+    for (int i = 0; i < P1::length; ++i) o.c[i] = c1[i];
+    return o;
+  }
+};
+template <typename T, class P1, class P2, class A2>
+struct StencilMerge<T, P1, DStencil<T, P2, A2>,
+                    typename std::enable_if<kCompose && (MinkSum<P1, P2>::type::length <= kComposeMaxPoints)>::type> {
+  typedef typename MinkSum<P1, P2>::type PM;
+  typedef DStencil<T, PM, A2> type;
+  static type make(const double* c1, const DStencil<T, P2, A2>& in) {
+    type o;
+    o.a = in.a;
+    for (int k = 0; k < PM::length; ++k) o.c[k] = 0.0;
+    for (int i = 0; i < P1::length; ++i)
+      for (int j = 0; j < P2::length; ++j) {
+        const int k = PtsAt<PM>::index_of(PtsAt<P1>::x(i) + PtsAt<P2>::x(j), PtsAt<P1>::y(i) + PtsAt<P2>::y(j),
+                                          PtsAt<P1>::z(i) + PtsAt<P2>::z(j));
+        o.c[k] += c1[i] * in.c[j];
+      }
+    return o;
+  }
+};
+
+// Compose<D>: D with every composable stencil pair merged (identity for anything else).
+template <class D>
+struct Compose {
+  typedef D type;
+  static type make(const D& d) { return d; }
+};
+template <class Op, typename T, class A, class B>
+struct Compose<DBin<Op, T, A, B>> {
+  typedef Compose<A> CA;
+  typedef Compose<B> CB;
+  typedef DBin<Op, T, typename CA::type, typename CB::type> type;
+  static type make(const DBin<Op, T, A, B>& d) { return type{CA::make(d.a), CB::make(d.b)}; }
+};
+template <class Fn, typename T, class A>
+struct Compose<DUn<Fn, T, A>> {
+  typedef Compose<A> CA;
+  typedef DUn<Fn, T, typename CA::type> type;
+  static type make(const DUn<Fn, T, A>& d) { return type{CA::make(d.a)}; }
+};
+template <typename T, class A>
+struct Compose<DPowInt<T, A>> {
+  typedef Compose<A> CA;
+  typedef DPowInt<T, typename CA::type> type;
+  static type make(const DPowInt<T, A>& d) { return type{CA::make(d.a), d.e}; }
+};
+template <class Op, class A, class B>
+struct Compose<DCmp<Op, A, B>> {
+  typedef Compose<A> CA;
+  typedef Compose<B> CB;
+  typedef DCmp<Op, typename CA::type, typename CB::type> type;
+  static type make(const DCmp<Op, A, B>& d) { return type{CA::make(d.a), CB::make(d.b)}; }
+};
+template <class Op, class A, class B>
+struct Compose<DLogic<Op, A, B>> {
+  typedef Compose<A> CA;
+  typedef Compose<B> CB;
+  typedef DLogic<Op, typename CA::type, typename CB::type> type;
+  static type make(const DLogic<Op, A, B>& d) { return type{CA::make(d.a), CB::make(d.b)}; }
+};
+template <class A>
+struct Compose<DNot<A>> {
+  typedef Compose<A> CA;
+  typedef DNot<typename CA::type> type;
+  static type make(const DNot<A>& d) { return type{CA::make(d.a)}; }
+};
+template <typename T, class Test, class Val, class Rest>
+struct Compose<DCond<T, Test, Val, Rest>> {
+  typedef Compose<Test> CT;
+  typedef Compose<Val> CV;
+  typedef Compose<Rest> CR;
+  typedef DCond<T, typename CT::type, typename CV::type, typename CR::type> type;
+  static type make(const DCond<T, Test, Val, Rest>& d) { return type{CT::make(d.t), CV::make(d.v), CR::make(d.r)}; }
+};
+template <typename T, class Pts, class A>
+struct Compose<DSumStencil<T, Pts, A>> {
+  typedef Compose<A> CA;
+  typedef DSumStencil<T, Pts, typename CA::type> type;
+  static type make(const DSumStencil<T, Pts, A>& d) { return type{CA::make(d.a)}; }
+};
+template <typename T, class P1, class A>
+struct Compose<DStencil<T, P1, A>> {
+  typedef Compose<A> CA;
+  typedef StencilMerge<T, P1, typename CA::type> M;
+  typedef typename M::type type;
+  static type make(const DStencil<T, P1, A>& d) { return M::make(d.c, CA::make(d.a)); }
+};
+
 // The plan for a functor: the tile depth TZ whose buffers fit the budget, or 0 when no stencil
 // needs a buffer (or none fits): the plain kernel then runs.
 template <class D, int TZ>

@@ -36,7 +36,7 @@ using namespace SpatialOps;
 #ifdef NEBO_UNTILED
 static const char* kLowering = "one thread per column (untiled)";
 #else
-static const char* kLowering = "tiled (inner stencil levels in shared memory)";
+static const char* kLowering = "tiled (linear stencil chains composed, other inner stencil levels in shared memory)";
 #endif
 #ifdef NEBO_CUDA_LIBM
 static const char* kMath = "CUDA exp/sin";
