@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include <spatialops/NeboCore.h>
+#include <spatialops/NeboFactor.h>
 #include <spatialops/NeboOperators.h>
 #include <spatialops/NeboTiled.h>
 
@@ -93,6 +94,31 @@ bool write_region(const F& lhs, const Node& rhs, bool useGhost, int32_t lim[6]) 
 template <typename T, class D>
 void assign_plain(T* out, int sy, long sz, const int32_t lim[6], const D& dev, cudaStream_t s);
 
+// One kernel for functor D over the write region: tiled when D has a stencil of an expression.
+template <typename T, class D>
+void assign_launch(T* out, int sy, long sz, const int32_t lim[6], const D& dev, cudaStream_t s) {
+#ifndef NEBO_UNTILED
+  if constexpr (TilePlan<D>::tz > 0) {
+    // nested stencils: one block per 32 x 8 x TZ tile, inner levels materialised in shared memory
+    const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
+    constexpr int TZ = TilePlan<D>::tz;
+    typedef typename TileAt<D, TZ>::type Plan;
+    typedef typename Plan::type DT;
+    const DT dt = Plan::make(dev);
+    constexpr int smem = Plan::end;
+    auto kern = nebo_tiled_assign_kernel<T, DT, TZ, Plan::rounds>;
+    if (smem > 48 * 1024)
+      throw_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                 "Nebo Assignment (shared memory)");
+    const dim3 grid((nx + kTileX - 1) / kTileX, (ny + kTileY - 1) / kTileY, (nz + TZ - 1) / TZ);
+    kern<<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(out, sy, sz, lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], dt);
+    throw_cuda(cudaGetLastError(), "Nebo Assignment (kernel launch)");
+    return;
+  }
+#endif
+  assign_plain<T>(out, sy, sz, lim, dev, s);
+}
+
 template <class F, class Node>
 void assign(F& lhs, const Node& rhs, bool useGhost) {
   typedef typename F::value_type T;
@@ -103,33 +129,23 @@ void assign(F& lhs, const Node& rhs, bool useGhost) {
   T* out = lhs.device_values_for_write() + lhs.interior_origin();
   const int sy = (int)lhs.window_with_ghost().glob_dim(0);
   const long sz = (long)lhs.window_with_ghost().glob_dim(0) * (long)lhs.window_with_ghost().glob_dim(1);
-  const int nx = lim[1] - lim[0], ny = lim[3] - lim[2], nz = lim[5] - lim[4];
   cudaStream_t s = (cudaStream_t)lhs.get_stream();
   // linear stencils of linear stencils merged into one (reassociating builds; NeboTiled.h)
   typedef Compose<typename std::decay<decltype(dev)>::type> CP;
   typedef typename CP::type D;
   const D devc = CP::make(dev);
-#ifndef NEBO_UNTILED
-  if constexpr (TilePlan<D>::tz > 0) {
-    // nested stencils: one block per 32 x 8 x TZ tile, inner levels materialised in shared memory
-    constexpr int TZ = TilePlan<D>::tz;
-    typedef typename TileAt<D, TZ>::type Plan;
-    typedef typename Plan::type DT;
-    const DT dt = Plan::make(devc);
-    constexpr int smem = Plan::end;
-    auto kern = nebo_tiled_assign_kernel<T, DT, TZ, Plan::rounds>;
-    if (smem > 48 * 1024)
-      throw_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                 "Nebo Assignment (shared memory)");
-    const dim3 grid((nx + kTileX - 1) / kTileX, (ny + kTileY - 1) / kTileY, (nz + TZ - 1) / TZ);
-    kern<<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(out, sy, sz, lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], dt);
-    throw_cuda(cudaGetLastError(), "Nebo Assignment (kernel launch)");
-  } else {
-    assign_plain<T>(out, sy, sz, lim, devc, s);
+  // constant factors carried on the host (reassociating builds; NeboFactor.h), when the launch's
+  // coefficients allow it
+  typedef FactorRoot<T, D> FR;
+  if constexpr (FR::changes) {
+    bool ok = true;
+    const typename FR::type fac = FR::make(devc, ok);
+    if (ok) {
+      assign_launch<T>(out, sy, sz, lim, fac, s);
+      return;
+    }
   }
-#else
-  assign_plain<T>(out, sy, sz, lim, devc, s);
-#endif
+  assign_launch<T>(out, sy, sz, lim, devc, s);
 }
 
 // The one-pass form: one thread per (x, y) column of a z-chunk.  The z split: the whole number

@@ -441,11 +441,22 @@ namespace nebo_detail {
 // Device stencil fold in listed order: ((a(p0)*c0 + a(p1)*c1) + a(p2)*c2) + ...
 template <class Coll>
 struct StencilFold;
+// v with the sign bit of s (a point of a signed sum: s = +-1)
+__device__ __forceinline__ double sign_of(double v, double s) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (__double_as_longlong(s) & (long long)0x8000000000000000ULL));
+}
+__device__ __forceinline__ float sign_of(float v, double s) {
+  return __int_as_float(__float_as_int(v) ^ (int)((unsigned)((unsigned long long)__double_as_longlong(s) >> 32) & 0x80000000u));
+}
 template <class P>
 struct StencilFold<NeboStencilPointCollection<P, NeboNil>> {
   template <typename T, class A>
   static __device__ __forceinline__ T weighted(const A& a, const double* c, int x, int y, int z) {
     return Arith<T>::mul(a.eval(x + P::X, y + P::Y, z + P::Z), (T)c[0]);
+  }
+  template <typename T, class A>
+  static __device__ __forceinline__ T signed_sum(const A& a, const double* c, int x, int y, int z) {
+    return sign_of(a.eval(x + P::X, y + P::Y, z + P::Z), c[0]);
   }
   template <typename T, class A>
   static __device__ __forceinline__ T sum(const A& a, int x, int y, int z) {
@@ -462,6 +473,11 @@ struct StencilFold<NeboStencilPointCollection<P, R>> {
   template <typename T, class A>
   static __device__ __forceinline__ T sum(const A& a, int x, int y, int z) {
     return Arith<T>::add(StencilFold<R>::template sum<T>(a, x, y, z), a.eval(x + P::X, y + P::Y, z + P::Z));
+  }
+  template <typename T, class A>
+  static __device__ __forceinline__ T signed_sum(const A& a, const double* c, int x, int y, int z) {
+    return Arith<T>::add(StencilFold<R>::template signed_sum<T>(a, c, x, y, z),
+                         sign_of(a.eval(x + P::X, y + P::Y, z + P::Z), c[R::length]));
   }
 };
 

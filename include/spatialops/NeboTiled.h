@@ -105,15 +105,20 @@ struct SmemView {
 #endif
 };
 
+// The folds of a materialised stencil: weighted (c in listed order), plain sum, signed sum (the
+// points' values with the sign bits of c, added in listed order; NeboFactor.h).
+enum StencilKind { kWeighted = 0, kSum = 1, kSigned = 2 };
+
 // A stencil whose argument is materialised over box R at byte offset Off in fill round Round.
-template <typename T, class Pts, class A, class R, int Off, int Round, bool Sum>
+template <typename T, class Pts, class A, class R, int Off, int Round, int Kind>
 struct DStencilSmem {
   A a;
   double c[Pts::length];
 #ifdef __CUDACC__
   __device__ __forceinline__ T eval(int x, int y, int z) const {
-    return Sum ? StencilFold<Pts>::template sum<T>(SmemView<T, R, Off>(), x, y, z)
-               : StencilFold<Pts>::template weighted<T>(SmemView<T, R, Off>(), c, x, y, z);
+    if (Kind == kSum) return StencilFold<Pts>::template sum<T>(SmemView<T, R, Off>(), x, y, z);
+    if (Kind == kSigned) return StencilFold<Pts>::template signed_sum<T>(SmemView<T, R, Off>(), c, x, y, z);
+    return StencilFold<Pts>::template weighted<T>(SmemView<T, R, Off>(), c, x, y, z);
   }
   __device__ __forceinline__ void rebase(int x0, int y0, int z0) { a.rebase(x0, y0, z0); }
   template <int H>
@@ -285,17 +290,17 @@ struct Tile<DSumStencil<T, Pts, A>, R, Off,
 constexpr int round16(int b) { return (b + 15) / 16 * 16; }
 
 // a stencil of an expression: the argument is materialised over the grown box
-template <typename T, class Pts, class A, class R, int Off, bool Sum>
+template <typename T, class Pts, class A, class R, int Off, int Kind>
 struct TileSmemStencil {
   typedef typename GrowBox<R, Pts>::type RA;
   typedef Tile<A, RA, Off> TA;
   enum { my_off = TA::end, end = TA::end + round16(RA::n * (int)sizeof(T)), rounds = TA::rounds + 1 };
-  typedef DStencilSmem<T, Pts, typename TA::type, RA, my_off, rounds, Sum> type;
+  typedef DStencilSmem<T, Pts, typename TA::type, RA, my_off, rounds, Kind> type;
 };
 template <typename T, class Pts, class A, class R, int Off>
 struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::value>::type>
-    : TileSmemStencil<T, Pts, A, R, Off, false> {
-  typedef TileSmemStencil<T, Pts, A, R, Off, false> B;
+    : TileSmemStencil<T, Pts, A, R, Off, kWeighted> {
+  typedef TileSmemStencil<T, Pts, A, R, Off, kWeighted> B;
   static typename B::type make(const DStencil<T, Pts, A>& d) {
     typename B::type t;
     t.a = B::TA::make(d.a);
@@ -306,8 +311,8 @@ struct Tile<DStencil<T, Pts, A>, R, Off, typename std::enable_if<!IsLeaf<A>::val
 template <typename T, class Pts, class A, class R, int Off>
 struct Tile<DSumStencil<T, Pts, A>, R, Off,
             typename std::enable_if<!IsLeaf<A>::value && !SplitBox<Pts>::value>::type>
-    : TileSmemStencil<T, Pts, A, R, Off, true> {
-  typedef TileSmemStencil<T, Pts, A, R, Off, true> B;
+    : TileSmemStencil<T, Pts, A, R, Off, kSum> {
+  typedef TileSmemStencil<T, Pts, A, R, Off, kSum> B;
   static typename B::type make(const DSumStencil<T, Pts, A>& d) {
     typename B::type t;
     t.a = B::TA::make(d.a);
