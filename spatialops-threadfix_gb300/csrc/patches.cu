@@ -234,10 +234,12 @@ __device__ __forceinline__ void pcp_wait() { asm volatile("cp.async.wait_group %
 // whatever the patch's shape (tiles of fixed width leave up to half the lanes idle on patches of
 // 16..96 cells).  The strip plus its one-cell halo, at most (R + 2)(W + 2) <= PR_STAGE floats,
 // streams through the same ring of PNS stages as the tiled kernel; each cell reads its six
-// neighbours from the stage and carries its centre value and low z face in registers.  The
+// neighbours from the stage and carries its centre value and the one below it in registers.  The
 // halo is read from the periodic images' sources (x = -1 -> nx - 1, ...), so no step writes
-// ghost cells: nebo_patchset_run fills them once after its last step.  Per cell the same
-// operations as the tiled kernel.
+// ghost cells: nebo_patchset_run fills them once after its last step.  With lambda constant over
+// a patch the six face fluxes sum to 2 lambda (sum of the neighbours - 6 T), so a cell costs 5
+// adds and 2 FMAs in FP32, T' = T + (dt lambda) (sum - 6 T) with dt lambda rounded once on the
+// host (the FP64 mode keeps the reference's face form, bit for bit).
 constexpr int PR_CELLS = 1024;                    // cells per strip plane
 constexpr int PR_CPT = PR_CELLS / PT_THREADS;     // cells per thread
 constexpr int PR_MAXW = 512;
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(PT_THREADS, 2) patches_f32_strip_kernel(const 
     const long interior = (long)1 + sy + sz;
     const float* tin = src + P.offset + interior;
     float* tout = dst + P.offset + interior;
-    const float l2 = (float)P.lam2, hdt = (float)P.hdt;
+    const float k = (float)(P.hdt * P.lam2);  // T' = T + k (sum of the 6 neighbours - 6 T)
     const int z0 = it.z0, z1 = it.z1;
     // copy slots: unit k of the (R+2) x (W+2) halo strip, halo cells at the patch's faces taken
     // from their periodic sources
@@ -317,11 +319,11 @@ __global__ void __launch_bounds__(PT_THREADS, 2) patches_f32_strip_kernel(const 
     }
     pcp_wait<PNS - 3>();
     __syncthreads();
-    float t[PR_CPT], fz[PR_CPT];
+    float t[PR_CPT], tb[PR_CPT];  // the cell and the one below it
 #pragma unroll
     for (int j = 0; j < PR_CPT; ++j) {
       t[j] = ring[si[j]];
-      fz[j] = l2 * (t[j] - ring[(PNS - 1) * PR_STAGE + si[j]]);
+      tb[j] = ring[(PNS - 1) * PR_STAGE + si[j]];
     }
     for (int zb = z0; zb < z1; zb += PNS) {
 #pragma unroll
@@ -338,14 +340,9 @@ __global__ void __launch_bounds__(PT_THREADS, 2) patches_f32_strip_kernel(const 
         for (int j = 0; j < PR_CPT; ++j) {
           const int c = si[j];
           const float tc = t[j], tn = Tn[c];
-          const float fxl = l2 * (tc - T0[c - 1]);
-          const float fxh = l2 * (T0[c + 1] - tc);
-          const float fyl = l2 * (tc - T0[c - SW]);
-          const float fyh = l2 * (T0[c + SW] - tc);
-          const float fzh = l2 * (tn - tc);
-          const float sflux = ((fxh - fxl) + (fyh - fyl)) + (fzh - fz[j]);
-          if ((live >> j) & 1u) tout[(long)gi[j] + sz * z] = tc + hdt * sflux;
-          fz[j] = fzh;
+          const float nb = ((T0[c - 1] + T0[c + 1]) + (T0[c - SW] + T0[c + SW])) + (tb[j] + tn);
+          if ((live >> j) & 1u) tout[(long)gi[j] + sz * z] = fmaf(k, fmaf(-6.0f, tc, nb), tc);
+          tb[j] = tc;
           t[j] = tn;
         }
       }
@@ -396,7 +393,7 @@ __global__ void __launch_bounds__(PT_THREADS) patches_f32_bulk_kernel(const Patc
     const long sz = (long)ny * pitch;
     const float* base = src + P.off32;
     float* obase = dst + P.off32;
-    const float l2 = (float)P.lam2, hdt = (float)P.hdt;
+    const float k = (float)(P.hdt * P.lam2);  // T' = T + k (sum of the 6 neighbours - 6 T)
     const int z0 = it.z0, z1 = it.z1;
     const uint32_t rowb = (uint32_t)pitch * 4u;
     const int ylo = it.y0 == 0 ? ny - 1 : it.y0 - 1;
@@ -438,11 +435,11 @@ __global__ void __launch_bounds__(PT_THREADS) patches_f32_bulk_kernel(const Patc
       go[j] = (it.y0 + r) * pitch + col;
     }
     ok &= mbar_wait(bar0, 0) & mbar_wait(bar0 + 8, 0);
-    float t[PB_CPT], fz[PB_CPT];
+    float t[PB_CPT], tb[PB_CPT];  // the cell and the one below it
 #pragma unroll
     for (int j = 0; j < PB_CPT; ++j) {
       t[j] = ring[stage_floats + si[j]];
-      fz[j] = l2 * (t[j] - ring[si[j]]);
+      tb[j] = ring[si[j]];
     }
     for (int z = z0; z < z1; ++z) {
       const int q = z - z0 + 1;  // centre plane
@@ -459,14 +456,9 @@ __global__ void __launch_bounds__(PT_THREADS) patches_f32_bulk_kernel(const Patc
       for (int j = 0; j < PB_CPT; ++j) {
         const int c = si[j];
         const float tc = t[j], tn = Tn[c];
-        const float fxl = l2 * (tc - T0[sl[j]]);
-        const float fxh = l2 * (T0[sr[j]] - tc);
-        const float fyl = l2 * (tc - T0[c - pitch]);
-        const float fyh = l2 * (T0[c + pitch] - tc);
-        const float fzh = l2 * (tn - tc);
-        const float sflux = ((fxh - fxl) + (fyh - fyl)) + (fzh - fz[j]);
-        if ((live >> j) & 1u) op[go[j]] = tc + hdt * sflux;
-        fz[j] = fzh;
+        const float nb = ((T0[sl[j]] + T0[sr[j]]) + (T0[c - pitch] + T0[c + pitch])) + (tb[j] + tn);
+        if ((live >> j) & 1u) op[go[j]] = fmaf(k, fmaf(-6.0f, tc, nb), tc);
+        tb[j] = tc;
         t[j] = tn;
       }
     }
