@@ -165,6 +165,7 @@ def run_catalog(domain):
     simple("s_fd_grady", "SVol", lambda: db.fd("grad", 1)(a))
     simple("s_fd_interpz", "SVol", lambda: db.fd("interp", 2)(a))
     simple("x_fd_gradz", "XVol", lambda: db.fd("grad", 2)(xa))
+    simple("s_user_pair", "SVol", lambda: O.Stencil([(0, 0, 0), (1, 0, 0)], [0.25, 0.75], a) * b)
 
     # box filter
     simple("s_filter", "SVol", lambda: db.filter()(a))
