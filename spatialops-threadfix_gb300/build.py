@@ -72,6 +72,8 @@ PROGRAMS = {
     "assign_timing": ("assign_timing.cu", []),
     "assign_timing_untiled": ("assign_timing.cu", ["-DNEBO_UNTILED", "-DNEBO_CUDA_LIBM"]),
     "assign_timing_libm": ("assign_timing.cu", ["-DNEBO_CUDA_LIBM"]),
+    # `<<=` on FP32 fields against FP64 (the lowering passes on float)
+    "float_assign": ("float_assign.cu", []),
 }
 
 
