@@ -316,6 +316,18 @@ struct FactorRoot {
 };
 
 // ---------------------------------------------------------------------------- tiled lowering
+#ifdef __CUDACC__
+// a factor applied to a z pair (the box filter's 1/27 at the root)
+template <typename T, class A>
+struct PairZ<T, DScaled<T, A>> {
+  static __device__ __forceinline__ void eval(const DScaled<T, A>& f, int x, int y, int z, T& v0, T& v1) {
+    PairZ<T, A>::eval(f.a, x, y, z, v0, v1);
+    v0 = Arith<T>::mul(v0, (T)f.r);
+    v1 = Arith<T>::mul(v1, (T)f.r);
+  }
+};
+#endif
+
 template <typename T, class A, class R, int Off>
 struct Tile<DScaled<T, A>, R, Off> {
   typedef Tile<A, R, Off> TA;

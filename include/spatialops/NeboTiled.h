@@ -109,6 +109,14 @@ struct SmemView {
 // points' values with the sign bits of c, added in listed order; NeboFactor.h).
 enum StencilKind { kWeighted = 0, kSum = 1, kSigned = 2 };
 
+// How the fill of a buffer whose points are the values of A may share work between two
+// neighbouring points: 0 none, 1 x pairs, 2 y pairs (specialised below for the line sums of a
+// split box filter, whose neighbouring sums share their middle pair).
+template <typename T, class A>
+struct PairFill {
+  static constexpr int axis = 0;
+};
+
 // A stencil whose argument is materialised over box R at byte offset Off in fill round Round.
 template <typename T, class Pts, class A, class R, int Off, int Round, int Kind>
 struct DStencilSmem {
@@ -129,13 +137,48 @@ struct DStencilSmem {
     // points read by the tile's output cells: the box, its upper ends cut by the partial tile
     const int hx = R::xh - tx, hy = R::yh - ty, hz = R::zh - tz;
     const int tid = (int)(threadIdx.x + blockDim.x * threadIdx.y);
+    constexpr int ax = PairFill<T, A>::axis;
+    if constexpr (ax == 1 && R::nx % 2 == 0) {
+      // x pairs (lx, lx+1): the second point (and its extra read) only when a cell needs it
+      constexpr int hn = R::nx / 2;
 #pragma unroll 2
-    for (int i = tid; i < R::n; i += kTileThreads) {
-      const int lx = R::xl + i % R::nx;
-      const int r = i / R::nx;
-      const int ly = R::yl + r % R::ny;
-      const int lz = R::zl + r / R::ny;
-      if (lx <= hx && ly <= hy && lz <= hz) buf[i] = a.eval(lx, ly, lz);
+      for (int i = tid; i < R::n / 2; i += kTileThreads) {
+        const int px = i % hn, r = i / hn;
+        const int lx = R::xl + 2 * px, ly = R::yl + r % R::ny, lz = R::zl + r / R::ny;
+        if (lx <= hx && ly <= hy && lz <= hz) {
+          const bool second = lx + 1 <= hx;
+          T v0, v1;
+          PairFill<T, A>::pair(a, lx, ly, lz, second, v0, v1);
+          const int bi = 2 * px + R::nx * r;
+          buf[bi] = v0;
+          if (second) buf[bi + 1] = v1;
+        }
+      }
+    } else if constexpr (ax == 2 && R::ny % 2 == 0) {
+      // y pairs (ly, ly+1)
+      constexpr int hn = R::ny / 2;
+#pragma unroll 2
+      for (int i = tid; i < R::n / 2; i += kTileThreads) {
+        const int ox = i % R::nx, r = i / R::nx, py = r % hn, oz = r / hn;
+        const int lx = R::xl + ox, ly = R::yl + 2 * py, lz = R::zl + oz;
+        if (lx <= hx && ly <= hy && lz <= hz) {
+          const bool second = ly + 1 <= hy;
+          T v0, v1;
+          PairFill<T, A>::pair(a, lx, ly, lz, second, v0, v1);
+          const int bi = ox + R::nx * (2 * py + R::ny * oz);
+          buf[bi] = v0;
+          if (second) buf[bi + R::nx] = v1;
+        }
+      }
+    } else {
+#pragma unroll 2
+      for (int i = tid; i < R::n; i += kTileThreads) {
+        const int lx = R::xl + i % R::nx;
+        const int r = i / R::nx;
+        const int ly = R::yl + r % R::ny;
+        const int lz = R::zl + r / R::ny;
+        if (lx <= hx && ly <= hy && lz <= hz) buf[i] = a.eval(lx, ly, lz);
+      }
     }
   }
 #endif
@@ -258,6 +301,52 @@ struct SplitBox {
 typedef NEBO_FIRST_IJK(-1, 0, 0)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(1, 0, 0) Line3X;
 typedef NEBO_FIRST_IJK(0, -1, 0)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(0, 1, 0) Line3Y;
 typedef NEBO_FIRST_IJK(0, 0, -1)::NEBO_ADD_IJK(0, 0, 0)::NEBO_ADD_IJK(0, 0, 1) Line3Z;
+
+#ifdef __CUDACC__
+// The line sums' shared pairs: s(p) = v(p-1) + m and s(p+1) = m + v(p+2) with m = v(p) + v(p+1),
+// 3 additions for two sums instead of 4 (reassociating builds only: the split box is theirs).
+template <typename T, class F>
+struct PairFill<T, DSumStencil<T, Line3X, F>> {  // x sums of any functor, read point by point
+  static constexpr int axis = 1;
+  static __device__ __forceinline__ void pair(const DSumStencil<T, Line3X, F>& s, int x, int y, int z, bool second,
+                                              T& v0, T& v1) {
+    const T m = Arith<T>::add(s.a.eval(x, y, z), s.a.eval(x + 1, y, z));
+    v0 = Arith<T>::add(s.a.eval(x - 1, y, z), m);
+    v1 = second ? Arith<T>::add(m, s.a.eval(x + 2, y, z)) : m;
+  }
+};
+template <typename T, class X, class RB, int OffB, int RoundB>
+struct PairFill<T, DStencilSmem<T, Line3Y, X, RB, OffB, RoundB, kSum>> {  // y sums of a buffer
+  static constexpr int axis = 2;
+  static __device__ __forceinline__ void pair(const DStencilSmem<T, Line3Y, X, RB, OffB, RoundB, kSum>&, int x, int y,
+                                              int z, bool second, T& v0, T& v1) {
+    const SmemView<T, RB, OffB> b;
+    const T m = Arith<T>::add(b.eval(x, y, z), b.eval(x, y + 1, z));
+    v0 = Arith<T>::add(b.eval(x, y - 1, z), m);
+    v1 = second ? Arith<T>::add(m, b.eval(x, y + 2, z)) : m;
+  }
+};
+
+// The output pass evaluates two z-neighbouring cells at once: two evaluations, except for the z
+// sums of a split box filter (the same shared middle pair) and a factor applied to them.
+template <typename T, class D>
+struct PairZ {
+  static __device__ __forceinline__ void eval(const D& f, int x, int y, int z, T& v0, T& v1) {
+    v0 = f.eval(x, y, z);
+    v1 = f.eval(x, y, z + 1);
+  }
+};
+template <typename T, class X, class RB, int OffB, int RoundB>
+struct PairZ<T, DStencilSmem<T, Line3Z, X, RB, OffB, RoundB, kSum>> {
+  static __device__ __forceinline__ void eval(const DStencilSmem<T, Line3Z, X, RB, OffB, RoundB, kSum>&, int x, int y,
+                                              int z, T& v0, T& v1) {
+    const SmemView<T, RB, OffB> b;
+    const T m = Arith<T>::add(b.eval(x, y, z), b.eval(x, y, z + 1));
+    v0 = Arith<T>::add(b.eval(x, y, z - 1), m);
+    v1 = Arith<T>::add(m, b.eval(x, y, z + 2));
+  }
+};
+#endif
 
 template <typename T, class Pts, class A, class R, int Off>
 struct Tile<DSumStencil<T, Pts, A>, R, Off, typename std::enable_if<SplitBox<Pts>::value>::type> {
@@ -598,8 +687,15 @@ __global__ void __launch_bounds__(kTileThreads) nebo_tiled_assign_kernel(T* __re
   const int lx = (int)threadIdx.x, ly = (int)threadIdx.y;
   if (lx >= nx || ly >= ny) return;
   T* o = out + ((long)x0 + lx) + (long)sy * (y0 + ly) + sz * z0;
+  int lz = 0;
 #pragma unroll 1
-  for (int lz = 0; lz < nz; ++lz) o[sz * lz] = f.eval(lx, ly, lz);
+  for (; lz + 1 < nz; lz += 2) {
+    T v0, v1;
+    PairZ<T, DT>::eval(f, lx, ly, lz, v0, v1);
+    o[sz * lz] = v0;
+    o[sz * (lz + 1)] = v1;
+  }
+  if (lz < nz) o[sz * lz] = f.eval(lx, ly, lz);
 }
 #endif
 
