@@ -6,8 +6,9 @@
 // (spatialops/structured/stencil/StencilBuilder.cpp:52-220).  Evaluated as written each costs a
 // multiply and a fused multiply-add; as s * (a[p0] +- a[p1]) it costs one add, with the factor s
 // carried upward: a product's factor is the product of its operands' factors, a quotient's their
-// quotient, a product with a scalar takes the scalar into the factor, and a sum a + b becomes
-// fma(s_b / s_a, b', a') with the factor s_a.  Factors are applied where a value is needed (a
+// quotient, a product with a scalar takes the scalar into the factor; a sum of operands without
+// factors stays a plain sum, one with a factor s enters as s * x in one FMA, and two with factors
+// become fma(s_b / s_a, b', a') with the factor s_a.  Factors are applied where a value is needed (a
 // function's argument, a comparison, a cond branch, a stencil of 3 or more points, which takes
 // its argument's factor into its weights) and at the root.  The heat expression
 //   T + dt * (DivX(InterpX(lambda) * GradX(T)) + DivY(...) + DivZ(...))
@@ -66,6 +67,21 @@ struct DFmaSum {
   __device__ __forceinline__ T eval(int x, int y, int z) const {
     const T rr = std::is_same<Op, OpSub>::value ? -(T)r : (T)r;
     return nebo_fma(rr, b.eval(x, y, z), a.eval(x, y, z));
+  }
+#endif
+  NEBO_TWO_CHILDREN(a, b)
+};
+
+// r * a + b (OpAdd) or r * a - b (OpSub): one FMA
+template <class Op, typename T, class A, class B>
+struct DFmaSumL {
+  A a;
+  B b;
+  double r;
+#ifdef __CUDACC__
+  __device__ __forceinline__ T eval(int x, int y, int z) const {
+    const T bb = b.eval(x, y, z);
+    return nebo_fma((T)r, a.eval(x, y, z), std::is_same<Op, OpSub>::value ? -bb : bb);
   }
 #endif
   NEBO_TWO_CHILDREN(a, b)
@@ -198,21 +214,49 @@ struct Factor<DBin<OpDiv, T, A, B>, typename std::enable_if<Floating<T>::value>:
   }
 };
 
-// a +- b: the left operand's factor, the right operand's relative factor in one FMA
+// a +- b.  Operands without factors stay a plain sum (so the compiler still fuses a product
+// operand into an FMA); one operand with a factor r enters as r * x in one FMA and the sum keeps
+// factor 1; two operands with factors keep the left one's and scale the right one by their ratio.
 template <class Op, typename T, class A, class B>
 struct Factor<DBin<Op, T, A, B>, typename std::enable_if<Floating<T>::value && (std::is_same<Op, OpAdd>::value ||
                                                                              std::is_same<Op, OpSub>::value)>::type> {
   typedef Factor<A> FA;
   typedef Factor<B> FB;
-  typedef DFmaSum<Op, T, typename FA::type, typename FB::type> type;
-  static constexpr bool unit = FA::unit;
+  typedef typename FA::type TA;
+  typedef typename FB::type TB;
+  static constexpr int kind = FA::unit && FB::unit ? 0 : FA::unit ? 1 : FB::unit ? 2 : 3;
+  typedef typename std::conditional<
+      kind == 0, DBin<Op, T, TA, TB>,
+      typename std::conditional<kind == 2, DFmaSumL<Op, T, TA, TB>, DFmaSum<Op, T, TA, TB>>::type>::type type;
+  static constexpr bool unit = kind != 3;
   static type make(const DBin<Op, T, A, B>& d, double& s, bool& ok) {
     double sa, sb;
-    type f{FA::make(d.a, sa, ok), FB::make(d.b, sb, ok), 1.0};
-    f.r = sb / sa;
+    const TA fa = FA::make(d.a, sa, ok);
+    const TB fb = FB::make(d.b, sb, ok);
+    return build(fa, fb, sa, sb, s, ok, std::integral_constant<int, kind>());
+  }
+
+ private:
+  static type build(const TA& fa, const TB& fb, double, double, double& s, bool&, std::integral_constant<int, 0>) {
+    s = 1.0;
+    return type{fa, fb};
+  }
+  static type build(const TA& fa, const TB& fb, double, double sb, double& s, bool& ok, std::integral_constant<int, 1>) {
+    s = 1.0;
+    ok = ok && clean_factor(sb);
+    return type{fa, fb, sb};
+  }
+  static type build(const TA& fa, const TB& fb, double sa, double, double& s, bool& ok, std::integral_constant<int, 2>) {
+    s = 1.0;
+    ok = ok && clean_factor(sa);
+    return type{fa, fb, sa};
+  }
+  static type build(const TA& fa, const TB& fb, double sa, double sb, double& s, bool& ok,
+                    std::integral_constant<int, 3>) {
     s = sa;
-    ok = ok && clean_factor(sa) && clean_factor(f.r);
-    return f;
+    const double r = sb / sa;
+    ok = ok && clean_factor(sa) && clean_factor(r);
+    return type{fa, fb, r};
   }
 };
 
@@ -342,6 +386,14 @@ struct Tile<DFmaSum<Op, T, A, B>, R, Off> {
   typedef DFmaSum<Op, T, typename TA::type, typename TB::type> type;
   enum { end = TB::end, rounds = cmax(TA::rounds, TB::rounds) };
   static type make(const DFmaSum<Op, T, A, B>& d) { return type{TA::make(d.a), TB::make(d.b), d.r}; }
+};
+template <class Op, typename T, class A, class B, class R, int Off>
+struct Tile<DFmaSumL<Op, T, A, B>, R, Off> {
+  typedef Tile<A, R, Off> TA;
+  typedef Tile<B, R, TA::end> TB;
+  typedef DFmaSumL<Op, T, typename TA::type, typename TB::type> type;
+  enum { end = TB::end, rounds = cmax(TA::rounds, TB::rounds) };
+  static type make(const DFmaSumL<Op, T, A, B>& d) { return type{TA::make(d.a), TB::make(d.b), d.r}; }
 };
 // a signed pair of a leaf reads its neighbours directly; of an expression, from shared memory
 template <typename T, class Pts, class A, class R, int Off>

@@ -356,14 +356,19 @@ struct NeboBoundaryConditionBuilder {
     std::vector<IntVec> reads;
     collect_points<PhiPts>(reads);
     const IntVec gp = GPt::int_vec();
-    for (const IntVec& m : pts) {
-      const IntVec p = m - shift;
+    // every condition bounds one coordinate of one point: the mask's per-axis extremes decide
+    // them all, and only a failure walks the points (for the first one that reaches out)
+    auto inside = [&](const IntVec& p) {
       bool ok = true;
       for (int i = 0; i < 3; ++i) {
         ok = ok && p[i] >= plo[i] && p[i] < phi_hi[i] && p[i] + gp[i] >= glo[i] && p[i] + gp[i] < ghi[i];
         for (const IntVec& q : reads) ok = ok && p[i] + q[i] >= plo[i] && p[i] + q[i] < phi_hi[i];
       }
-      if (!ok) {
+      return ok;
+    };
+    if (!inside(mask.point_min() - shift) || !inside(mask.point_max() - shift)) {
+      for (const IntVec& m : pts) {
+        if (inside(m - shift)) continue;
         std::ostringstream msg;
         msg << "Nebo error in Nebo Boundary Condition:\nmask point (" << m[0] << "," << m[1] << "," << m[2]
             << ") reaches outside the fields' valid cells";

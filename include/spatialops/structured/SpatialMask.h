@@ -38,6 +38,7 @@ class SpatialMask {
   GhostData ghosts_, validGhosts_;
   std::shared_ptr<std::vector<IntVec>> points_;
   std::shared_ptr<nebo_detail::MaskStore> store_;
+  IntVec pmin_, pmax_;  // per-axis bounds of the points (when there are any)
 
   void build() {
     store_ = std::make_shared<nebo_detail::MaskStore>();
@@ -49,10 +50,15 @@ class SpatialMask {
     nebo_detail::throw_status(nebo_memset(w, 0, store_->nwords * 4, nullptr), "SpatialMask allocation");
     std::vector<int32_t> host;
     host.reserve(points_->size() * 3);
+    if (!points_->empty()) pmin_ = pmax_ = points_->front();
     for (const IntVec& p : *points_) {
       host.push_back(p[0]);
       host.push_back(p[1]);
       host.push_back(p[2]);
+      for (int i = 0; i < 3; ++i) {
+        pmin_[i] = p[i] < pmin_[i] ? p[i] : pmin_[i];
+        pmax_[i] = p[i] > pmax_[i] ? p[i] : pmax_[i];
+      }
     }
     store_->npoints = (int)points_->size();
     if (!host.empty()) {
@@ -102,6 +108,9 @@ class SpatialMask {
   const uint32_t* mask_values(short int = GPU_INDEX) const { return store_->words; }
   const int32_t* device_points() const { return store_->points; }
   int num_points() const { return store_->npoints; }
+  // the smallest and largest coordinate of the points along each axis (num_points() > 0)
+  const IntVec& point_min() const { return pmin_; }
+  const IntVec& point_max() const { return pmax_; }
   long interior_origin() const {
     return (long)(maskWindow_.offset(0) + validGhosts_.get_minus(0)) +
            (long)maskWindow_.glob_dim(0) *

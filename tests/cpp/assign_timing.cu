@@ -8,6 +8,12 @@
 //   filter  f <<= BoxFilter_XX(out)
 //   heat    Tn <<= T + dt * (DivX(InterpX(lam) * GradX(T)) + DivY(...) + DivZ(...))
 //           (examples/heat_equation.cpp:216-220 folded into the Euler update)
+//   next    the drop-in's widened rows at the same size:
+//           masked_assign(mask, out, a * b) over 5 % of the cells (a point list) and the same
+//           values by a full-sweep cond(mask, a * b)(out);
+//           out <<= apply_pointwise<F>(a, b, c, d), F = (a + b) * c + d, and the same as an
+//           expression;
+//           NeboBoundaryConditionBuilder<GradX> on the x = -1 face (one 256 x 256 plane);
 // and, through the C ABI on the same fields, nebo_deep_chain (out and filt), nebo_box_filter and
 // nebo_heat_step.  Prints one JSON object: per expression the milliseconds per launch (CUDA
 // events around `reps` launches after 3 warm-up launches; every input is larger than L2), the
@@ -43,6 +49,10 @@ static const char* kMath = "CUDA exp/sin";
 #else
 static const char* kMath = "fixed-point exp/sin";
 #endif
+
+struct TimingSum4 {
+  NEBO_HD double operator()(double a, double b, double c, double d) const { return (a + b) * c + d; }
+};
 
 static void check(int rc, const char* what) {
   if (rc != 0) {
@@ -224,6 +234,41 @@ int main(int argc, char** argv) {
         }
     out.add("heat_assign", t_heat, cells, 24.0, mm > 0 ? d / mm : d);
     out.add("heat_hand", t_hand, cells, 24.0, 0.0);
+  }
+  if (all || which == "next") {
+    typedef BasicOpTypes<SVolField> OS;
+    SVolField a = make_field<SVolField>(n, 7, -1.0, 1.0), b = make_field<SVolField>(n, 8, -1.0, 1.0);
+    SVolField c = make_field<SVolField>(n, 9, -1.0, 1.0), d = make_field<SVolField>(n, 10, -1.0, 1.0);
+    SVolField o1 = zero_field<SVolField>(n), o2 = zero_field<SVolField>(n);
+    std::vector<IntVec> pts;
+    for (int z = 0; z < n; ++z)
+      for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x)
+          if (catalog::uniform_pm1(12, (uint64_t)((z * n + y) * n + x)) < -0.9) pts.push_back(IntVec(x, y, z));
+    SpatialMask<SVolField> m(o1, pts);
+    const double npts = (double)pts.size();
+    // point list: per point a, b read, out written (24 B) and its 3 ints (12 B)
+    const double t_masked = time_ms([&] { masked_assign(m, o1, a * b); }, reps);
+    const double t_sweep = time_ms([&] { o2 <<= cond(m, a * b)(o2); }, reps);
+    const double d_mask = max_rel_diff(o1, o2);
+    out.add("masked_assign_5pct", t_masked, npts, 36.0, d_mask);
+    out.add("masked_full_sweep_cond", t_sweep, cells, 16.0 + 1.0 / 8.0 + 2.0 * npts / cells * 8.0, 0.0);
+    const double t_apply = time_ms([&] { o1 <<= apply_pointwise<TimingSum4>(a, b, c, d); }, reps);
+    const double t_expr = time_ms([&] { o2 <<= (a + b) * c + d; }, reps);
+    out.add("apply_pointwise_4", t_apply, cells, 40.0, max_rel_diff(o1, o2));
+    out.add("apply_pointwise_as_expression", t_expr, cells, 40.0, 0.0);
+    // a boundary condition on one face: 256 x 256 points, phi read at the stencil's two points
+    // and written at one, gamma read (32 B per point)
+    typedef OS::GradX Op;
+    typedef Op::DestFieldType SX;
+    NeboBoundaryConditionBuilder<Op> bc(*opdb.retrieve_operator<Op>());
+    SX gamma = make_field<SX>(n, 11, -1.0, 1.0), proto = zero_field<SX>(n);
+    std::vector<IntVec> face;
+    for (int z = 0; z < n; ++z)
+      for (int y = 0; y < n; ++y) face.push_back(IntVec(0, y, z));
+    SpatialMask<SX> fm(proto, face);
+    const double t_bc = time_ms([&] { bc(fm, a, gamma, true); }, reps);
+    out.add("bc_gradx_face", t_bc, (double)face.size(), 32.0, 0.0);
   }
   int dev = 0;
   cudaGetDevice(&dev);
