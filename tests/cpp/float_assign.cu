@@ -5,6 +5,9 @@
 //
 //   float_assign [n]      (default 20)
 //
+// The expressions: the heat update (factored), a pair with unequal coefficients (kept as
+// written), a nested chain (composed), and a factored operand minus an unfactored one.
+//
 // Prints one JSON object: per expression the relative max-norm difference between the FP32 and
 // the FP64 results over the written cells.
 #include <spatialops/Nebo.h>
@@ -93,6 +96,11 @@ static Results<T> run(int n) {
     out <<= o.ix(o.gx(o.ix(a))) * lam;
     keep(out);
   }
+  {  // a factored left operand minus an unfactored one (r * x - y in one FMA)
+    SF<T> out = sentinel_field<T>(n);
+    out <<= o.gx(a) * lam - a;
+    keep(out);
+  }
   return r;
 }
 
@@ -101,7 +109,7 @@ int main(int argc, char** argv) {
   if (n < 8) return 1;
   const Results<double> d = run<double>(n);
   const Results<float> f = run<float>(n);
-  const char* names[] = {"heat_update", "unequal_pair", "composed_chain"};
+  const char* names[] = {"heat_update", "unequal_pair", "composed_chain", "left_factor_difference"};
   std::string json = "{";
   for (size_t e = 0; e < d.out.size(); ++e) {
     double diff = 0.0, mag = 0.0;
