@@ -3,7 +3,8 @@ expressions on FP64 fields with the FP32 inputs rounded from the FP64 ones: the 
 constant factoring on float: signed pairs, FMA sums), a pair with unequal coefficients (the
 factoring's fallback), a nested chain (the stencil composition) and a factored operand minus an
 unfactored one (r * x - y in one FMA).  The written-cell sets must
-be identical and the values within 1e-5 relative max-norm (FP32 rounding)."""
+be identical and the values within 1e-5 relative max-norm (FP32 rounding); the FP64 results must
+equal direct host loops of the expressions to 1e-13."""
 import json
 import os
 import subprocess
@@ -26,3 +27,4 @@ def test_float_assign_matches_double(n):
         print(n, name, e)
         assert e["written"] > 0 and e["write_set_mismatch"] == 0, (name, e)
         assert e["rel_diff"] <= 1e-5, (name, e)
+        assert e["fp64_rel_diff_host"] <= 1e-13, (name, e)
