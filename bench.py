@@ -692,6 +692,7 @@ def part_dropin(bus):
     d = json.loads(r.stdout.strip().splitlines()[-1])
     d["clocks"] = clocks
     d["deep_assign_over_hand_chain"] = d["deep_assign"]["ms"] / d["deep_hand_chain"]["ms"]
+    d["filter_assign_over_hand"] = d["filter_assign"]["ms"] / d["filter_hand"]["ms"]
     d["heat_assign_over_hand"] = d["heat_assign"]["ms"] / d["heat_hand"]["ms"]
     return d
 
