@@ -410,14 +410,16 @@ class AdjointWL:
         self.J, self.gT, self.gl = self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt,
                                                         products=self.products)
 
-    def gradient_ms(self, products, checkpoint_every=0):
-        """Device time of one gradient with the given face-product precision and checkpoints."""
+    def gradient_ms(self, products, checkpoint_every=0, forward="f64"):
+        """Device time of one gradient with the given face-product precision, checkpoints and
+        forward-state precision."""
         import torch
 
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record()
-        self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt, checkpoint_every, products=products)
+        self.N.heat_gradient(self.T0, self.L, self.Tt, self.nsteps, self.dt, checkpoint_every, products=products,
+                             forward=forward)
         e1.record()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
@@ -668,13 +670,19 @@ def part_adjoint(N, bus):
     g32 = W.gradient_ms("f32")
     W.gradient_ms("f32", N.CHECKPOINT_AUTO)  # warm: the pool grows to hold every state
     gall = W.gradient_ms("f32", N.CHECKPOINT_AUTO)
+    W.gradient_ms("f64", forward="f32")  # warm
+    gf32 = W.gradient_ms("f64", forward="f32")
     clocks = sampler.stop()
     del W
     torch.cuda.empty_cache()
     return {"workload": adjoint_label(192, 500), "forward_ms": fwd, "gradient_ms_fp64": g64,
             "gradient_ms_f32_products": g32, "gradient_ms_every_state_kept": gall,
             "adjoint_over_forward_fp64": g64 / fwd, "adjoint_over_forward_f32_products": g32 / fwd,
-            "adjoint_over_forward_every_state_kept": gall / fwd, "checkpoints": "ceil(sqrt(500)) = 23",
+            "adjoint_over_forward_every_state_kept": gall / fwd,
+            "gradient_ms_fp32_forward": gf32, "adjoint_over_forward_fp32_forward": gf32 / fwd,
+            "fp32_forward_note": "FP32 forward states and checkpoints, FP64 adjoint and products; "
+                                 "the ratio is against the FP64 forward run",
+            "checkpoints": "ceil(sqrt(500)) = 23",
             "clocks": clocks}
 
 
