@@ -703,15 +703,15 @@ def part_dropin(bus):
     d["filter_assign_over_hand"] = d["filter_assign"]["ms"] / d["filter_hand"]["ms"]
     d["heat_assign_over_hand"] = d["heat_assign"]["ms"] / d["heat_hand"]["ms"]
     # the transport configuration written in Nebo (FP64, 512^3 + 2 ghosts), one RK2 step
-    exe_t = os.path.join(REPO, "tests", "cpp", "_build", "transport_dropin")
+    exe_t = os.path.join(REPO, "tests", "cpp", "_build", "configs_dropin")
     if os.path.exists(exe_t):
-        r = subprocess.run([exe_t, "time", "512", "3"], capture_output=True, text=True, timeout=600)
+        r = subprocess.run([exe_t, "transport-time", "512", "3"], capture_output=True, text=True, timeout=600)
         if r.returncode == 0:
             t = json.loads(r.stdout.strip().splitlines()[-1])
             t["assign_over_hand"] = t["transport_assign"]["ms_per_rk2_step"] / t["transport_hand"]["ms_per_rk2_step"]
             d["transport"] = t
         else:
-            d["transport"] = {"unavailable": f"transport_dropin exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+            d["transport"] = {"unavailable": f"configs_dropin exited {r.returncode}: {r.stderr.strip()[-200:]}"}
     return d
 
 

@@ -74,8 +74,9 @@ PROGRAMS = {
     "assign_timing_libm": ("assign_timing.cu", ["-DNEBO_CUDA_LIBM"]),
     # `<<=` on FP32 fields against FP64 (the lowering passes on float)
     "float_assign": ("float_assign.cu", []),
-    # the transport configuration written in Nebo (golden check and timing against the hand kernel)
-    "transport_dropin": ("transport_dropin.cu", []),
+    # the heat and transport configurations written in Nebo (golden checks, and the transport
+    # timed against the hand kernel)
+    "configs_dropin": ("configs_dropin.cu", []),
 }
 
 

@@ -1,13 +1,18 @@
-// The scalar-transport configuration written in Nebo, as the reference's users write it, through
-// the drop-in headers: per direction the face flux nu * Interp(lambda) * G4(phi) - u * cond(u >
-// 0, phi[i-1])(phi[i]) with user stencil builders (the 4th-order gradient {1, -27, 27, -1}/24 and
-// the one-point upwind reads), its divergence by the Gradient operators, and Heun's RK2 with
-// periodic ghost fills, the code that generated tests/golden/transport.npz from the reference's
-// own Nebo.
+// Two of the configurations written in Nebo, as the reference's users write them, through the
+// drop-in headers: the code that generated tests/golden/heat.npz and transport.npz from the
+// reference's own Nebo.
+//   heat       T' <<= T + dt * (DivX(InterpX(lambda) * GradX(T)) + DivY(...) + DivZ(...)) with the
+//              operator database's operators, periodic ghost fills, then nebo_sum/max/norm(T)
+//   transport  per direction the face flux nu * Interp(lambda) * G4(phi) - u * cond(u > 0,
+//              phi[i-1])(phi[i]) with user stencil builders (the 4th-order gradient
+//              {1, -27, 27, -1}/24 and the one-point upwind reads), its divergence by the Gradient
+//              operators, Heun's RK2 with periodic ghost fills
 //
-//   transport_dropin check <n> <steps> <dt> <nu> <phi> <u> <v> <w> <lam> <out>
-//       inputs and output are whole FP64 windows (2 ghost layers) as raw little-endian doubles
-//   transport_dropin time <n> <reps>
+//   configs_dropin heat <nx> <ny> <nz> <steps> <dt> <lam> <T0> <out>
+//       whole FP64 windows (1 ghost layer) as raw little-endian doubles; prints the reductions
+//   configs_dropin transport <n> <steps> <dt> <nu> <phi> <u> <v> <w> <lam> <out>
+//       whole FP64 windows (2 ghost layers)
+//   configs_dropin transport-time <n> <reps>
 //       one RK2 step through `<<=` against nebo_transport_run (the hand-fused FP64 stages) on the
 //       same fields; prints one JSON object
 #include <spatialops/Nebo.h>
@@ -34,9 +39,8 @@ static void check(int rc, const char* what) {
 }
 
 template <typename F>
-static F make_field(int n, const std::vector<double>* v) {
-  const IntVec N(n, n, n);
-  const GhostData g(2);
+static F make_field(IntVec N, int ghost, const std::vector<double>* v) {
+  const GhostData g(ghost);
   const BoundaryCellInfo bc = BoundaryCellInfo::build<F>(false, false, false);
   const MemoryWindow w = get_window_with_ghost(N, g, bc);
   std::vector<double> zero;
@@ -80,9 +84,11 @@ struct Transport {
   YVolField v;
   ZVolField w;
   Transport(int n_, double dt_, double nu_, const std::vector<double>* in[5])
-      : n(n_), dt(dt_), nu(nu_), phi(make_field<SVolField>(n_, in[0])), phi1(make_field<SVolField>(n_, nullptr)),
-        phin(make_field<SVolField>(n_, nullptr)), lam(make_field<SVolField>(n_, in[4])),
-        u(make_field<XVolField>(n_, in[1])), v(make_field<YVolField>(n_, in[2])), w(make_field<ZVolField>(n_, in[3])) {
+      : n(n_), dt(dt_), nu(nu_), phi(make_field<SVolField>(IntVec(n_, n_, n_), 2, in[0])),
+        phi1(make_field<SVolField>(IntVec(n_, n_, n_), 2, nullptr)),
+        phin(make_field<SVolField>(IntVec(n_, n_, n_), 2, nullptr)),
+        lam(make_field<SVolField>(IntVec(n_, n_, n_), 2, in[4])), u(make_field<XVolField>(IntVec(n_, n_, n_), 2, in[1])),
+        v(make_field<YVolField>(IntVec(n_, n_, n_), 2, in[2])), w(make_field<ZVolField>(IntVec(n_, n_, n_), 2, in[3])) {
     build_stencils(n, n, n, (double)n, (double)n, (double)n, opdb);
     fill_periodic(lam);
     fill_periodic(u);
@@ -125,9 +131,48 @@ struct Transport {
   }
 };
 
+static int run_heat(int argc, char** argv) {
+  const IntVec N(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]));
+  const int steps = std::atoi(argv[5]);
+  const double dt = std::strtod(argv[6], NULL);
+  const size_t np = (size_t)(N[0] + 2) * (N[1] + 2) * (N[2] + 2);
+  const std::vector<double> vl = read_doubles(argv[7], np), vt = read_doubles(argv[8], np);
+  SVolField lam = make_field<SVolField>(N, 1, &vl), T0 = make_field<SVolField>(N, 1, &vt);
+  SVolField T1 = make_field<SVolField>(N, 1, nullptr);
+  OperatorDatabase opdb;
+  build_stencils(N[0], N[1], N[2], (double)N[0], (double)N[1], (double)N[2], opdb);
+  typedef BasicOpTypes<SVolField> OT;
+  const OT::InterpC2FX& ix = *opdb.retrieve_operator<OT::InterpC2FX>();
+  const OT::InterpC2FY& iy = *opdb.retrieve_operator<OT::InterpC2FY>();
+  const OT::InterpC2FZ& iz = *opdb.retrieve_operator<OT::InterpC2FZ>();
+  const OT::GradX& gx = *opdb.retrieve_operator<OT::GradX>();
+  const OT::GradY& gy = *opdb.retrieve_operator<OT::GradY>();
+  const OT::GradZ& gz = *opdb.retrieve_operator<OT::GradZ>();
+  const OT::DivX& dx = *opdb.retrieve_operator<OT::DivX>();
+  const OT::DivY& dy = *opdb.retrieve_operator<OT::DivY>();
+  const OT::DivZ& dz = *opdb.retrieve_operator<OT::DivZ>();
+  fill_periodic(lam);
+  SVolField* cur = &T0;
+  SVolField* nxt = &T1;
+  for (int s = 0; s < steps; ++s) {
+    fill_periodic(*cur);
+    *nxt <<= *cur + dt * (dx(ix(lam) * gx(*cur)) + dy(iy(lam) * gy(*cur)) + dz(iz(lam) * gz(*cur)));
+    std::swap(cur, nxt);
+  }
+  fill_periodic(*cur);
+  const double* p = cur->field_values(CPU_INDEX);
+  FILE* fp = std::fopen(argv[9], "wb");
+  if (!fp || std::fwrite(p, sizeof(double), np, fp) != np) return 1;
+  std::fclose(fp);
+  std::printf("{\"sum\": %.17g, \"max\": %.17g, \"norm\": %.17g}\n", nebo_sum(*cur), nebo_max(*cur),
+              nebo_norm(*cur));
+  return 0;
+}
+
 int main(int argc, char** argv) {
   const std::string mode = argc > 1 ? argv[1] : "";
-  if (mode == "check" && argc >= 12) {
+  if (mode == "heat" && argc >= 10) return run_heat(argc, argv);
+  if (mode == "transport" && argc >= 12) {
     const int n = std::atoi(argv[2]), steps = std::atoi(argv[3]);
     const double dt = std::strtod(argv[4], NULL), nu = std::strtod(argv[5], NULL);
     const size_t np = (size_t)(n + 4) * (n + 4) * (n + 4);
@@ -146,7 +191,7 @@ int main(int argc, char** argv) {
     std::fclose(fp);
     return 0;
   }
-  if (mode == "time" && argc >= 4) {
+  if (mode == "transport-time" && argc >= 4) {
     const int n = std::atoi(argv[2]), reps = std::atoi(argv[3]);
     const size_t np = (size_t)(n + 4) * (n + 4) * (n + 4);
     std::vector<double> vals[5];
@@ -191,6 +236,6 @@ int main(int argc, char** argv) {
                 n, reps, t_assign, cells / (t_assign * 1e-3) / 1e9, t_hand, cells / (t_hand * 1e-3) / 1e9);
     return 0;
   }
-  std::fprintf(stderr, "usage: transport_dropin check|time ...\n");
+  std::fprintf(stderr, "usage: configs_dropin heat|transport|transport-time ...\n");
   return 1;
 }
