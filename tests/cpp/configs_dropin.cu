@@ -1,8 +1,10 @@
-// Two of the configurations written in Nebo, as the reference's users write them, through the
-// drop-in headers: the code that generated tests/golden/heat.npz and transport.npz from the
-// reference's own Nebo.
+// Three of the configurations written in Nebo, as the reference's users write them, through the
+// drop-in headers: the code that generated tests/golden/heat.npz, deep.npz and transport.npz
+// from the reference's own Nebo.
 //   heat       T' <<= T + dt * (DivX(InterpX(lambda) * GradX(T)) + DivY(...) + DivZ(...)) with the
 //              operator database's operators, periodic ghost fills, then nebo_sum/max/norm(T)
+//   deep       out <<= cond(mask, 0.0)(Interp_SX(Grad_XS(Interp_SX(a))) * exp(b) + sin(c)),
+//              filt <<= BoxFilter(out), then nebo_sum/max/norm(filt)
 //   transport  per direction the face flux nu * Interp(lambda) * G4(phi) - u * cond(u > 0,
 //              phi[i-1])(phi[i]) with user stencil builders (the 4th-order gradient
 //              {1, -27, 27, -1}/24 and the one-point upwind reads), its divergence by the Gradient
@@ -10,6 +12,8 @@
 //
 //   configs_dropin heat <nx> <ny> <nz> <steps> <dt> <lam> <T0> <out>
 //       whole FP64 windows (1 ghost layer) as raw little-endian doubles; prints the reductions
+//   configs_dropin deep <nx> <ny> <nz> <a> <b> <c> <points> <out> <filt>
+//       a SVol, b, c XVol windows (1 ghost layer); points: int32 (x, y, z) triples
 //   configs_dropin transport <n> <steps> <dt> <nu> <phi> <u> <v> <w> <lam> <out>
 //       whole FP64 windows (2 ghost layers)
 //   configs_dropin transport-time <n> <reps>
@@ -169,9 +173,56 @@ static int run_heat(int argc, char** argv) {
   return 0;
 }
 
+static void write_doubles(const char* path, const double* p, size_t n) {
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp || std::fwrite(p, sizeof(double), n, fp) != n) {
+    std::fprintf(stderr, "cannot write %s\n", path);
+    std::exit(1);
+  }
+  std::fclose(fp);
+}
+
+static int run_deep(int argc, char** argv) {
+  const IntVec N(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]));
+  const size_t ns = (size_t)(N[0] + 2) * (N[1] + 2) * (N[2] + 2);
+  SVolField a = make_field<SVolField>(N, 1, nullptr);
+  XVolField b = make_field<XVolField>(N, 1, nullptr);
+  const size_t nx = b.window_with_ghost().glob_npts();
+  const std::vector<double> va = read_doubles(argv[5], ns), vb = read_doubles(argv[6], nx), vc = read_doubles(argv[7], nx);
+  a = make_field<SVolField>(N, 1, &va);
+  b = make_field<XVolField>(N, 1, &vb);
+  XVolField c = make_field<XVolField>(N, 1, &vc);
+  XVolField out = make_field<XVolField>(N, 1, nullptr), filt = make_field<XVolField>(N, 1, nullptr);
+  FILE* fp = std::fopen(argv[8], "rb");
+  std::vector<int32_t> p;
+  int32_t q;
+  while (fp && std::fread(&q, sizeof q, 1, fp) == 1) p.push_back(q);
+  if (fp) std::fclose(fp);
+  std::vector<IntVec> pts;
+  for (size_t i = 0; i + 2 < p.size(); i += 3) pts.push_back(IntVec(p[i], p[i + 1], p[i + 2]));
+  SpatialMask<XVolField> mask(out, pts);
+  OperatorDatabase opdb;
+  build_stencils(N[0], N[1], N[2], (double)N[0], (double)N[1], (double)N[2], opdb);
+  typedef OperatorTypeBuilder<Interpolant, SVolField, XVolField>::type IS2X;
+  typedef OperatorTypeBuilder<Gradient, XVolField, SVolField>::type GX2S;
+  typedef OperatorTypeBuilder<Filter, XVolField, XVolField>::type Box;
+  const IS2X& is2x = *opdb.retrieve_operator<IS2X>();
+  const GX2S& gx2s = *opdb.retrieve_operator<GX2S>();
+  const Box& box = *opdb.retrieve_operator<Box>();
+  out <<= 0.0;
+  out <<= cond(mask, 0.0)(is2x(gx2s(is2x(a))) * exp(b) + sin(c));
+  filt <<= 0.0;
+  filt <<= box(out);
+  write_doubles(argv[9], out.field_values(CPU_INDEX), nx);
+  write_doubles(argv[10], filt.field_values(CPU_INDEX), nx);
+  std::printf("{\"sum\": %.17g, \"max\": %.17g, \"norm\": %.17g}\n", nebo_sum(filt), nebo_max(filt), nebo_norm(filt));
+  return 0;
+}
+
 int main(int argc, char** argv) {
   const std::string mode = argc > 1 ? argv[1] : "";
   if (mode == "heat" && argc >= 10) return run_heat(argc, argv);
+  if (mode == "deep" && argc >= 11) return run_deep(argc, argv);
   if (mode == "transport" && argc >= 12) {
     const int n = std::atoi(argv[2]), steps = std::atoi(argv[3]);
     const double dt = std::strtod(argv[4], NULL), nu = std::strtod(argv[5], NULL);
@@ -236,6 +287,6 @@ int main(int argc, char** argv) {
                 n, reps, t_assign, cells / (t_assign * 1e-3) / 1e9, t_hand, cells / (t_hand * 1e-3) / 1e9);
     return 0;
   }
-  std::fprintf(stderr, "usage: configs_dropin heat|transport|transport-time ...\n");
+  std::fprintf(stderr, "usage: configs_dropin heat|deep|transport|transport-time ...\n");
   return 1;
 }
