@@ -601,6 +601,26 @@ def part_heat(N, bus, peak):
 
     s64, s32 = state_after(W, 50), state_after(W32, 50)
     err = float((s32 - s64).abs().max() / s64.abs().max())
+    # the heat configuration itself: 64^3 + 1 ghost, 100 FP64 steps in one nebo_heat_run (a CUDA
+    # graph of the 100 launches; the fields fit in L2, so launches and latency bound it)
+    from spatialops_gb300 import workloads as WL
+
+    # (dt = 0.15 / max lambda: the configuration's 0.2 grows the checkerboard mode x1.4 per step,
+    # and the 2400 timed steps would overflow)
+    lam64, T064, dt64 = WL.heat_inputs((64, 64, 64), cfl=0.15)
+    T64 = N.Field.from_numpy("SVol", T064, 1)
+    Tt64 = N.Field("SVol", (64, 64, 64), 1)
+    L64 = N.Field.from_numpy("SVol", lam64, 1)
+    c1 = {"workload": "heat 64^3 + 1 ghost, 100 FP64 Euler steps per call, dt = 0.15 / max lambda",
+          "steps_per_call": 100}
+    for mode in ("exact", "fixed"):
+        call = (lambda k: [N.heat_run(T64, Tt64, L64, 100, dt64) for _ in range(k)]) if mode == "exact" else \
+            (lambda k: [N.heat_run_ex(T64, Tt64, L64, 100, dt64, mode="fixed") for _ in range(k)])
+        call(2)
+        ms1, clocks1 = _timed(call, 10, bus)
+        c1[mode] = {"ms_per_call": ms1, "us_per_step": ms1 * 10.0,
+                    "gcell_upd_s": 64 ** 3 * 100 / (ms1 * 1e-3) / 1e9, "clocks": clocks1}
+    out["config_64cubed_100_steps"] = c1
     out["fp32"] = {"gcell_upd_s": cells / (ms32 * 1e-3) / 1e9, "ms_per_step": ms32, "steps": k32,
                    "alg_gbs": gbs32, "hbm_frac": gbs32 / peak, "clocks": clocks32,
                    "fp32_over_fp64": ms / ms32, "rel_err_50_steps_vs_fp64": err,
