@@ -117,16 +117,34 @@ __host__ __device__ __forceinline__ int fbits(float x) {
 __host__ __device__ __forceinline__ uint64_t uabs(int64_t a) { return a < 0 ? 0 - (uint64_t)a : (uint64_t)a; }
 
 // a * b / 2^62 for a, b >= 0: high word only (truncation below 4 units of 2^-62), and rounded to
-// nearest (the full 128-bit product plus one half, a < 2^64, a * b < 2^126).
+// nearest (the full 128-bit product plus one half, a < 2^64, a * b < 2^126).  ssq: a^2 / 2^62
+// truncated like umulq, from the signed high word (a^2 = |a|^2, so the same bits as umulq(|a|, |a|)).
 __host__ __device__ __forceinline__ uint64_t umulq(uint64_t a, uint64_t b) { return umulhi(a, b) << 2; }
+__host__ __device__ __forceinline__ uint64_t ssq(int64_t a) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__mul64hi(a, a) << 2;
+#else
+  return (uint64_t)(((__int128)a * (__int128)a) >> 64) << 2;
+#endif
+}
 __host__ __device__ __forceinline__ uint64_t umulx(uint64_t a, uint64_t b) {
   const uint64_t lo = a * b, lo2 = lo + (1ULL << 61);
   return ((umulhi(a, b) + (lo2 < lo)) << 2) | (lo2 >> 62);
 }
-// signed a * b / 2^62 (magnitudes rounded, then the sign)
+// signed a * b / 2^62 rounded to nearest (halves up), from the signed 128-bit product
+// (|a * b| < 2^125)
 __host__ __device__ __forceinline__ int64_t smulx(int64_t a, int64_t b) {
-  const uint64_t m = umulx(uabs(a), uabs(b));
-  return ((a ^ b) < 0) ? -(int64_t)m : (int64_t)m;
+#ifdef __CUDA_ARCH__
+  const uint64_t lo = (uint64_t)a * (uint64_t)b;
+  const int64_t hi = __mul64hi(a, b);
+#else
+  const __int128 pr = (__int128)a * (__int128)b;
+  const uint64_t lo = (uint64_t)pr;
+  const int64_t hi = (int64_t)(pr >> 64);
+#endif
+  const uint64_t lo2 = lo + (1ULL << 61);
+  const uint64_t hi2 = (uint64_t)hi + (lo2 < lo);
+  return (int64_t)((hi2 << 2) | (lo2 >> 62));
 }
 
 // A finite double with |v| < 2 at 2^62 (truncated toward zero; 0 for subnormals).
@@ -254,11 +272,10 @@ __host__ __device__ __forceinline__ double exp_fix(double x, const T& tb) {
   const int32_t r40 = (int32_t)(r >> 22);  // r at 2^40
   const int64_t g = SIXTH + (((int64_t)r40 * g2f) >> 13);               // 1/6 + r g2
   const int64_t h = HALF + (((int64_t)r40 * (int32_t)(g >> 30)) >> 10);  // 1/2 + r g
-  const uint64_t u = umulq(uabs(r), uabs(r));                           // r^2
+  const uint64_t u = ssq(r);                                            // r^2
   const int64_t p = r + (int64_t)umulq(u, (uint64_t)h);
-  const uint64_t tj = (uint64_t)tb.e(k & 255);
-  const uint64_t tp = umulx(tj, uabs(p));
-  const uint64_t y = p < 0 ? tj - tp : tj + tp;
+  const int64_t tj = tb.e(k & 255);
+  const uint64_t y = (uint64_t)(tj + smulx(tj, p));
   return from_bits(fix_to_bits(y, k >> 8));
 }
 
@@ -321,9 +338,8 @@ __host__ __device__ __forceinline__ double sin_fix(double x, const T& tb) {
     return from_bits((rb & 0x8000000000000000ULL) | (((uint64_t)(er - lz) << 52) + m));
   }
   const int64_t r = to_fix(r1) - mul_k<32>(k, A23_FIX94);
-  const uint64_t ra = uabs(r);
   int64_t sm1, cm1;
-  sin_cos_poly(umulq(ra, ra), &sm1, &cm1);
+  sin_cos_poly(ssq(r), &sm1, &cm1);
   const int64_t sr = r + smulx(r, sm1);  // sin r
   const int j = k & 127;
   const int64_t sj = tb.s(j), cj = tb.c(j);
