@@ -272,6 +272,12 @@ class Heat:
         self.host_red = torch.zeros(1, dtype=torch.float64).pin_memory()
         self.k = 0
 
+    def reset(self):
+        """T back to the initial state (ghosts filled)."""
+        self.T.tensor.copy_(self.host[0])
+        self.N.fill_periodic(self.T)
+        self.k = 0
+
     def step(self):
         a, b = (self.T, self.Tt) if self.k % 2 == 0 else (self.Tt, self.T)
         self.N.heat_step(a, b, self.L, self.dt)
@@ -571,15 +577,23 @@ def part_heat(N, bus, peak):
     gbs = BYTES_PER_CELL["heat"] * cells / (ms * 1e-3) / 1e9
     out = {"workload": heat_label(256, "f64"), "gcell_upd_s": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
            "steps": k, "alg_gbs": gbs, "hbm_frac": gbs / peak, "hbm_peak_gbs": peak, "clocks": clocks}
-    # the same step with the flux arithmetic on the integer pipe (NEBO_HEAT_FIXED_POINT): k steps in
-    # one nebo_heat_run_ex call (two exponent reductions per call, a 4-byte reset per step)
-    runfix = lambda kk: N.heat_run_ex(W.T, W.Tt, W.L, kk, W.dt, mode="fixed")
-    runfix(3)
-    msf, clocksf = _timed(runfix, k, bus)
-    gbsf = BYTES_PER_CELL["heat"] * cells / (msf * 1e-3) / 1e9
-    out["fixed_point"] = {"gcell_upd_s": cells / (msf * 1e-3) / 1e9, "ms_per_step": msf, "steps": k,
-                          "alg_gbs": gbsf, "hbm_frac": gbsf / peak, "clocks": clocksf,
-                          "accuracy": "within 1e-13 relative max-norm of the bit-exact form (tests)"}
+    # the same steps in the integer forms, k steps in one nebo_heat_run_ex call each, from the
+    # initial state (the exact steps above grew it x1.4 per step; from there the k steps below
+    # stay finite and inside the integer forms' ranges):
+    #   NEBO_HEAT_FIXED_POINT: FP64 state, fluxes on the integer pipe (two exponent reductions per
+    #   call, a 4-byte reset per step);
+    #   NEBO_HEAT_FIXED_STATE: the state itself in 64-bit integers (one conversion pass in, one
+    #   out per call, both inside the timed region)
+    for key, mode in (("fixed_point", "fixed"), ("fixed_state", "fixed_state")):
+        runm = lambda kk, m=mode: N.heat_run_ex(W.T, W.Tt, W.L, kk, W.dt, mode=m)
+        W.reset()
+        runm(3)
+        W.reset()
+        msf, clocksf = _timed(runm, k, bus)
+        gbsf = BYTES_PER_CELL["heat"] * cells / (msf * 1e-3) / 1e9
+        out[key] = {"gcell_upd_s": cells / (msf * 1e-3) / 1e9, "ms_per_step": msf, "steps": k,
+                    "alg_gbs": gbsf, "hbm_frac": gbsf / peak, "clocks": clocksf,
+                    "accuracy": "within 1e-13 relative max-norm of the bit-exact form (tests)"}
     # FP32 storage and arithmetic (the bandwidth path), and its error against the FP64 step after
     # 50 steps from the same state at the stable step 0.15 / max(lambda)
     W32 = Heat(N, 256, "f32")
@@ -613,9 +627,9 @@ def part_heat(N, bus, peak):
     L64 = N.Field.from_numpy("SVol", lam64, 1)
     c1 = {"workload": "heat 64^3 + 1 ghost, 100 FP64 Euler steps per call, dt = 0.15 / max lambda",
           "steps_per_call": 100}
-    for mode in ("exact", "fixed"):
+    for mode in ("exact", "fixed", "fixed_state"):
         call = (lambda k: [N.heat_run(T64, Tt64, L64, 100, dt64) for _ in range(k)]) if mode == "exact" else \
-            (lambda k: [N.heat_run_ex(T64, Tt64, L64, 100, dt64, mode="fixed") for _ in range(k)])
+            (lambda k, m=mode: [N.heat_run_ex(T64, Tt64, L64, 100, dt64, mode=m) for _ in range(k)])
         call(2)
         ms1, clocks1 = _timed(call, 10, bus)
         c1[mode] = {"ms_per_call": ms1, "us_per_step": ms1 * 10.0,

@@ -156,8 +156,17 @@ int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field*
  *                          largest exponent of T, carried from step to step), then
  *                          T' = fma(dt/2, RN(divergence), T): one FP64 operation per cell, the
  *                          rest on the integer pipe.  Within a few 2^-60 of max|T| per step of
- *                          the exact form (not bit-identical).  FP64, unit spacing. */
-enum { NEBO_HEAT_EXACT = 0, NEBO_HEAT_FIXED_POINT = 1 };
+ *                          the exact form (not bit-identical).  FP64, unit spacing.
+ *   NEBO_HEAT_FIXED_STATE  FP64 fields in and out; the run keeps T as signed 64-bit integers
+ *                          (about 60 bits below the largest |T|, rescaled as the values grow or
+ *                          decay) and (dt/2) lambda as 64-bit integers, so a step is integer
+ *                          arithmetic only: face flux = high half of (lw_a + lw_b)(T_b - T_a),
+ *                          T' = T + divergence.  Within a few 2^-60 of max|T| per step of the
+ *                          exact form; one rounding back to FP64 at the end.  Needs scratch for
+ *                          one FP64 field (the lambda weights).  FP64, unit spacing.
+ * Both non-exact modes run the exact form (bit-identical) when T or lam holds an infinity or a
+ * NaN, or when the scales leave the ranges the integer forms cover. */
+enum { NEBO_HEAT_EXACT = 0, NEBO_HEAT_FIXED_POINT = 1, NEBO_HEAT_FIXED_STATE = 2 };
 int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
                      double dt, const double spacing[3], int mode, nebo_stream_t stream);
 

@@ -281,12 +281,13 @@ def heat_run(T, Ttmp, lam, steps, dt, spacing=(1.0, 1.0, 1.0), use_graph=True, s
                                int(use_graph), _stream(stream)))
 
 
-HEAT_MODES = {"exact": 0, "fixed": 1}  # NEBO_HEAT_EXACT, NEBO_HEAT_FIXED_POINT
+HEAT_MODES = {"exact": 0, "fixed": 1, "fixed_state": 2}  # NEBO_HEAT_EXACT, _FIXED_POINT, _FIXED_STATE
 
 
 def heat_run_ex(T, Ttmp, lam, steps, dt, mode="fixed", spacing=(1.0, 1.0, 1.0), stream=None):
     """nebo_heat_run_ex: `steps` FP64 Euler steps, the result in T; mode "fixed" computes the fluxes
-    on the integer pipe (within a few 2^-60 of max|T| per step of the exact form)."""
+    on the integer pipe, "fixed_state" keeps the whole run's state in 64-bit integers (both within
+    a few 2^-60 of max|T| per step of the exact form)."""
     a, b, c = T.desc(), Ttmp.desc(), lam.desc()
     sp = (ctypes.c_double * 3)(*spacing)
     _check(lib().nebo_heat_run_ex(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt), sp,

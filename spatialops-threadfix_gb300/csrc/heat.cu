@@ -633,6 +633,305 @@ __global__ void __launch_bounds__(BX* BY) heat_step_fix_kernel(const double* __r
   if ((tx & 31) == 0) atomicMax(eOut, emax);
 }
 
+// ------------------------------------------------------------------ FP64 heat, fixed-point state
+// NEBO_HEAT_FIXED_STATE: a run converts T once into signed 64-bit integers in units of 2^U and
+// lambda once into integers of (dt/2) lambda in units of 2^(k-64); every step then works on
+// integers only,
+//   F  = hi64((lw_a + lw_b)(T_b - T_a))            (units 2^(U+k): the 128-bit product's high half)
+//   T' = (T + (((Fx+ - Fx-) + (Fy+ - Fy-)) + (Fz+ - Fz-)) 2^k) 2^-s,
+// and the last state goes back to doubles (one rounding).  No value is converted inside the time
+// loop and the FP64 pipe is idle.  Both cells of a face form its flux with the same operations,
+// so between rescalings the steps conserve the integer sum of T exactly, and the truncations of
+// the high halves (toward -inf) cancel in expectation between a cell's two faces per axis.
+// Bounds: with L = 2^(EL-1022) > max|lambda| and g = 1 + 24 |dt/2| L < 2^G, a state with
+// |T| <= 2^b gives |T + divergence| < 2^(b+G).  Each launch ORs the ones' complements of the
+// values it writes (|v| - 1 for v < 0: |v| <= 2^b for the OR's bit length b) into a device
+// word; the next launch rescales what it writes by s = b + G - B (B = 63 - G; rounded to nearest
+// when s > 0, exact when s < 0), so every state stays within 2^B, every sum inside 64 bits, and a
+// state that neither grows nor decays settles at B - G bits (about 57) with s = 0.  U += s.  k is
+// the smallest k >= 0 with |dt/2| L 2^(64-k) <= 2^61, so a sum of two lambda weights stays below
+// 2^62; lambda >= 0 (checked), so that sum is unsigned and each face takes one unsigned high
+// product and one sign correction for T_b - T_a.
+// Error: a truncation (less than 2^(U+k) per face) and a rescaling (half a unit) per step, a few
+// 2^-56 of max|T| at most, well inside 1e-13 relative; the final conversion rounds once.  A field
+// with an infinity or a NaN, a negative lambda, exponents outside +-900, or a growth bound g
+// above 2^20 runs the exact FP64 form on the same buffers (bit-identical to nebo_heat_run).
+struct FxState {
+  int eT, eL;                // largest biased exponents of T's and lambda's windows
+  int negL;                  // some lambda < 0
+  int plain, G, k;           // plain: the exact FP64 form; G, k as above (B = 63 - G)
+  int U[3];                  // state j counts units of 2^U[j % 3]
+  unsigned long long M[3];   // OR of the magnitudes of state j (the bit length of the largest)
+};
+
+// ceil(log2 v) for v > 0 (exact: frexp is exact)
+__device__ __forceinline__ int ceil_log2(double v) {
+  int e;
+  const double m = frexp(v, &e);  // v = m 2^e, m in [0.5, 1)
+  return m == 0.5 ? e - 1 : e;
+}
+
+__global__ void fxs_setup_kernel(FxState* c, double w) {
+  const int eT = c->eT, eL = c->eL;
+  const double aw = fabs(w);
+  const double wl = aw * ldexp(1.0, (eL ? eL : 1) - 1022);  // > max |w lambda|
+  const int G = ceil_log2(1.0 + 24.0 * wl);
+  const int k = wl > 0.0 ? max(0, ceil_log2(wl) + 3) : 0;
+  const int u = (eT ? eT : 1) - 1022;
+  c->plain = eT >= 2047 || eL >= 2047 || c->negL || !(aw < INFINITY) || u > 900 || u < -900 || G > 20 || k > 40;
+  c->G = G;
+  c->k = k;
+  c->U[0] = u - (63 - G);  // |T| < 2^u: state 0 has at most B bits
+  c->M[0] = c->M[1] = c->M[2] = 0ull;
+}
+
+// largest biased exponent of lambda -> atomicMax(c->eL); any lambda < 0 -> c->negL = 1
+__global__ void fxs_lambda_scan_kernel(const double* __restrict__ f, long n, FxState* __restrict__ c) {
+  int m = 0, neg = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = f[i];
+    m = max(m, (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff));
+    neg |= v < 0.0;
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  neg = __reduce_or_sync(0xffffffffu, neg);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&c->eL, m);
+    if (neg) atomicOr(&c->negL, 1);
+  }
+}
+
+__device__ __forceinline__ unsigned long long or_warp64(unsigned long long v) {
+  const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)v);
+  const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(v >> 32));
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// state 0 and the lambda weights (every cell of the windows, ghosts included)
+__global__ void fxs_convert_kernel(const double* __restrict__ t, long long* __restrict__ tfix,
+                                   const double* __restrict__ lam, long long* __restrict__ lw, long n,
+                                   FxState* __restrict__ c, double w) {
+  const bool plain = c->plain;
+  const int U = c->U[0], k = c->k;
+  unsigned long long m = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double tv = t[i], lv = lam[i];
+    if (plain) {
+      tfix[i] = __double_as_longlong(tv);
+      lw[i] = __double_as_longlong(lv);
+    } else {
+      const long long a = __double2ll_rn(ldexp(tv, -U));
+      tfix[i] = a;
+      lw[i] = __double2ll_rn(ldexp(w * lv, 64 - k));
+      m |= (unsigned long long)(a ^ (a >> 63));
+    }
+  }
+  m = or_warp64(m);
+  if ((threadIdx.x & 31) == 0 && m) atomicOr(&c->M[0], m);
+}
+
+__global__ void fxs_finish_kernel(const long long* __restrict__ tfix, double* __restrict__ t, long n,
+                                  const FxState* __restrict__ c, int slot) {
+  const bool plain = c->plain;
+  const int U = c->U[slot];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long long v = tfix[i];
+    t[i] = plain ? __longlong_as_double(v) : ldexp(__ll2double_rn(v), U);
+  }
+}
+
+// One step on a 32 x 8 tile marching z, staged like heat_step_fix_kernel (the tile and its x / y
+// halo in shared memory, two buffers, one barrier per plane; z faces in registers), with the
+// global loads one plane ahead: iteration z stages plane z (loaded in iteration z-1) and loads the
+// halo of plane z+1 and the cell of plane z+2.
+// KIND 0: the doubles' bits, exact FP64 form; 1: integers; 2: integers, output rescaled by 2^-s.
+typedef long long FxPlane[BY + 2][BX + 2];
+
+template <int KIND>
+__device__ __forceinline__ void fxs_step(const long long* __restrict__ tin, long long* __restrict__ tout,
+                                         const long long* __restrict__ lw, int sy, long sz, int nx, int ny, int nz,
+                                         int zchunk, int s, int k, double hdt, FxPlane* cT, FxPlane* cL,
+                                         unsigned long long& mag) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+  const int x = x0 + tx, y = y0 + ty;
+  const int z0 = blockIdx.z * zchunk;
+  const int z1 = min(z0 + zchunk, nz);
+  const bool active = x < nx && y < ny;
+  const int xc = min(x, nx), yc = min(y, ny);
+  auto at = [&](int i, int j, int kk) { return (long)i + (long)sy * j + sz * kk; };
+  auto asd = [](long long b) { return __longlong_as_double(b); };
+  auto flux = [&](long long la, long long lb, long long ta, long long tb) -> long long {
+    if (KIND == 0) return __double_as_longlong(__dmul_rn(__dadd_rn(asd(la), asd(lb)), __dsub_rn(asd(tb), asd(ta))));
+    const unsigned long long kap = (unsigned long long)(la + lb);  // < 2^62, lambda >= 0
+    const long long d = tb - ta;
+    return (long long)(__umul64hi(kap, (unsigned long long)d) - (d < 0 ? kap : 0ull));
+  };
+  // halo staging as in heat_step_fix_kernel: warp 0 the row below, warp 1 the row above, lanes
+  // 0..15 of warp 2 the columns x0 - 1 and x0 + 32 (coordinates clamped into the window)
+  bool has_halo = false;
+  int hx = 0, hy = 0, hsx = 0, hsy = 0;
+  if (ty == 0) {
+    has_halo = true;
+    hx = xc;
+    hy = y0 - 1;
+    hsx = tx + 1;
+  } else if (ty == 1) {
+    has_halo = true;
+    hx = xc;
+    hy = min(y0 + BY, ny);
+    hsx = tx + 1;
+    hsy = BY + 1;
+  } else if (ty == 2 && tx < 2 * BY) {
+    has_halo = true;
+    const int r = tx % BY;
+    hx = tx < BY ? x0 - 1 : min(x0 + BX, nx);
+    hy = min(y0 + r, ny);
+    hsx = tx < BY ? 0 : BX + 1;
+    hsy = r + 1;
+  }
+  const long c0 = at(xc, yc, z0), h0 = at(hx, hy, z0);
+  long long tc = __ldg(tin + c0), lc = __ldg(lw + c0);
+  long long fzlo = flux(__ldg(lw + c0 - sz), lc, __ldg(tin + c0 - sz), tc);
+  long long tn = __ldg(tin + c0 + sz), ln = __ldg(lw + c0 + sz);  // plane z0 + 1 (z0 + 1 <= nz)
+  long long ht = 0, hl = 0;
+  if (has_halo) {
+    ht = __ldg(tin + h0);
+    hl = __ldg(lw + h0);
+  }
+  for (int z = z0; z < z1; ++z) {
+    const int buf = z & 1;
+    const long dz = (long)(z - z0) * sz;
+    cT[buf][ty + 1][tx + 1] = tc;
+    cL[buf][ty + 1][tx + 1] = lc;
+    if (has_halo) {
+      cT[buf][hsy][hsx] = ht;
+      cL[buf][hsy][hsx] = hl;
+    }
+    // the loads of the next iteration: the halo of plane z+1 (<= nz) and the cell of plane
+    // z+2 (clamped to the ghost plane nz; the clamped value is never used)
+    const long n2 = c0 + dz + (z + 2 <= nz ? 2 : 1) * sz;
+    const long long tn2 = __ldg(tin + n2), ln2 = __ldg(lw + n2);
+    long long ht2 = 0, hl2 = 0;
+    if (has_halo) {
+      ht2 = __ldg(tin + h0 + dz + sz);
+      hl2 = __ldg(lw + h0 + dz + sz);
+    }
+    __syncthreads();
+    const long long fzhi = flux(lc, ln, tc, tn);
+    if (active) {
+      const long long tw = cT[buf][ty + 1][tx], te = cT[buf][ty + 1][tx + 2];
+      const long long ts = cT[buf][ty][tx + 1], tnn = cT[buf][ty + 2][tx + 1];
+      const long long lwe = cL[buf][ty + 1][tx], le = cL[buf][ty + 1][tx + 2];
+      const long long ls = cL[buf][ty][tx + 1], lnn = cL[buf][ty + 2][tx + 1];
+      const long long fx = flux(lwe, lc, tw, tc), fxhi = flux(lc, le, tc, te);
+      const long long fy = flux(ls, lc, ts, tc), fyhi = flux(lc, lnn, tc, tnn);
+      long long v;
+      if (KIND == 0) {
+        const double sum = __dadd_rn(__dadd_rn(__dsub_rn(asd(fxhi), asd(fx)), __dsub_rn(asd(fyhi), asd(fy))),
+                                     __dsub_rn(asd(fzhi), asd(fzlo)));
+        v = __double_as_longlong(__dadd_rn(asd(tc), __dmul_rn(hdt, sum)));
+      } else {
+        const long long S = ((fxhi - fx) + (fyhi - fy)) + (fzhi - fzlo);
+        v = tc + (long long)((unsigned long long)S << k);
+        if (KIND == 2) v = s > 0 ? (v >> s) + ((v >> (s - 1)) & 1) : (long long)((unsigned long long)v << -s);
+        mag |= (unsigned long long)(v ^ (v >> 63));
+      }
+      store_with_images(tout, sy, sz, x, y, z, nx, ny, nz, v);
+    }
+    fzlo = fzhi;
+    tc = tn;
+    lc = ln;
+    tn = tn2;
+    ln = ln2;
+    ht = ht2;
+    hl = hl2;
+  }
+}
+
+__global__ void __launch_bounds__(BX* BY) heat_step_fxs_kernel(const long long* __restrict__ tin,
+                                                              long long* __restrict__ tout,
+                                                              const long long* __restrict__ lw, int sy, long sz,
+                                                              int nx, int ny, int nz, int zchunk,
+                                                              FxState* __restrict__ c, int j, double hdt) {
+  __shared__ long long cT[2][BY + 2][BX + 2];
+  __shared__ long long cL[2][BY + 2][BX + 2];
+  const int slot = j % 3;
+  const bool plain = c->plain != 0;
+  const unsigned long long M = c->M[slot];
+  const int G = c->G;
+  const int s = (plain || M == 0ull) ? 0 : (64 - __clzll((long long)M)) + G - (63 - G);
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    c->U[(j + 1) % 3] = c->U[slot] + s;  // read by the next launch
+    c->M[(j + 2) % 3] = 0ull;            // the slot the previous launch read; the next one ORs into it
+  }
+  unsigned long long mag = 0;
+  if (plain)
+    fxs_step<0>(tin, tout, lw, sy, sz, nx, ny, nz, zchunk, 0, 0, hdt, cT, cL, mag);
+  else if (s == 0)
+    fxs_step<1>(tin, tout, lw, sy, sz, nx, ny, nz, zchunk, 0, c->k, hdt, cT, cL, mag);
+  else
+    fxs_step<2>(tin, tout, lw, sy, sz, nx, ny, nz, zchunk, s, c->k, hdt, cT, cL, mag);
+  if (!plain) {
+    mag = or_warp64(mag);
+    if (((threadIdx.y * BX + threadIdx.x) & 31) == 0 && mag) atomicOr(&c->M[(j + 1) % 3], mag);
+  }
+}
+
+// The time loop of NEBO_HEAT_FIXED_STATE (T's ghosts filled, steps >= 1): state 0 goes into Ttmp,
+// the states ping-pong between Ttmp and T (as integers), the last one is converted into T.
+int heat_run_fixed_state(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps, double dt,
+                         cudaStream_t s, const char* what) {
+  int n[3];
+  interior_extent(*T, n);
+  const long cells = (long)T->glob[0] * T->glob[1] * T->glob[2];
+  FxState* c = nullptr;
+  long long* lw = nullptr;
+  pool_retain();
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&c, sizeof(FxState), s));
+  cudaError_t err = cudaMallocAsync((void**)&lw, (size_t)cells * sizeof(long long), s);
+  if (err != cudaSuccess) {
+    cudaFreeAsync(c, s);
+    return cuda_fail(err, what);
+  }
+  const double w = 0.5 * dt;
+  const int rblocks = num_sms() * 4;
+  err = cudaMemsetAsync(c, 0, sizeof(FxState), s);
+  if (err == cudaSuccess) {
+    LaunchScope ls("heat_fixed_state_in", s);
+    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)T->data, cells, &c->eT);
+    fxs_lambda_scan_kernel<<<rblocks, 256, 0, s>>>((const double*)lam->data, cells, c);
+    fxs_setup_kernel<<<1, 1, 0, s>>>(c, w);
+    fxs_convert_kernel<<<rblocks, 256, 0, s>>>((const double*)T->data, (long long*)Ttmp->data,
+                                               (const double*)lam->data, lw, cells, c, w);
+    err = cudaGetLastError();
+  }
+  const View<long long> va = make_view<long long>(*Ttmp), vb = make_view<long long>(*T);
+  const long long* lwb = lw + (va.base - (long long*)Ttmp->data);  // lambda weights, same layout
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  static std::atomic<int> per_sm{0};
+  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * blocks_per_sm(heat_step_fxs_kernel, BX * BY, per_sm),
+                                 n[2], 1, 8, 1);
+  const dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
+  long long* buf[2] = {va.base, vb.base};
+  for (int j = 0; j < steps && err == cudaSuccess; ++j) {
+    LaunchScope ls("heat_step_fixed_state", s);
+    heat_step_fxs_kernel<<<grid, block, 0, s>>>(buf[j & 1], buf[(j + 1) & 1], lwb, va.sy, va.sz, n[0], n[1], n[2],
+                                                zchunk, c, j, w);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) {
+    LaunchScope ls("heat_fixed_state_out", s);
+    const long long* last = (steps & 1) ? (const long long*)T->data : (const long long*)Ttmp->data;
+    fxs_finish_kernel<<<rblocks, 256, 0, s>>>(last, (double*)T->data, cells, c, steps % 3);
+    err = cudaGetLastError();
+  }
+  cudaFreeAsync(lw, s);
+  cudaFreeAsync(c, s);
+  if (err != cudaSuccess) return cuda_fail(err, what);
+  return NEBO_OK;
+}
+
 // ------------------------------------------------------------------ FP32 step on bulk-copied slabs
 // The FP32 fields' rows are full-width slabs in HBM: rows y0-1 .. y0+8 of a plane (10 x gx floats)
 // are one contiguous run that starts on an even row, so with an even row pitch it is 16-byte
@@ -910,7 +1209,8 @@ extern "C" int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, con
                                 double dt, const double spacing[3], int mode, nebo_stream_t stream) {
   const char* what = "nebo_heat_run_ex";
   if (mode == NEBO_HEAT_EXACT) return nebo_heat_run(T, Ttmp, lam, steps, dt, spacing, 0, stream);
-  if (mode != NEBO_HEAT_FIXED_POINT) return fail(NEBO_ERR_INVALID, "Nebo error in %s: mode %d", what, mode);
+  if (mode != NEBO_HEAT_FIXED_POINT && mode != NEBO_HEAT_FIXED_STATE)
+    return fail(NEBO_ERR_INVALID, "Nebo error in %s: mode %d", what, mode);
   int rc = check_heat(T, Ttmp, lam, what);
   if (rc) return rc;
   if (T->dtype != NEBO_F64) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: fixed point is FP64 only", what);
@@ -920,6 +1220,7 @@ extern "C" int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, con
   cudaStream_t s = (cudaStream_t)stream;
   if ((rc = fill_periodic_any(T, s))) return rc;
   if (steps == 0) return NEBO_OK;
+  if (mode == NEBO_HEAT_FIXED_STATE) return heat_run_fixed_state(T, Ttmp, lam, steps, dt, s, what);
   int n[3];
   interior_extent(*T, n);
   const size_t cells = (size_t)T->glob[0] * T->glob[1] * T->glob[2];

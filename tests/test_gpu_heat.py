@@ -142,3 +142,60 @@ def test_heat_fixed_point_falls_back_to_fp64_on_non_finite_values():
     a = _run_ex(lam, T0, steps, dt, "fixed")
     b = _run_ex(lam, T0, steps, dt, "exact")
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+# ----------------------------------------------------------------- fixed-point state FP64 mode
+@pytest.mark.parametrize("n,steps,cfl", [((64, 64, 64), 100, None), ((37, 21, 19), 10, None),
+                                         ((24, 20, 16), 50, None), ((2, 8, 5), 3, None),
+                                         ((24, 20, 16), 200, 0.1)])
+def test_heat_fixed_state_vs_oracle(n, steps, cfl):
+    """NEBO_HEAT_FIXED_STATE against the oracle's serial walk: the configuration's step (values
+    grow x1.4 per step in the checkerboard mode, so the state is rescaled down) and a stable step
+    (values decay, rescaled up); within 1e-13 relative max-norm, ghost images included."""
+    kw = {} if cfl is None else {"cfl": cfl}
+    lam, T0, dt = W.heat_inputs(n, sigma=min(n) / 4.0, **kw)
+    ref = O.heat_run(lam, T0, n, steps, dt)
+    got = _run_ex(lam, T0, steps, dt, "fixed_state")
+    err = float(np.abs(got - ref).max() / np.abs(ref).max())
+    print(f"fixed-state heat {n} x {steps}: rel max-norm err {err:.2e}")
+    assert err <= 1e-13, err
+
+
+def test_heat_fixed_state_256_against_exact_kernel():
+    n, steps = (256, 256, 256), 20
+    lam, T0, dt = W.heat_inputs(n)
+    a = _run_ex(lam, T0, steps, dt, "fixed_state")
+    b = _run_ex(lam, T0, steps, dt, "exact")
+    err = float(np.abs(a - b).max() / np.abs(b).max())
+    print(f"fixed-state heat 256^3 x {steps}: rel max-norm err vs the exact form {err:.2e}")
+    assert err <= 1e-13, err
+
+
+@pytest.mark.parametrize("where", ["T", "lam", "negative_lam"])
+def test_heat_fixed_state_falls_back_to_fp64(where):
+    """An infinity or a NaN in T or lambda, or a negative lambda (the integer form takes the lambda
+    sums unsigned): the exact FP64 form runs on the integer buffers, bit for bit."""
+    n, steps = (20, 16, 12), 5
+    lam, T0, dt = W.heat_inputs(n)
+    T0, lam = T0.copy(), lam.copy()
+    if where == "T":
+        T0[5, 6, 7] = np.nan
+    elif where == "lam":
+        lam[3, 4, 5] = np.inf
+    else:
+        lam[3, 4, 5] = -0.75
+    a = _run_ex(lam, T0, steps, dt, "fixed_state")
+    b = _run_ex(lam, T0, steps, dt, "exact")
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_heat_fixed_state_zero_steps_and_zero_field():
+    n = (12, 10, 8)
+    lam, T0, dt = W.heat_inputs(n)
+    # zero steps: T keeps its values, ghosts filled (as the other modes)
+    a = _run_ex(lam, T0, 0, dt, "fixed_state")
+    b = _run_ex(lam, T0, 0, dt, "exact")
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    # an all-zero T stays zero
+    z = _run_ex(lam, np.zeros_like(T0), 4, dt, "fixed_state")
+    assert not z.any()
