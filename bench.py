@@ -626,10 +626,10 @@ def part_heat(N, bus, peak):
     Tt64 = N.Field("SVol", (64, 64, 64), 1)
     L64 = N.Field.from_numpy("SVol", lam64, 1)
     c1 = {"workload": "heat 64^3 + 1 ghost, 100 FP64 Euler steps per call, dt = 0.15 / max lambda",
-          "steps_per_call": 100}
+          "steps_per_call": 100, "launches": "one CUDA graph per call (captured once) in every mode"}
     for mode in ("exact", "fixed", "fixed_state"):
         call = (lambda k: [N.heat_run(T64, Tt64, L64, 100, dt64) for _ in range(k)]) if mode == "exact" else \
-            (lambda k, m=mode: [N.heat_run_ex(T64, Tt64, L64, 100, dt64, mode=m) for _ in range(k)])
+            (lambda k, m=mode: [N.heat_run_ex(T64, Tt64, L64, 100, dt64, mode=m, use_graph=True) for _ in range(k)])
         call(2)
         ms1, clocks1 = _timed(call, 10, bus)
         c1[mode] = {"ms_per_call": ms1, "us_per_step": ms1 * 10.0,

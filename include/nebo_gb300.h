@@ -167,6 +167,10 @@ int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field*
  * Both non-exact modes run the exact form (bit-identical) when T or lam holds an infinity or a
  * NaN, or when the scales leave the ranges the integer forms cover. */
 enum { NEBO_HEAT_EXACT = 0, NEBO_HEAT_FIXED_POINT = 1, NEBO_HEAT_FIXED_STATE = 2 };
+/* OR'd into mode: capture the call's launches (conversions and steps) in a CUDA graph the first
+ * time and replay it for the same arguments, as nebo_heat_run's use_graph does (for small grids,
+ * where launches bound the steps; the graph keeps its scratch in the stream-ordered pool). */
+enum { NEBO_HEAT_GRAPH = 0x100 };
 int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
                      double dt, const double spacing[3], int mode, nebo_stream_t stream);
 

@@ -282,16 +282,18 @@ def heat_run(T, Ttmp, lam, steps, dt, spacing=(1.0, 1.0, 1.0), use_graph=True, s
 
 
 HEAT_MODES = {"exact": 0, "fixed": 1, "fixed_state": 2}  # NEBO_HEAT_EXACT, _FIXED_POINT, _FIXED_STATE
+HEAT_GRAPH = 0x100  # NEBO_HEAT_GRAPH
 
 
-def heat_run_ex(T, Ttmp, lam, steps, dt, mode="fixed", spacing=(1.0, 1.0, 1.0), stream=None):
+def heat_run_ex(T, Ttmp, lam, steps, dt, mode="fixed", spacing=(1.0, 1.0, 1.0), stream=None, use_graph=False):
     """nebo_heat_run_ex: `steps` FP64 Euler steps, the result in T; mode "fixed" computes the fluxes
     on the integer pipe, "fixed_state" keeps the whole run's state in 64-bit integers (both within
-    a few 2^-60 of max|T| per step of the exact form)."""
+    a few 2^-60 of max|T| per step of the exact form); use_graph captures the call in a CUDA graph
+    once and replays it for the same arguments."""
     a, b, c = T.desc(), Ttmp.desc(), lam.desc()
     sp = (ctypes.c_double * 3)(*spacing)
     _check(lib().nebo_heat_run_ex(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), int(steps), float(dt), sp,
-                                  HEAT_MODES[mode], _stream(stream)))
+                                  HEAT_MODES[mode] | (HEAT_GRAPH if use_graph else 0), _stream(stream)))
 
 
 def deep_chain(a, b, c, words, out, filt, dx=1.0, stream=None, reductions=None, interior=False):

@@ -911,7 +911,7 @@ int heat_run_fixed_state(const nebo_field* T, const nebo_field* Ttmp, const nebo
   const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
   static std::atomic<int> per_sm{0};
   const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * blocks_per_sm(heat_step_fxs_kernel, BX * BY, per_sm),
-                                 n[2], 1, 8, 1);
+                                 n[2], 2, 4, 1);
   const dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
   long long* buf[2] = {va.base, vb.base};
   for (int j = 0; j < steps && err == cudaSuccess; ++j) {
@@ -1096,7 +1096,7 @@ int launch_heat(const nebo_field* Tf, const nebo_field* Tof, const nebo_field* L
     static std::atomic<int> per_sm[2];  // zero: not queried
     const int bps = unit ? blocks_per_sm(heat_step_kernel<double, ExactD, MODE_UNIT>, BX * BY, per_sm[1])
                          : blocks_per_sm(heat_step_kernel<double, ExactD, MODE_REFERENCE>, BX * BY, per_sm[0]);
-    const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 8, 1);
+    const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * bps, n[2], 1, 4, 1);
     dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
     LaunchScope ls("heat_step_f64", s);
     if (unit)
@@ -1163,18 +1163,91 @@ int heat_step_any(const nebo_field* T, const nebo_field* To, const nebo_field* L
   return T->dtype == NEBO_F64 ? launch_heat<double>(T, To, L, dt, sp, s) : launch_heat<float>(T, To, L, dt, sp, s);
 }
 
-// CUDA-graph cache for nebo_heat_run: one instantiated graph per argument set.
+// CUDA-graph cache for nebo_heat_run and nebo_heat_run_ex: one instantiated graph per argument set
+// (mode -1: nebo_heat_run's steps).
 struct GraphKey {
   void *t, *t2, *l;
-  int glob[3], dtype, steps;
+  int glob[3], dtype, steps, mode;
   double dt, sp[3];
   bool operator<(const GraphKey& o) const {
-    return std::tie(t, t2, l, glob[0], glob[1], glob[2], dtype, steps, dt, sp[0], sp[1], sp[2]) <
-           std::tie(o.t, o.t2, o.l, o.glob[0], o.glob[1], o.glob[2], o.dtype, o.steps, o.dt, o.sp[0], o.sp[1], o.sp[2]);
+    return std::tie(t, t2, l, glob[0], glob[1], glob[2], dtype, steps, mode, dt, sp[0], sp[1], sp[2]) <
+           std::tie(o.t, o.t2, o.l, o.glob[0], o.glob[1], o.glob[2], o.dtype, o.steps, o.mode, o.dt, o.sp[0],
+                    o.sp[1], o.sp[2]);
   }
 };
 std::mutex g_graph_mu;
 std::map<GraphKey, cudaGraphExec_t> g_graphs;
+
+// Launch the graph cached for key on s, capturing body(capture stream) into it the first time.
+template <class Body>
+int graph_launch(const GraphKey& key, Body body, cudaStream_t s, const char* what) {
+  cudaGraphExec_t exec = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    auto it = g_graphs.find(key);
+    if (it != g_graphs.end()) exec = it->second;
+  }
+  if (!exec) {
+    cudaStream_t cap;
+    NEBO_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    NEBO_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    const int rc = body(cap);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    g_graphs[key] = exec;
+  }
+  NEBO_CUDA_TRY(cudaGraphLaunch(exec, s));
+  return NEBO_OK;
+}
+
+// The time loop of NEBO_HEAT_FIXED_POINT (T's ghosts filled, steps >= 1).
+int heat_run_fixed_point(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps, double dt,
+                         cudaStream_t s, const char* what) {
+  int n[3];
+  interior_extent(*T, n);
+  const size_t cells = (size_t)T->glob[0] * T->glob[1] * T->glob[2];
+  int* e = nullptr;  // [0], [1]: T's exponents, ping-pong; [2]: lambda's
+  NEBO_CUDA_TRY(cudaMallocAsync((void**)&e, 3 * sizeof(int), s));
+  cudaError_t err = cudaMemsetAsync(e, 0, 3 * sizeof(int), s);
+  const int rblocks = num_sms() * 4;
+  {
+    LaunchScope ls("max_exponent", s);
+    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)T->data, (long)cells, e);
+    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)lam->data, (long)cells, e + 2);
+  }
+  if (err == cudaSuccess) err = cudaGetLastError();
+  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
+  static std::atomic<int> per_sm{0};
+  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * blocks_per_sm(heat_step_fix_kernel, BX * BY, per_sm),
+                                 n[2], 2, 4, 1);
+  const dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
+  for (int k = 0; k < steps && err == cudaSuccess; ++k) {
+    const nebo_field* a = (k & 1) ? Ttmp : T;
+    const nebo_field* b = (k & 1) ? T : Ttmp;
+    const View<double> va = make_view<double>(*a), vb = make_view<double>(*b), vl = make_view<double>(*lam);
+    err = cudaMemsetAsync(e + ((k + 1) & 1), 0, sizeof(int), s);
+    if (err != cudaSuccess) break;
+    LaunchScope ls("heat_step_fix", s);
+    heat_step_fix_kernel<<<grid, block, 0, s>>>(va.base, vb.base, vl.base, va.sy, va.sz, n[0], n[1], n[2], zchunk,
+                                                e + (k & 1), e + 2, e + ((k + 1) & 1), 0.5 * dt);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess && (steps & 1))
+    err = cudaMemcpyAsync(T->data, Ttmp->data, cells * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  cudaFreeAsync(e, s);
+  if (err != cudaSuccess) return cuda_fail(err, what);
+  return NEBO_OK;
+}
 
 }  // namespace
 
@@ -1208,7 +1281,9 @@ extern "C" int nebo_heat_step(const nebo_field* T, const nebo_field* Tout, const
 extern "C" int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps,
                                 double dt, const double spacing[3], int mode, nebo_stream_t stream) {
   const char* what = "nebo_heat_run_ex";
-  if (mode == NEBO_HEAT_EXACT) return nebo_heat_run(T, Ttmp, lam, steps, dt, spacing, 0, stream);
+  const bool graph = (mode & NEBO_HEAT_GRAPH) != 0;
+  mode &= ~NEBO_HEAT_GRAPH;
+  if (mode == NEBO_HEAT_EXACT) return nebo_heat_run(T, Ttmp, lam, steps, dt, spacing, graph ? 1 : 0, stream);
   if (mode != NEBO_HEAT_FIXED_POINT && mode != NEBO_HEAT_FIXED_STATE)
     return fail(NEBO_ERR_INVALID, "Nebo error in %s: mode %d", what, mode);
   int rc = check_heat(T, Ttmp, lam, what);
@@ -1220,42 +1295,15 @@ extern "C" int nebo_heat_run_ex(const nebo_field* T, const nebo_field* Ttmp, con
   cudaStream_t s = (cudaStream_t)stream;
   if ((rc = fill_periodic_any(T, s))) return rc;
   if (steps == 0) return NEBO_OK;
-  if (mode == NEBO_HEAT_FIXED_STATE) return heat_run_fixed_state(T, Ttmp, lam, steps, dt, s, what);
-  int n[3];
-  interior_extent(*T, n);
-  const size_t cells = (size_t)T->glob[0] * T->glob[1] * T->glob[2];
-  int* e = nullptr;  // [0], [1]: T's exponents, ping-pong; [2]: lambda's
   pool_retain();
-  NEBO_CUDA_TRY(cudaMallocAsync((void**)&e, 3 * sizeof(int), s));
-  cudaError_t err = cudaMemsetAsync(e, 0, 3 * sizeof(int), s);
-  const int rblocks = num_sms() * 4;
-  {
-    LaunchScope ls("max_exponent", s);
-    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)T->data, (long)cells, e);
-    max_biased_exp_kernel<<<rblocks, 256, 0, s>>>((const double*)lam->data, (long)cells, e + 2);
-  }
-  if (err == cudaSuccess) err = cudaGetLastError();
-  const int gxb = (n[0] + BX - 1) / BX, gyb = (n[1] + BY - 1) / BY;
-  static std::atomic<int> per_sm{0};
-  const int zchunk = wave_zchunk((long)gxb * gyb, (long)num_sms() * blocks_per_sm(heat_step_fix_kernel, BX * BY, per_sm),
-                                 n[2], 1, 8, 1);
-  const dim3 grid(gxb, gyb, (n[2] + zchunk - 1) / zchunk), block(BX, BY);
-  for (int k = 0; k < steps && err == cudaSuccess; ++k) {
-    const nebo_field* a = (k & 1) ? Ttmp : T;
-    const nebo_field* b = (k & 1) ? T : Ttmp;
-    const View<double> va = make_view<double>(*a), vb = make_view<double>(*b), vl = make_view<double>(*lam);
-    err = cudaMemsetAsync(e + ((k + 1) & 1), 0, sizeof(int), s);
-    if (err != cudaSuccess) break;
-    LaunchScope ls("heat_step_fix", s);
-    heat_step_fix_kernel<<<grid, block, 0, s>>>(va.base, vb.base, vl.base, va.sy, va.sz, n[0], n[1], n[2], zchunk,
-                                                e + (k & 1), e + 2, e + ((k + 1) & 1), 0.5 * dt);
-    err = cudaGetLastError();
-  }
-  if (err == cudaSuccess && (steps & 1))
-    err = cudaMemcpyAsync(T->data, Ttmp->data, cells * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  cudaFreeAsync(e, s);
-  if (err != cudaSuccess) return cuda_fail(err, what);
-  return NEBO_OK;
+  auto body = [&](cudaStream_t st) {
+    return mode == NEBO_HEAT_FIXED_STATE ? heat_run_fixed_state(T, Ttmp, lam, steps, dt, st, what)
+                                         : heat_run_fixed_point(T, Ttmp, lam, steps, dt, st, what);
+  };
+  if (!graph) return body(s);
+  GraphKey key{T->data, Ttmp->data, lam->data, {T->glob[0], T->glob[1], T->glob[2]}, T->dtype, steps, mode, dt,
+               {1.0, 1.0, 1.0}};
+  return graph_launch(key, body, s, what);
 }
 
 extern "C" int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const nebo_field* lam, int steps, double dt,
@@ -1279,41 +1327,20 @@ extern "C" int nebo_heat_run(const nebo_field* T, const nebo_field* Ttmp, const 
     if (steps & 1) NEBO_CUDA_TRY(cudaMemcpyAsync(T->data, Ttmp->data, bytes, cudaMemcpyDeviceToDevice, s));
     return NEBO_OK;
   }
-  GraphKey key{T->data, Ttmp->data, lam->data, {T->glob[0], T->glob[1], T->glob[2]}, T->dtype, steps, dt,
+  GraphKey key{T->data, Ttmp->data, lam->data, {T->glob[0], T->glob[1], T->glob[2]}, T->dtype, steps, -1, dt,
                {sp[0], sp[1], sp[2]}};
-  cudaGraphExec_t exec = nullptr;
-  {
-    std::lock_guard<std::mutex> g(g_graph_mu);
-    auto it = g_graphs.find(key);
-    if (it != g_graphs.end()) exec = it->second;
-  }
-  if (!exec) {
-    cudaStream_t cap;
-    NEBO_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    NEBO_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < steps && !rc; ++k) {
+  auto body = [&](cudaStream_t cap) {
+    int r = 0;
+    for (int k = 0; k < steps && !r; ++k) {
       const nebo_field* a = (k & 1) ? Ttmp : T;
       const nebo_field* b = (k & 1) ? T : Ttmp;
-      rc = heat_step_any(a, b, lam, dt, sp, cap);
+      r = heat_step_any(a, b, lam, dt, sp, cap);
     }
-    if (!rc && (steps & 1)) {
+    if (!r && (steps & 1)) {
       cudaError_t e = cudaMemcpyAsync(T->data, Ttmp->data, bytes, cudaMemcpyDeviceToDevice, cap);
-      if (e != cudaSuccess) rc = cuda_fail(e, "nebo_heat_run capture copy");
+      if (e != cudaSuccess) r = cuda_fail(e, "nebo_heat_run capture copy");
     }
-    cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(cap, &graph);
-    cudaStreamDestroy(cap);
-    if (rc) {
-      if (graph) cudaGraphDestroy(graph);
-      return rc;
-    }
-    if (e != cudaSuccess) return cuda_fail(e, "nebo_heat_run capture");
-    e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return cuda_fail(e, "nebo_heat_run instantiate");
-    std::lock_guard<std::mutex> g(g_graph_mu);
-    g_graphs[key] = exec;
-  }
-  NEBO_CUDA_TRY(cudaGraphLaunch(exec, s));
-  return NEBO_OK;
+    return r;
+  };
+  return graph_launch(key, body, s, "nebo_heat_run");
 }

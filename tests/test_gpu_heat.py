@@ -199,3 +199,21 @@ def test_heat_fixed_state_zero_steps_and_zero_field():
     # an all-zero T stays zero
     z = _run_ex(lam, np.zeros_like(T0), 4, dt, "fixed_state")
     assert not z.any()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fixed", "fixed_state"])
+def test_heat_run_ex_graph_equals_direct_launches(mode):
+    """NEBO_HEAT_GRAPH: the captured call (conversions, steps, scratch from the stream-ordered pool)
+    and its replay give the direct launches' bits."""
+    n, steps = (24, 20, 16), 7
+    lam, T0, dt = W.heat_inputs(n, cfl=0.15)
+
+    def run(use_graph):
+        T = N.Field.from_numpy("SVol", T0, 1)
+        Tt = N.Field.from_numpy("SVol", np.zeros_like(T0), 1)
+        L = N.Field.from_numpy("SVol", lam, 1)
+        for _ in range(2):  # capture, then replay on the evolved state
+            N.heat_run_ex(T, Tt, L, steps, dt, mode=mode, use_graph=use_graph)
+        return T.numpy()
+
+    assert np.array_equal(run(True).view(np.uint64), run(False).view(np.uint64))
