@@ -12,10 +12,14 @@
 //
 // The scatter keeps the reference's order without a serial loop:
 //   1. count  every particle adds 1 to the counter of each cell of its box (and its box size to a
-//             64-bit total);
+//             64-bit total), and is filed under the 4 x 4 x 4 block of cells its box starts in;
 //   2. scan   an exclusive prefix sum of the counters gives each cell a slice of one entry list;
+//             a prefix sum of the per-block counts and one scatter give the particles in block
+//             order;
 //   3. fill   every (particle, cell) pair writes a 16-byte entry (particle index, v * w) into a
-//             free slot of its cell's slice;
+//             free slot of its cell's slice, the particles taken in block order so that a warp's
+//             stores land in nearby slices (random particle order scatters them over the list:
+//             8.2 ms against 4.2 for 16.8 M particles on 256^3);
 //   4. fold   each window cell sorts its slice by particle index (an insertion sort: slots are
 //             taken in nearly increasing index order) and sums it from +0 in that order; a cell
 //             with no entry gets +0 (the reference's `dest <<= 0` before it adds).
@@ -191,6 +195,7 @@ struct WarpShared {
   double cont[3][PB][32];  // overlap of lane's particle with its box's t-th cell along each axis
   double pvol[32], rcp[32];
   double val[32];          // FILL: the particles' values
+  long long pid[32];       // FILL: the particles' indices (the entries' keys)
   double prod[MODE == PM_C2P ? PCAP : 1];  // C2P: products of pairs [S, S + PCAP) of the warp's list
   int lo[3][32];
   int n[3][32];
@@ -235,16 +240,19 @@ template <int MODE>
 __global__ void __launch_bounds__(PWARPS * 32, 2) particles_kernel(
     PGeom g, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
     const double* __restrict__ psize, long np, const double* __restrict__ cell, double* __restrict__ dest,
-    const double* __restrict__ src, const int* __restrict__ off, int* __restrict__ cnt, Entry* __restrict__ ent) {
+    const double* __restrict__ src, const int* __restrict__ off, int* __restrict__ cnt, Entry* __restrict__ ent,
+    const int* __restrict__ order) {
   extern __shared__ __align__(16) unsigned char particle_smem[];
   WarpShared<MODE>* smem = reinterpret_cast<WarpShared<MODE>*>(particle_smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpShared<MODE>& sm = smem[warp];
   for (long base = ((long)blockIdx.x * PWARPS + warp) * 32; base < np; base += (long)gridDim.x * PWARPS * 32) {
-    const long p = base + lane;
+    // FILL with an order: the warp's particles in that order (particles of nearby cells together,
+    // so the entries' stores land near each other); the entries keep the particles' indices
+    const long p = (MODE == PM_FILL && order && base + lane < np) ? (long)order[base + lane] : base + lane;
     int npairs = 0;
     bool big = false;
-    if (p < np) {
+    if (base + lane < np) {
       Box b;
       make_box(b, g, px, py, pz, psize, p);
       const int n0 = b.count(0), n1 = b.count(1), n2 = b.count(2);
@@ -264,7 +272,10 @@ __global__ void __launch_bounds__(PWARPS * 32, 2) particles_kernel(
         for (int t = 0; t < n0; ++t) sm.cont[0][t][lane] = axis_cont(b.a[0], g, 0, b.a[0].lo + t);
         for (int t = 0; t < n1; ++t) sm.cont[1][t][lane] = axis_cont(b.a[1], g, 1, b.a[1].lo + t);
         for (int t = 0; t < n2; ++t) sm.cont[2][t][lane] = axis_cont(b.a[2], g, 2, b.a[2].lo + t);
-        if (MODE == PM_FILL) sm.val[lane] = src[p];
+        if (MODE == PM_FILL) {
+          sm.val[lane] = src[p];
+          sm.pid[lane] = p;
+        }
       }
     }
     // exclusive prefix of the pair counts
@@ -303,7 +314,7 @@ __global__ void __launch_bounds__(PWARPS * 32, 2) particles_kernel(
         } else {
           const long cc = win_flat(g, ci, cj, ck);
           const int slot = off[cc + 1] - atomicSub(cnt + cc, 1);
-          put_entry(ent + slot, base + o, __dmul_rn(sm.val[o], w));
+          put_entry(ent + slot, sm.pid[o], __dmul_rn(sm.val[o], w));
         }
       }
       if (MODE == PM_C2P && (c0 + 32 == S + PCAP || c0 + 32 >= total_pairs)) {
@@ -321,23 +332,31 @@ __global__ void __launch_bounds__(PWARPS * 32, 2) particles_kernel(
       }
     }
     if (big) acc = serial_particle<MODE>(g, px, py, pz, psize, p, cell, src, off, cnt, ent);
-    if (MODE == PM_C2P && p < np) dest[p] = acc;
+    if (MODE == PM_C2P && base + lane < np) dest[p] = acc;
     __syncwarp();
   }
 }
 
 // Counting pass of ParticleToCell: one lane per particle adds 1 to each cell of its box.  The
-// pairs need no floating-point work here, so the lane's own loop beats spreading them.
+// pairs need no floating-point work here, so the lane's own loop beats spreading them.  It also
+// files each particle under the 4 x 4 x 4 block of cells that holds its box's first cell (key;
+// nkey for an empty box) and counts the particles per key (hist), from which the fill's order is
+// built.
 __global__ void __launch_bounds__(256) p2c_count_kernel(PGeom g, const double* __restrict__ px,
                                                         const double* __restrict__ py, const double* __restrict__ pz,
                                                         const double* __restrict__ psize, long np,
-                                                        int* __restrict__ cnt, unsigned long long* __restrict__ total) {
+                                                        int* __restrict__ cnt, unsigned long long* __restrict__ total,
+                                                        int* __restrict__ key, int* __restrict__ hist, int kbx,
+                                                        int kby, int nkey) {
   unsigned long long mine = 0;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np; p += (long)gridDim.x * blockDim.x) {
     Box b;
     make_box(b, g, px, py, pz, psize, p);
     const int n0 = b.count(0), n1 = b.count(1), n2 = b.count(2);
     mine += (unsigned long long)((long)n0 * n1 * n2);
+    const int k = (n0 && n1 && n2) ? (b.a[0].lo >> 2) + kbx * ((b.a[1].lo >> 2) + kby * (b.a[2].lo >> 2)) : nkey;
+    key[p] = k;
+    atomicAdd(hist + k, 1);
     if (!n0 || !n1 || !n2) continue;
     for (int k = b.a[2].lo; k < b.a[2].hi; ++k)
       for (int j = b.a[1].lo; j < b.a[1].hi; ++j)
@@ -345,6 +364,14 @@ __global__ void __launch_bounds__(256) p2c_count_kernel(PGeom g, const double* _
   }
   for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
   if ((threadIdx.x & 31) == 0 && mine) atomicAdd(total, mine);
+}
+
+// The fill's order: the particles grouped by key (pos: the keys' exclusive prefix, advanced as
+// the slots are taken; the order within a key does not matter, the fold sorts by index).
+__global__ void __launch_bounds__(256) p2c_order_kernel(const int* __restrict__ key, long np, int* __restrict__ pos,
+                                                        int* __restrict__ order) {
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np; p += (long)gridDim.x * blockDim.x)
+    order[atomicAdd(pos + key[p], 1)] = (int)p;
 }
 
 // Fold of ParticleToCell: a warp takes 32 consecutive window cells, whose slices form one
@@ -567,7 +594,7 @@ extern "C" int nebo_cell_to_particle(const nebo_particle_mesh* mesh, const doubl
     LaunchScope ls("cell_to_particle", s);
     particles_kernel<PM_C2P><<<particle_blocks(nparticles), PWARPS * 32, PWARPS * sizeof(WarpShared<PM_C2P>), s>>>(
         g, px, py, pz, psize, (long)nparticles, static_cast<const double*>(cell->data), dest, nullptr, nullptr,
-        nullptr, nullptr);
+        nullptr, nullptr, nullptr);
   }
   NEBO_LAUNCH_CHECK("nebo_cell_to_particle");
   return NEBO_OK;
@@ -586,14 +613,25 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: at most 2^31-1 particles", who);
   const long ncell = (long)g.nmax[0] * g.nmax[1] * g.nmax[2];
   if (ncell <= 0) return NEBO_OK;
+  if (ncell >= (1L << 31) - 1) return fail(NEBO_ERR_UNSUPPORTED, "Nebo error in %s: window above 2^31-2 cells", who);
   cudaStream_t s = (cudaStream_t)stream;
   // the scan runs over ncell + 1 counters (the last one stays 0), so off[ncell] is the total
   const long nscan = ncell + 1;
   const long ntile = (nscan + SCAN_TILE - 1) / SCAN_TILE;
-  // one allocation: counters, offsets, tile sums, grand total, 64-bit box total
+  // one allocation: counters, offsets, tile sums, grand total, 64-bit box total, then the fill's
+  // order: particles per key (a key is a box's first cell, or ncell), their prefix, each
+  // particle's key and the order
+  auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   const size_t cnt_b = (size_t)nscan * 4, off_b = (size_t)nscan * 4, bs_b = (size_t)ntile * 4;
-  const size_t cnt_o = 0, off_o = (cnt_b + 15) & ~(size_t)15, bs_o = off_o + ((off_b + 15) & ~(size_t)15);
-  const size_t gr_o = bs_o + ((bs_b + 15) & ~(size_t)15), tot_o = gr_o + 16, ws_b = tot_o + 16;
+  const size_t cnt_o = 0, off_o = up16(cnt_b), bs_o = off_o + up16(off_b);
+  const size_t gr_o = bs_o + up16(bs_b), tot_o = gr_o + 16;
+  // keys: 4 x 4 x 4 blocks of window cells
+  const int kbx = (g.nmax[0] + 3) >> 2, kby = (g.nmax[1] + 3) >> 2, kbz = (g.nmax[2] + 3) >> 2;
+  const int nkey = kbx * kby * kbz;
+  const long nkscan = (long)nkey + 1, nktile = (nkscan + SCAN_TILE - 1) / SCAN_TILE;
+  const size_t hist_b = (size_t)nkscan * 4;
+  const size_t hist_o = tot_o + 16, hpos_o = hist_o + up16(hist_b), key_o = hpos_o + up16(hist_b);
+  const size_t ord_o = key_o + up16((size_t)nparticles * 4), ws_b = ord_o + up16((size_t)nparticles * 4);
   char* ws = nullptr;
   pool_retain();
   NEBO_CUDA_TRY(cudaMallocAsync((void**)&ws, ws_b, s));
@@ -602,11 +640,16 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
   int* bsum = (int*)(ws + bs_o);
   int* grand = (int*)(ws + gr_o);
   unsigned long long* total = (unsigned long long*)(ws + tot_o);
+  int* hist = (int*)(ws + hist_o);
+  int* hpos = (int*)(ws + hpos_o);
+  int* key = (int*)(ws + key_o);
+  int* order = (int*)(ws + ord_o);
   Entry* ent = nullptr;
   unsigned long long htotal = 0;
   int rc = NEBO_OK;
   cudaError_t e = cudaMemsetAsync(cnt, 0, cnt_b, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(total, 0, 8, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, hist_b, s);
   if (e != cudaSuccess) {
     rc = cuda_fail(e, "nebo_particle_to_cell workspace");
     goto done;
@@ -615,7 +658,7 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     {
       LaunchScope ls("particle_to_cell_count", s);
       p2c_count_kernel<<<particle_blocks(nparticles, 16), 256, 0, s>>>(g, px, py, pz, psize, (long)nparticles, cnt,
-                                                                   total);
+                                                                   total, key, hist, kbx, kby, nkey);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) {
       rc = cuda_fail(e, "nebo_particle_to_cell count");
@@ -648,6 +691,19 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     goto done;
   }
   if (htotal > 0) {
+    {
+      // the fill's order: the particles grouped by key (the tile sums and total of the scan above
+      // are free again)
+      LaunchScope ls("particle_to_cell_order", s);
+      scan_tile_sums_kernel<<<(unsigned)nktile, SCAN_THREADS, 0, s>>>(hist, nkscan, bsum);
+      scan_block_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(bsum, (int)nktile, grand);
+      scan_tile_apply_kernel<<<(unsigned)nktile, SCAN_THREADS, 0, s>>>(hist, nkscan, bsum, hpos);
+      p2c_order_kernel<<<particle_blocks(nparticles, 16), 256, 0, s>>>(key, (long)nparticles, hpos, order);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+      rc = cuda_fail(e, "nebo_particle_to_cell order");
+      goto done;
+    }
     if ((e = cudaMallocAsync((void**)&ent, htotal * sizeof(Entry), s)) != cudaSuccess) {
       rc = fail(NEBO_ERR_ALLOC, "Nebo error in %s: %llu entries do not fit on the device", who, htotal);
       goto done;
@@ -655,7 +711,7 @@ extern "C" int nebo_particle_to_cell(const nebo_particle_mesh* mesh, const doubl
     {
       LaunchScope ls("particle_to_cell_fill", s);
       particles_kernel<PM_FILL><<<particle_blocks(nparticles), PWARPS * 32, PWARPS * sizeof(WarpShared<PM_FILL>), s>>>(
-          g, px, py, pz, psize, (long)nparticles, nullptr, nullptr, src, off, cnt, ent);
+          g, px, py, pz, psize, (long)nparticles, nullptr, nullptr, src, off, cnt, ent, order);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) {
       rc = cuda_fail(e, "nebo_particle_to_cell fill");
