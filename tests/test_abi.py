@@ -50,6 +50,26 @@ def test_null_descriptor_is_rejected_without_gpu():
     assert b"null field descriptor" in L.nebo_last_error()
 
 
+def _header_enum(name):
+    txt = open(os.path.join(REPO, "include", "nebo_gb300.h")).read()
+    return int(re.search(r"\b%s\s*=\s*(0x[0-9a-fA-F]+|-?\d+)" % name, txt).group(1), 0)
+
+
+def test_heat_modes_match_header():
+    assert N.HEAT_MODES == {"exact": _header_enum("NEBO_HEAT_EXACT"), "fixed": _header_enum("NEBO_HEAT_FIXED_POINT"),
+                            "fixed_state": _header_enum("NEBO_HEAT_FIXED_STATE")}
+    assert N.HEAT_GRAPH == _header_enum("NEBO_HEAT_GRAPH")
+    assert not any(v & N.HEAT_GRAPH for v in N.HEAT_MODES.values())
+
+
+@pytest.mark.parametrize("mode", [7, 7 | 0x100])
+def test_heat_run_ex_rejects_an_unknown_mode_without_gpu(mode):
+    L = N.lib()
+    rc = L.nebo_heat_run_ex(None, None, None, 1, 0.1, None, mode, None)
+    assert rc == 1
+    assert b"mode 7" in L.nebo_last_error()
+
+
 def _rand_expr(rng, fields, depth, db):
     """Random Nebo expression over SVol fields (pointwise ops, cond, same-type stencils)."""
     if depth == 0 or rng.random() < 0.2:
